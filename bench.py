@@ -1,0 +1,341 @@
+"""Benchmark: GDoF/s of the matrix-free hexahedral operator action on GB300.
+
+Workload (the benchmark configuration the headline metric is quoted on):
+stiffness action, degree P=4 (125 DOFs/cell), Q=6 Gauss points per axis,
+32768 cells, affine Jacobians J = I + 0.1 N(0,1), G = detJ w J^-1 J^-T as 6
+components per point, u ~ U(-1,1); FP64 storage and arithmetic (the plain
+FP64 path).  The same workload is also timed in FP32 and reported under
+"variants".  Inputs (405 MB in FP64) exceed the 129 MB L2, so no L2 flush is
+needed between steps.
+
+A step is one operator application over all cells.  `value` is timed with
+inputs resident in HBM; `e2e` goes through the host-buffer C-ABI entry point
+(femtc_stiffness_apply_host) with pinned host buffers, so each step includes
+the host->device copy of u and G and the device->host copy of y.
+
+--impl reference times the CPU implementation of the same operator on the
+host cores instead (the reference's algorithm restated in C, OpenMP over
+cells, FP64): that is the reference arm.
+
+Multi-GPU: cells are independent (the operator is block diagonal), so N
+ranks run N independent replicas of the workload (weak scaling, no data
+exchange); the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# FP64 FMA throughput measured on this machine's GB300 with a dependent-chain
+# FMA kernel (profiles/gb300_pipe_peaks.md); the generated peaks file
+# carries no FP64 figure.
+FP64_PEAK_TFLOPS = 1.20
+FALLBACK_HBM_GBS = 6800.0
+
+
+def flops_per_cell(op: int, n: int, q: int) -> float:
+    if op == 0:
+        return 4.0 * q * n * (n * n + q * n + q * q) + q ** 3
+    return 4.0 * q * n * (2 * n * n + 3 * q * n + 3 * q * q) + 15.0 * q ** 3
+
+
+def bytes_per_cell(op: int, n: int, q: int, es: int) -> float:
+    return es * (2 * n ** 3 + (1 if op == 0 else 6) * q ** 3)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.proc = None
+        self.index = index
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the oracle's C restatement of the reference's algorithm."""
+    if rank != 0:
+        return
+    import oracle
+    from femtc_gb300 import workloads as W
+    oracle.lib()
+    w = W.make(args.workload)
+    n, q = w.n, w.nquad
+    # bounded sample: enough cells for ~2 s per step on the host cores
+    per_cell_s = 40e-6 if w.op == 1 else 15e-6
+    cores = os.cpu_count() or 1
+    sample = int(min(w.ncells, max(256, 2.0 * cores / per_cell_s)))
+    u, g = w.u[:sample], w.geo[:sample]
+    fn = oracle.mass if w.op == 0 else oracle.stiffness
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        fn(oracle.EXACT, w.degree, q, w.tables, u, g, nthreads=cores)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            times.append(t1 - t0)
+    t = float(np.mean(times))
+    gdofs = sample * n ** 3 / t / 1e9
+    line = {
+        "metric": "GDoF/s stiffness action (P=4, Q=6)" if w.op == 1 else "GDoF/s mass action (P=3, Q=5)",
+        "value": gdofs, "unit": "GDoF/s", "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": args.workload, "cells": w.ncells, "degree": w.degree,
+                                        "nquad": q, "sample_cells": sample},
+        "cpu_baseline": {"value": gdofs, "unit": "GDoF/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} of {w.ncells} cells per step, FP64, OpenMP over cells"},
+        "e2e": {"value": gdofs, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(w, seconds=10.0):
+    """Time the oracle's C restatement on the host cores on a bounded sample."""
+    import oracle
+    oracle.lib()
+    cores = os.cpu_count() or 1
+    fn = oracle.mass if w.op == 0 else oracle.stiffness
+    sample = min(w.ncells, 2048)
+    u, g = w.u[:sample], w.geo[:sample]
+    fn(oracle.EXACT, w.degree, w.nquad, w.tables, u, g, nthreads=cores)  # warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        fn(oracle.EXACT, w.degree, w.nquad, w.tables, u, g, nthreads=cores)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or reps >= 200:
+            break
+    v = reps * sample * w.n ** 3 / el / 1e9
+    return {"value": v, "unit": "GDoF/s", "cores": cores, "kind": "port",
+            "sample": f"{reps} x {sample} cells of the workload, FP64, OpenMP over cells, {el:.1f} s"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="femtc", choices=["femtc", "reference"])
+    ap.add_argument("--workload", default="stiffness_p4",
+                    choices=["stiffness_p4", "mass_p3", "stiffness_p6"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import femtc_gb300 as F
+    from femtc_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    F.load()
+
+    w = W.make(args.workload)
+    n, q, op = w.n, w.nquad, w.op
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    def maxreduce(x):
+        if pg is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    for dtype in (F.F64, F.F32):
+        tdt = torch.float64 if dtype == F.F64 else torch.float32
+        u = torch.from_numpy(w.u).to(dev, tdt)
+        g = torch.from_numpy(w.geo).to(dev, tdt)
+        y = torch.empty_like(u)
+
+        def step():
+            F.apply(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
+
+        for _ in range(args.warmup):
+            step()
+        barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        sampler = ClockSampler(local) if dtype == F.F64 else None
+        if sampler:
+            sampler.__enter__()
+        barrier()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        t_end.record(stream)
+        barrier()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        total_ms = maxreduce(t_start.elapsed_time(t_end))
+        kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+        results[dtype] = dict(total_ms=total_ms, kern_ms=kern_ms, clocks=sampler.summary() if sampler else None)
+        if F.device_status() != 0:
+            raise RuntimeError("device fault word set during the benchmark")
+        del u, g, y
+        torch.cuda.empty_cache()
+
+    # end-to-end through the host-buffer C-ABI entry point, pinned buffers
+    e2e = {}
+    for dtype in (F.F64,):
+        npdt = np.float64 if dtype == F.F64 else np.float32
+        uh = torch.from_numpy(w.u.astype(npdt)).pin_memory()
+        gh = torch.from_numpy(w.geo.astype(npdt)).pin_memory()
+        yh = torch.empty_like(uh).pin_memory()
+
+        def estep():
+            F.apply_host(op, dtype, F.EXACT, w.degree, q, w.tables, uh, yh, gh, w.ncells)
+
+        for _ in range(args.warmup):
+            estep()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            estep()
+        barrier()
+        el = maxreduce(time.perf_counter() - t0)
+        e2e[dtype] = dict(gdofs=world * args.steps * w.ndofs / el / 1e9,
+                          h2d=uh.numel() * uh.element_size() + gh.numel() * gh.element_size(),
+                          d2h=yh.numel() * yh.element_size())
+
+    r = results[F.F64]
+    value = world * args.steps * w.ndofs / (r["total_ms"] * 1e-3) / 1e9
+    fpc = flops_per_cell(op, n, q)
+    bpc = bytes_per_cell(op, n, q, 8)
+    ach_tf = fpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e12
+    ach_gbs = bpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e9
+    hbm, hbm_src = peaks()
+    variants = {}
+    for dtype, res in results.items():
+        es = 8 if dtype == F.F64 else 4
+        variants[F.DTYPE_NAMES[dtype]] = {
+            "gdofs": world * args.steps * w.ndofs / (res["total_ms"] * 1e-3) / 1e9,
+            "kernel_ms": res["kern_ms"],
+            "hbm_gbs": bytes_per_cell(op, n, q, es) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
+            "tflops": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
+        }
+    if rank == 0:
+        line = {
+            "metric": "GDoF/s stiffness action (P=4, Q=6)" if op == 1 else "GDoF/s mass action (P=3, Q=5)",
+            "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "cells": w.ncells, "degree": w.degree, "nquad": q,
+                       "dofs": w.ndofs, "parallelism": f"replicas{world}",
+                       "l2": f"inputs {bpc * w.ncells / 1e6:.0f} MB > 129 MB L2, no flush"},
+            "roofline": {"bound": "fp64", "achieved": ach_tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                         "frac": ach_tf / FP64_PEAK_TFLOPS, "traffic": None,
+                         "peak_source": "measured FP64 FMA pipe (profiles/gb300_pipe_peaks.md)",
+                         "hbm": {"achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
+                                 "frac": ach_gbs / hbm, "peak_source": hbm_src}},
+            "e2e": {"value": e2e[F.F64]["gdofs"], "unit": "GDoF/s",
+                    "h2d_bytes_per_step": e2e[F.F64]["h2d"], "d2h_bytes_per_step": e2e[F.F64]["d2h"]},
+            "gpu_launches": 2 * args.steps + args.steps,
+            "clocks": r["clocks"],
+            "variants": variants,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(w)
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

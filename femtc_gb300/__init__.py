@@ -1,0 +1,12 @@
+"""femtc_gb300: GB300-native (sm_103a) matrix-free hexahedral operator action.
+
+The product is libfemtc_gpu.so (C ABI, include/femtc_gpu.h) with its C++
+drop-in header include/femtc_gpu/operators.hpp.  This package builds it
+in-tree and binds it with ctypes for Python callers, tests and benchmarks.
+"""
+from ._lib import (  # noqa: F401
+    BF16X3, EXACT, F16X2, F32, F64, MASS, REFERENCE, STIFFNESS, DTYPE_NAMES,
+    FemtcError, apply, apply_host, check, device_status, get_tile_config, load,
+    set_tile_config, supported, tabulate,
+)
+from .buildlib import build, lib_path  # noqa: F401

@@ -1,0 +1,3 @@
+// CUDA-core mass cell kernels, double arithmetic and storage.
+#include "cell_inst.cuh"
+FEMTC_CELL_UNIT(register_cell_f64_mass, double, 0, OP_MASS)

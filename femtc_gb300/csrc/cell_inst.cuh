@@ -1,0 +1,68 @@
+// Instantiates the CUDA-core cell kernels of one (element type, operator)
+// for every supported (N, Q, semantics) and registers them.
+//   exact semantics     : N = 2..8 (degree 1..7), Q = N, N+1, N+2 (Q <= 10)
+//   reference semantics : Q = N (the reference's only option)
+#pragma once
+
+#include "cell_kernel.cuh"
+#include "registry.hpp"
+
+namespace femtc
+{
+template <typename T, int N, int Q, int OP, int SEM>
+unsigned cell_smem_bytes(int cb, int staged)
+{
+  return make_layout<N, Q, OP, SEM, T>(cb, staged).total;
+}
+
+template <typename T, int N, int Q, int OP, int SEM>
+void add_variant(std::vector<CellVariant>& v, int dtype)
+{
+  v.push_back(CellVariant{dtype, OP, SEM, N, Q,
+                          reinterpret_cast<const void*>(
+                              &cell_kernel<T, N, Q, OP, SEM>),
+                          &cell_smem_bytes<T, N, Q, OP, SEM>});
+}
+
+template <typename T, int OP, int N>
+void add_degree(std::vector<CellVariant>& v, int dtype)
+{
+  add_variant<T, N, N, OP, SEM_EXACT>(v, dtype);
+  add_variant<T, N, N + 1, OP, SEM_EXACT>(v, dtype);
+  if constexpr (N + 2 <= kMaxQ)
+    add_variant<T, N, N + 2, OP, SEM_EXACT>(v, dtype);
+  add_variant<T, N, N, OP, SEM_REFERENCE>(v, dtype);
+}
+
+template <typename T, int OP>
+void add_all(std::vector<CellVariant>& v, int dtype)
+{
+  add_degree<T, OP, 2>(v, dtype);
+  add_degree<T, OP, 3>(v, dtype);
+  add_degree<T, OP, 4>(v, dtype);
+  add_degree<T, OP, 5>(v, dtype);
+  add_degree<T, OP, 6>(v, dtype);
+  add_degree<T, OP, 7>(v, dtype);
+  add_degree<T, OP, 8>(v, dtype);
+}
+
+inline unsigned read_clear_fault_word()
+{
+  unsigned w = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&w, g_fault_word, sizeof(w)) != cudaSuccess)
+    return 0;
+  if (w)
+    cudaMemcpyToSymbol(g_fault_word, &z, sizeof(z));
+  return w;
+}
+} // namespace femtc
+
+#define FEMTC_CELL_UNIT(NAME, T, DTYPE, OP)                                    \
+  namespace femtc                                                              \
+  {                                                                            \
+  void NAME(std::vector<CellVariant>& v, std::vector<FaultReader>& f)          \
+  {                                                                            \
+    add_all<T, OP>(v, DTYPE);                                                  \
+    f.push_back(&read_clear_fault_word);                                       \
+  }                                                                            \
+  }

@@ -1,0 +1,122 @@
+// Shared device helpers for the femtc GB300 kernels: bulk-copy (TMA) and
+// mbarrier wrappers in inline PTX, the bounded wait, and the device fault
+// word that a timed-out wait sets instead of hanging.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace femtc
+{
+
+// Fault bits recorded by kernels (read back by femtc_device_status()).
+enum : unsigned
+{
+  FAULT_MBAR_TIMEOUT = 1u,   // a TMA load never completed within the limit
+  FAULT_BAD_DESCRIPTOR = 2u, // a batched work item named an unknown variant
+};
+
+// One word per device and translation unit; bounded waits set bits here and
+// the host reads (and clears) it through the unit's registration hook.
+static __device__ unsigned g_fault_word;
+
+// Iteration limit of every mbarrier spin in this library.  try_wait suspends
+// for a bounded, hardware-chosen time per call, so the limit is a bound on
+// wall time of the order of a second, never an infinite loop.
+constexpr int kMbarSpinLimit = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar,
+                                                      uint32_t bytes)
+{
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_addr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+// Returns false when the phase did not complete within kMbarSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+  const uint32_t a = smem_addr(bar);
+  for (int i = 0; i < kMbarSpinLimit; ++i)
+  {
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(a), "r"(parity)
+                 : "memory");
+    if (done)
+      return true;
+  }
+  return false;
+}
+
+// 1D bulk copy global -> shared (TMA engine), completion on `bar`.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src,
+                                         uint32_t bytes, uint64_t* bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::"
+               "bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// 1D bulk copy shared -> global (TMA store), tracked by bulk groups.
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src,
+                                         uint32_t bytes)
+{
+  asm volatile(
+      "cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+      "r"(smem_addr(src)), "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit()
+{
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// Wait until the smem sources of all committed bulk stores may be reused.
+__device__ __forceinline__ void bulk_wait_read0()
+{
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// Wait until all committed bulk stores are complete (visible in global).
+__device__ __forceinline__ void bulk_wait0()
+{
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+__device__ __forceinline__ void record_fault(unsigned bits)
+{
+  atomicOr(&g_fault_word, bits);
+}
+
+} // namespace femtc

@@ -1,0 +1,29 @@
+// Host-side registry of the compiled kernel variants.  Each translation unit
+// that instantiates kernels appends its variants (and the reader of its
+// device fault word) at library load.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <vector>
+
+namespace femtc
+{
+
+struct CellVariant
+{
+  int dtype;   // femtc_dtype
+  int op;      // femtc_op
+  int sem;     // femtc_semantics
+  int n, q;    // DOFs and quadrature points per axis
+  const void* fn;
+  unsigned (*smem)(int cb, int staged); // dynamic shared memory, bytes
+};
+
+using FaultReader = unsigned (*)(); // returns and clears the unit's fault word
+
+void register_cell_f64_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+
+} // namespace femtc

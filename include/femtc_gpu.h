@@ -1,0 +1,130 @@
+/* femtc_gpu.h -- C ABI of the GB300 (sm_103a) matrix-free hexahedral
+ * operator library.
+ *
+ * This is the drop-in boundary for the hot path of IgorBaratta/femtc: the
+ * per-cell, sum-factorized mass and stiffness action.  Every entry point
+ * names the reference interface it replaces.  All functions return
+ * FEMTC_OK (0) or a negative status; femtc_last_error() then describes the
+ * failure (per calling thread).  No function allocates memory that outlives
+ * the call except the library context (a cached stream and grow-only device
+ * staging buffers used by the *_host entry points).
+ *
+ * Layouts (the reference's):
+ *   u, y   : [ncells][N][N][N], N = degree+1, axis 0 slowest
+ *            (src/mass.hpp:25-29)
+ *   dw     : mass quadrature weights detJ*w, [ncells][Q][Q][Q]
+ *            (src/mass.hpp:27, where the reference has Q == N)
+ *   G      : stiffness geometry, [ncells][Q^3][6], components
+ *            [zz, yz, xz, yy, xy, xx] (src/stiffness.hpp:20-27)
+ *   tables : Phi(q,i) = tables[q + i*Q] (column-major Q x N,
+ *            src/linalg.hpp:49), followed by Gamma(q,i) = tables[Q*N + q + i*Q]
+ *            (src/stiffness.hpp:44-48).  Mass reads only Phi.  Tables are
+ *            HOST memory: they are copied into the launch's parameter block.
+ *
+ * Element types: FEMTC_F64 -> double everywhere; FEMTC_F32 and the mixed
+ * forms -> float storage of u, y, dw/G and the tables.
+ */
+#ifndef FEMTC_GPU_H
+#define FEMTC_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEMTC_OK 0
+#define FEMTC_ERR_INVALID (-1)     /* bad argument: size, pointer, alignment */
+#define FEMTC_ERR_UNSUPPORTED (-2) /* (degree, Q, dtype, semantics) not built */
+#define FEMTC_ERR_CUDA (-3)        /* a CUDA runtime call failed */
+#define FEMTC_ERR_NOMEM (-4)       /* device or pinned allocation failed */
+#define FEMTC_ERR_DEVICE (-5)      /* a kernel's bounded wait gave up */
+
+typedef enum
+{
+  FEMTC_F64 = 0,   /* FP64 storage and arithmetic */
+  FEMTC_F32 = 1,   /* FP32 storage and arithmetic (CUDA cores) */
+  FEMTC_F16X2 = 2, /* FP32 storage; tensor-core FP16 hi/lo split, FP32 acc. */
+  FEMTC_BF16X3 = 3 /* FP32 storage; tensor-core BF16 3-term split, FP32 acc. */
+} femtc_dtype;
+
+typedef enum
+{
+  FEMTC_EXACT = 0,    /* the true operators, any supported Q */
+  FEMTC_REFERENCE = 1 /* the reference's literal arithmetic, Q == N only */
+} femtc_semantics;
+
+typedef enum
+{
+  FEMTC_OP_MASS = 0,
+  FEMTC_OP_STIFFNESS = 1
+} femtc_op;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int femtc_version(void);
+
+/* Description of the last failure on the calling thread ("" if none). */
+const char* femtc_last_error(void);
+
+/* Reads and clears the device fault word of every kernel unit (bits set by
+ * bounded waits that gave up).  Synchronises the device.  Returns the OR of
+ * the words, 0 when clean, or a negative status. */
+int femtc_device_status(void);
+
+/* Whether (op, dtype, semantics, degree, nquad) has a compiled kernel:
+ * 1 yes, 0 no. */
+int femtc_supported(int op, int dtype, int semantics, int degree, int nquad);
+
+/* Mass action y = B^T D B u on device-resident buffers, asynchronous on
+ * `stream` (a cudaStream_t; NULL = legacy default stream).
+ * Replaces operators::mass_operator<T,P,Order,Mb,Nb>(phi, U, W, detJ,
+ * num_cells) (src/mass.hpp:10-12) and its runtime dispatcher
+ * operators::mass_operator<T>(phi, U, W, detJ, num_cells, degree, order,
+ * Mb, Nb) (src/mass.hpp:196-219); the loop order and register blocks of
+ * the CPU code have no GPU meaning and are not arguments here.
+ * u, y, dw: device pointers, 16-byte aligned.  tables: host pointer. */
+int femtc_mass_apply(int dtype, int semantics, int degree, int nquad,
+                     const void* tables, const void* u, void* y,
+                     const void* dw, size_t ncells, void* stream);
+
+/* Stiffness action y = sum_d D_d^T (G D u)_d, device-resident buffers.
+ * Replaces operators::stiffness_operator<T,P,Order,Mb,Nb>(phi, U, W, G,
+ * num_cells) (src/stiffness.hpp:34-36) and its dispatcher
+ * (src/stiffness.hpp:245-268). */
+int femtc_stiffness_apply(int dtype, int semantics, int degree, int nquad,
+                          const void* tables, const void* u, void* y,
+                          const void* G, size_t ncells, void* stream);
+
+/* Host-buffer forms of the two calls above: every pointer is host memory
+ * (pinned memory copies fastest).  Copies u and dw/G to the device, applies
+ * the operator, copies y back and returns when y is written -- the drop-in
+ * path behind the templated C++ header femtc_gpu/operators.hpp. */
+int femtc_mass_apply_host(int dtype, int semantics, int degree, int nquad,
+                          const void* tables, const void* u, void* y,
+                          const void* dw, size_t ncells);
+int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
+                               int nquad, const void* tables, const void* u,
+                               void* y, const void* G, size_t ncells);
+
+/* Tile shape used for a variant: cells per tile (multiple of 4) and whether
+ * the geometry slab is staged through shared memory by TMA.  cb <= 0 restores
+ * the built-in heuristic.  (The autotuner writes these.) */
+int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
+                          int nquad, int cb, int geo_staged);
+int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
+                          int nquad, int* cb, int* geo_staged);
+
+/* 1D basis tables for degree P with Q Gauss-Legendre points on [0,1]:
+ * Lagrange basis on the P+1 Gauss-Lobatto-Legendre nodes (tabulated in
+ * FP64 on the host).  tables: 2*Q*(P+1) doubles in the layout above;
+ * any of points (Q), weights (Q), nodes (P+1) may be NULL.
+ * The reference has no tabulation (bench_mass.cpp:72-76 fills phi with
+ * random numbers). */
+int femtc_tabulate(int degree, int nquad, double* tables, double* points,
+                   double* weights, double* nodes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEMTC_GPU_H */

@@ -1,0 +1,79 @@
+"""CPU: the C-ABI library loads, exports every symbol include/*.h declares,
+and rejects bad arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            txt = open(os.path.join(inc, f)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            syms |= set(re.findall(r"\b(femtc_[a-z0-9_]+)\s*\(", txt))
+    return sorted(syms)
+
+
+def test_exports_every_declared_symbol(femtc):
+    lib = femtc.load()
+    syms = declared_symbols()
+    assert "femtc_mass_apply" in syms and "femtc_stiffness_apply" in syms
+    for s in syms:
+        assert hasattr(lib, s), f"{s} declared in include/ but not exported"
+
+
+def test_version(femtc):
+    assert femtc.load().femtc_version() >= 100
+
+
+def test_supported_matrix(femtc):
+    for P in range(1, 8):
+        for op in (femtc.MASS, femtc.STIFFNESS):
+            for dt in (femtc.F64, femtc.F32):
+                assert femtc.supported(op, dt, femtc.REFERENCE, P, P + 1)
+                for Q in (P + 1, P + 2):
+                    assert femtc.supported(op, dt, femtc.EXACT, P, Q)
+                assert not femtc.supported(op, dt, femtc.REFERENCE, P, P + 2)
+    assert not femtc.supported(femtc.MASS, femtc.F64, femtc.EXACT, 30, 31)
+
+
+@pytest.mark.parametrize("args,code", [
+    (dict(degree=0), -1),            # degree < 1 (bench_mass.cpp:69-70 throws)
+    (dict(nquad=0), -1),
+    (dict(semantics=1, nquad=6), -1), # reference semantics needs Q == N
+    (dict(degree=30, nquad=31), -2),  # not built
+    (dict(dtype=9), -1),
+])
+def test_argument_errors(femtc, args, code):
+    kw = dict(dtype=femtc.F64, semantics=femtc.EXACT, degree=3, nquad=4)
+    kw.update(args)
+    lib = femtc.load()
+    buf = np.zeros(16)
+    rc = lib.femtc_mass_apply(kw["dtype"], kw["semantics"], kw["degree"], kw["nquad"],
+                              buf.ctypes.data, 16, 16, 16, 1, None)
+    assert rc == code
+    assert len(lib.femtc_last_error()) > 0
+
+
+def test_null_pointer_rejected(femtc):
+    lib = femtc.load()
+    t = np.zeros(64)
+    rc = lib.femtc_stiffness_apply(femtc.F64, femtc.EXACT, 3, 4, t.ctypes.data, None, 16, 16, 1, None)
+    assert rc == -1
+
+
+def test_tile_config_roundtrip(femtc):
+    old = femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5)
+    femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 8, 0)
+    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0)
+    with pytest.raises(femtc.FemtcError):
+        femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 6, 0)  # not a multiple of 4
+    femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)  # back to default
+    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == old

@@ -1,0 +1,132 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the oracle.
+
+Tolerances (normwise: max|y - y_ref| / max|y_ref|):
+  FP64 path vs FP64 oracle ...................... 1e-12
+  FP32 path vs FP64 oracle ...................... 2e-6
+  reference semantics vs the reference's own outputs (golden vectors),
+    FP64 1e-12, FP32 vs the reference's float build 2e-6
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TOL = {0: 1e-12, 1: 2e-6}
+
+
+def relerr(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def run_gpu(femtc, dev, op, dtype, sem, P, Q, tables, u, geo, host=False):
+    import torch
+    tdt = torch.float64 if dtype == femtc.F64 else torch.float32
+    if host:
+        uh = np.ascontiguousarray(u, dtype=np.float64 if dtype == femtc.F64 else np.float32)
+        gh = np.ascontiguousarray(geo, dtype=uh.dtype)
+        yh = np.empty_like(uh)
+        femtc.apply_host(op, dtype, sem, P, Q, tables, uh, yh, gh, u.shape[0])
+        return yh.astype(np.float64)
+    ud = torch.from_numpy(np.ascontiguousarray(u)).to(dev, tdt)
+    gd = torch.from_numpy(np.ascontiguousarray(geo)).to(dev, tdt)
+    yd = torch.full_like(ud, float("nan"))
+    femtc.apply(op, dtype, sem, P, Q, tables, ud, yd, gd, u.shape[0])
+    torch.cuda.synchronize()
+    assert femtc.device_status() == 0
+    return yd.cpu().double().numpy()
+
+
+def oracle_apply(orc, op, sem, P, Q, tables, u, geo):
+    fn = orc.mass if op == 0 else orc.stiffness
+    return fn(sem, P, Q, tables, u, geo)
+
+
+@pytest.mark.parametrize("dtype", [0, 1])
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", range(1, 8))
+@pytest.mark.parametrize("dq", [0, 1, 2])
+def test_exact_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
+    from femtc_gb300 import workloads as W
+    Q = P + 1 + dq
+    if not femtc.supported(op, dtype, femtc.EXACT, P, Q):
+        pytest.skip("variant not built")
+    for ncells in (37, 1001):  # ragged tails, many tiles and CTAs
+        w = W.make_custom("t", op, P, Q, ncells, seed=10 * P + dq + 100 * op)
+        y = run_gpu(femtc, dev, op, dtype, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+        ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
+        assert relerr(y, ref) <= TOL[dtype], (ncells, relerr(y, ref))
+
+
+@pytest.mark.parametrize("dtype", [0, 1])
+@pytest.mark.parametrize("op", ["mass", "stiffness"])
+@pytest.mark.parametrize("P", range(1, 8))
+def test_reference_semantics_vs_golden(femtc, dev, dtype, op, P):
+    """Literal parity with the reference's own kernels (golden vectors)."""
+    z = np.load(os.path.join(HERE, "golden", "reference_ops.npz"))
+    t, u, g = z[f"{op}_P{P}_tables"], z[f"{op}_P{P}_u"], z[f"{op}_P{P}_geo"]
+    opc = 0 if op == "mass" else 1
+    y = run_gpu(femtc, dev, opc, dtype, femtc.REFERENCE, P, P + 1, t, u, g)
+    yref = z[f"{op}_P{P}_{'f64' if dtype == 0 else 'f32'}_y"]
+    assert relerr(y, yref) <= TOL[dtype]
+
+
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", [1, 3, 5, 7])
+def test_reference_semantics_vs_oracle_many_cells(femtc, orc, dev, op, P):
+    from femtc_gb300 import workloads as W
+    t, u, g = W.random_reference_inputs(op, P, 777, seed=P)
+    y = run_gpu(femtc, dev, op, femtc.F64, femtc.REFERENCE, P, P + 1, t, u, g)
+    assert relerr(y, oracle_apply(orc, op, orc.REFERENCE, P, P + 1, t, u, g)) <= 1e-12
+
+
+@pytest.mark.parametrize("op", [0, 1])
+def test_host_path_matches_device_path(femtc, dev, op):
+    from femtc_gb300 import workloads as W
+    w = W.make_custom("t", op, 3, 5, 333, seed=4)
+    a = run_gpu(femtc, dev, op, femtc.F64, femtc.EXACT, 3, 5, w.tables, w.u, w.geo)
+    b = run_gpu(femtc, dev, op, femtc.F64, femtc.EXACT, 3, 5, w.tables, w.u, w.geo, host=True)
+    assert np.array_equal(a, b)
+
+
+def test_zero_cells_is_a_noop(femtc, dev):
+    import torch
+    t, _, _, _ = femtc.tabulate(3, 5)
+    u = torch.zeros(64, dtype=torch.float64, device=dev)
+    femtc.apply(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, t, u, u, u, 0)
+    torch.cuda.synchronize()
+
+
+def test_in_place(femtc, orc, dev):
+    import torch
+    from femtc_gb300 import workloads as W
+    w = W.make_custom("t", 1, 4, 6, 500, seed=9)
+    ud = torch.from_numpy(w.u).to(dev)
+    gd = torch.from_numpy(w.geo).to(dev)
+    femtc.apply(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, w.tables, ud, ud, gd, 500)
+    torch.cuda.synchronize()
+    ref = orc.stiffness(orc.EXACT, 4, 6, w.tables, w.u, w.geo)
+    assert relerr(ud.cpu().numpy(), ref) <= 1e-12
+
+
+def test_misaligned_pointer_rejected(femtc, dev):
+    import torch
+    t, _, _, _ = femtc.tabulate(3, 5)
+    u = torch.zeros(1000, dtype=torch.float64, device=dev)
+    with pytest.raises(femtc.FemtcError):
+        femtc.apply(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, t, u.data_ptr() + 8, u, u, 2)
+
+
+@pytest.mark.parametrize("staged", [0, 1])
+@pytest.mark.parametrize("cb", [4, 8, 20])
+def test_tile_configs_agree(femtc, orc, dev, staged, cb):
+    from femtc_gb300 import workloads as W
+    w = W.make_custom("t", 1, 3, 5, 203, seed=2)
+    femtc.set_tile_config(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 3, 5, cb, staged)
+    try:
+        y = run_gpu(femtc, dev, 1, femtc.F64, femtc.EXACT, 3, 5, w.tables, w.u, w.geo)
+    finally:
+        femtc.set_tile_config(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)
+    assert relerr(y, orc.stiffness(orc.EXACT, 3, 5, w.tables, w.u, w.geo)) <= 1e-12

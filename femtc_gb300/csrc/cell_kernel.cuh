@@ -407,17 +407,19 @@ struct CellTile
   }
 };
 
-template <typename T, int N, int Q, int OP, int SEM>
-__global__ void __launch_bounds__(kCellThreads)
-    cell_kernel(const __grid_constant__ CellParams<T> p)
+// The streaming main loop shared by every kernel family: persistent CTAs,
+// two TMA stages, five passes per tile, TMA bulk store of the result.
+// `Tile` provides the Shape `S` and the static passes pass1..pass5.
+template <typename T, typename Tile>
+__device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
 {
-  using S = Shape<N, Q, OP, SEM>;
-  using K = CellTile<T, N, Q, OP, SEM>;
+  using S = typename Tile::S;
   extern __shared__ __align__(128) unsigned char smem[];
   const int cb = p.cb;
   const bool staged = p.geo_staged != 0;
   const long long ntiles = (p.ncells + cb - 1) / cb;
-  const CellLayout L = make_layout<N, Q, OP, SEM, T>(cb, p.geo_staged);
+  const CellLayout L(cb, (int)sizeof(T), S::N3, S::Q3 * S::NC, S::work,
+                     p.geo_staged);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   // stage s buffers (selected arithmetically: no local-memory arrays)
   auto su = [&](int s) { return reinterpret_cast<T*>(smem + (s ? L.u1 : L.u0)); };
@@ -480,20 +482,20 @@ __global__ void __launch_bounds__(kCellThreads)
         record_fault(FAULT_MBAR_TIMEOUT);
       break;
     }
-    K::pass1(p, su(s), sw, ncb);
+    Tile::pass1(p, su(s), sw, ncb);
     __syncthreads();
-    K::pass2(p, sw, ncb);
+    Tile::pass2(p, sw, ncb);
     __syncthreads();
     if (staged)
-      K::pass3(p, sw, ncb, sg(s), 0);
+      Tile::pass3(p, sw, ncb, sg(s), 0);
     else
-      K::pass3(p, sw, ncb, p.geo, tile * cb);
+      Tile::pass3(p, sw, ncb, p.geo, tile * cb);
     __syncthreads();
-    K::pass4(p, sw, ncb);
+    Tile::pass4(p, sw, ncb);
     if (threadIdx.x == 0)
       bulk_wait_read0(); // previous tile's store has left sy
     __syncthreads();
-    K::pass5(p, sw, sy, ncb);
+    Tile::pass5(p, sw, sy, ncb);
     if (full)
     {
       fence_proxy_async_smem();
@@ -514,6 +516,13 @@ __global__ void __launch_bounds__(kCellThreads)
   }
   if (threadIdx.x == 0)
     bulk_wait0();
+}
+
+template <typename T, int N, int Q, int OP, int SEM>
+__global__ void __launch_bounds__(kCellThreads)
+    cell_kernel(const __grid_constant__ CellParams<T> p)
+{
+  stream_tiles<T, CellTile<T, N, Q, OP, SEM>>(p);
 }
 
 } // namespace femtc

@@ -56,6 +56,10 @@ Registry& registry()
     register_cell_f64_stiffness(r.cells, r.faults);
     register_cell_f32_mass(r.cells, r.faults);
     register_cell_f32_stiffness(r.cells, r.faults);
+    register_mma_f16x2_mass(r.cells, r.faults);
+    register_mma_f16x2_stiffness(r.cells, r.faults);
+    register_mma_bf16x3_mass(r.cells, r.faults);
+    register_mma_bf16x3_stiffness(r.cells, r.faults);
   });
   return r;
 }

@@ -1,0 +1,649 @@
+// Mixed-precision cell kernels: the same five-pass sum factorization as
+// cell_kernel.cuh, with every 1D contraction on the tensor cores.
+//
+// Each contraction is Out^T[pencils x M] = X^T[pencils x K] . T^T[K x M],
+// issued as warp-level mma.sync m16n8k16 tiles: 16 pencils per MMA row block,
+// the contracted index K = N or Q (<= 10) padded to 16, the output index
+// M = Q or N (<= 10) in one or two n-tiles of 8.  Storage stays FP32 (u, y,
+// D/G, the shared-memory intermediates); every MMA operand is split into
+// low-precision terms and the products are accumulated in FP32:
+//   FEMTC_F16X2  : x = hi + lo (FP16 each), rows scaled by a power of two
+//                  so the largest entry of each 16-wide row sits at 2^13
+//                  (no FP16 overflow, the low term stays normal); products
+//                  lo*HI + hi*LO + hi*HI                          (3 MMAs)
+//   FEMTC_BF16X3 : x = hi + mid + lo (BF16 each, FP32 range, no scaling);
+//                  the six products whose order is at most 2^-16  (6 MMAs)
+// The tables are split the same way once per pass from the launch's
+// parameter block.  In the fused pass the forward accumulator fragment is
+// re-used as the A operand of the backward MMA (the C and A fragment layouts
+// of m16n8k16 coincide), so the point-wise D / G work never touches shared
+// memory.  Exact semantics only.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "cell_kernel.cuh"
+
+namespace femtc
+{
+
+enum Split : int
+{
+  SPLIT_F16X2 = 0,
+  SPLIT_BF16X3 = 1
+};
+
+template <int SPLIT>
+struct SplitTraits;
+
+template <>
+struct SplitTraits<SPLIT_F16X2>
+{
+  static constexpr int terms = 2;
+  static constexpr int nprod = 3;
+  // (A term, B term) of product p, smallest first
+  static __host__ __device__ constexpr int pa(int p) { return p == 0 ? 1 : 0; }
+  static __host__ __device__ constexpr int pb(int p) { return p == 1 ? 1 : 0; }
+  static constexpr bool scaled = true;
+  static __device__ __forceinline__ uint32_t pack(float a, float b)
+  {
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+  }
+  static __device__ __forceinline__ float round(float x)
+  {
+    return __half2float(__float2half_rn(x));
+  }
+  static __device__ __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4],
+                                             uint32_t b0, uint32_t b1)
+  {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+  }
+};
+
+template <>
+struct SplitTraits<SPLIT_BF16X3>
+{
+  static constexpr int terms = 3;
+  static constexpr int nprod = 6;
+  // (A term, B term) of product p: (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)
+  static __host__ __device__ constexpr int pa(int p)
+  {
+    return p == 0 ? 2 : (p == 1 || p == 3) ? 1 : 0;
+  }
+  static __host__ __device__ constexpr int pb(int p)
+  {
+    return p == 2 ? 2 : (p == 1 || p == 4) ? 1 : 0;
+  }
+  static constexpr bool scaled = false;
+  static __device__ __forceinline__ uint32_t pack(float a, float b)
+  {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+  }
+  static __device__ __forceinline__ float round(float x)
+  {
+    return __bfloat162float(__float2bfloat16_rn(x));
+  }
+  static __device__ __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4],
+                                             uint32_t b0, uint32_t b1)
+  {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+  }
+};
+
+// Power-of-two scale that puts max|x| of a row in [2^13, 2^14) (FP16 split);
+// 1 for an all-zero row.  Exact to apply and to undo.
+__device__ __forceinline__ float row_scale(float m)
+{
+  const int e = (__float_as_int(m) >> 23) & 0xff; // biased exponent of max
+  if (e == 0)
+    return 1.0f;
+  int se = 127 + 13 - (e - 127);
+  se = se < 1 ? 1 : (se > 254 ? 254 : se);
+  return __int_as_float(se << 23);
+}
+
+// A operand of one 16-row block: v[0..1] row g (k=2t,2t+1), v[2..3] row g+8,
+// v[4..5] row g (k=2t+8,2t+9), v[6..7] row g+8 -- the m16n8k16 A layout.
+template <int SPLIT>
+struct AFrag
+{
+  using Tr = SplitTraits<SPLIT>;
+  uint32_t r[Tr::terms][4];
+  float inv0, inv1; // undo the row scales of rows g and g+8
+
+  __device__ __forceinline__ void build(float (&v)[8])
+  {
+    float s0 = 1.0f, s1 = 1.0f;
+    if constexpr (Tr::scaled)
+    {
+      float m0 = fmaxf(fmaxf(fabsf(v[0]), fabsf(v[1])), fmaxf(fabsf(v[4]), fabsf(v[5])));
+      float m1 = fmaxf(fmaxf(fabsf(v[2]), fabsf(v[3])), fmaxf(fabsf(v[6]), fabsf(v[7])));
+      m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, 1));
+      m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, 2));
+      m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, 1));
+      m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, 2));
+      s0 = row_scale(m0);
+      s1 = row_scale(m1);
+      v[0] *= s0; v[1] *= s0; v[4] *= s0; v[5] *= s0;
+      v[2] *= s1; v[3] *= s1; v[6] *= s1; v[7] *= s1;
+    }
+    inv0 = 1.0f / s0;
+    inv1 = 1.0f / s1;
+#pragma unroll
+    for (int j = 0; j < Tr::terms; ++j)
+    {
+      float h[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+      {
+        h[i] = (j + 1 < Tr::terms) ? Tr::round(v[i]) : v[i];
+        v[i] -= h[i];
+      }
+      r[j][0] = Tr::pack(h[0], h[1]);
+      r[j][1] = Tr::pack(h[2], h[3]);
+      r[j][2] = Tr::pack(h[4], h[5]);
+      r[j][3] = Tr::pack(h[6], h[7]);
+    }
+  }
+};
+
+// B operand of one table orientation and n-tile, split into terms:
+// B[k][n] = tab[n*SN + k*SK] for k < K, n < M (zero elsewhere).
+template <int SPLIT>
+struct BFrag
+{
+  using Tr = SplitTraits<SPLIT>;
+  uint32_t r[Tr::terms][2];
+
+  template <int K, int M, int SN, int SK>
+  __device__ __forceinline__ void build(const float* __restrict__ tab, int ntile)
+  {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int n = ntile * 8 + g;
+    float v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+    {
+      const int k = 2 * t + (i & 1) + (i >> 1) * 8;
+      v[i] = (k < K && n < M) ? tab[n * SN + k * SK] : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < Tr::terms; ++j)
+    {
+      float h[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+      {
+        h[i] = (j + 1 < Tr::terms) ? Tr::round(v[i]) : v[i];
+        v[i] -= h[i];
+      }
+      r[j][0] = Tr::pack(h[0], h[1]);
+      r[j][1] = Tr::pack(h[2], h[3]);
+    }
+  }
+};
+
+// Tables of one contraction: NT n-tiles of one orientation.
+template <int SPLIT, int K, int M, bool FWD, int Q>
+struct Table
+{
+  static constexpr int NT = (M + 7) / 8;
+  BFrag<SPLIT> f[NT];
+  __device__ __forceinline__ void build(const float* __restrict__ tab)
+  {
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+    {
+      if constexpr (FWD) // out q, contracted i: B[k=i][n=q] = tab[q + i*Q]
+        f[j].template build<K, M, 1, Q>(tab, j);
+      else // exact transpose: out i, contracted q: B[k=q][n=i] = tab[q + i*Q]
+        f[j].template build<K, M, Q, 1>(tab, j);
+    }
+  }
+};
+
+template <int SPLIT, int NT>
+struct Acc
+{
+  float d[NT][4];
+  __device__ __forceinline__ void zero()
+  {
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+      d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.0f;
+  }
+  template <int K, int M, bool FWD, int Q>
+  __device__ __forceinline__ void mma(const AFrag<SPLIT>& a,
+                                      const Table<SPLIT, K, M, FWD, Q>& b)
+  {
+    using Tr = SplitTraits<SPLIT>;
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int p = 0; p < Tr::nprod; ++p)
+        Tr::mma(d[j], a.r[Tr::pa(p)], b.f[j].r[Tr::pb(p)][0], b.f[j].r[Tr::pb(p)][1]);
+  }
+  // undo the A-row scales (rows g and g+8) and add into `o`
+  __device__ __forceinline__ void unscale_into(const AFrag<SPLIT>& a, float (&o)[NT][4]) const
+  {
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+    {
+      o[j][0] += d[j][0] * a.inv0;
+      o[j][1] += d[j][1] * a.inv0;
+      o[j][2] += d[j][2] * a.inv1;
+      o[j][3] += d[j][3] * a.inv1;
+    }
+  }
+};
+
+// Gather the A values of rows r0 = base+g, r1 = base+g+8 of a pencil pass:
+// element k of pencil r is src[idx(r) + k*stride], k < K; zero past K or np.
+template <int K, typename Idx>
+__device__ __forceinline__ void gather(const float* __restrict__ src, Idx idx,
+                                       int stride, int base, int np,
+                                       float (&v)[8])
+{
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int r0 = base + g, r1 = base + g + 8;
+  const bool ok0 = r0 < np, ok1 = r1 < np;
+  const int b0 = ok0 ? idx(r0) : 0, b1 = ok1 ? idx(r1) : 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+  {
+    const int k = 2 * t + (i & 1) + ((i >> 2) & 1) * 8;
+    const bool row1 = (i >> 1) & 1;
+    const bool ok = (k < K) && (row1 ? ok1 : ok0);
+    v[i] = ok ? src[(row1 ? b1 : b0) + k * stride] : 0.0f;
+  }
+}
+
+// Scatter an accumulator of rows r0, r1: output m of pencil r goes to
+// dst[idx(r) + m*stride], m < M.
+template <int M, int NT, typename Idx>
+__device__ __forceinline__ void scatter(float* __restrict__ dst, Idx idx,
+                                        int stride, int base, int np,
+                                        const float (&o)[NT][4])
+{
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int r0 = base + g, r1 = base + g + 8;
+  if (r0 < np)
+  {
+    const int b = idx(r0);
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+      {
+        const int m = j * 8 + 2 * t + e;
+        if (m < M)
+          dst[b + m * stride] = o[j][e];
+      }
+  }
+  if (r1 < np)
+  {
+    const int b = idx(r1);
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int e = 0; e < 2; ++e)
+      {
+        const int m = j * 8 + 2 * t + e;
+        if (m < M)
+          dst[b + m * stride] = o[j][2 + e];
+      }
+  }
+}
+
+template <int NT>
+__device__ __forceinline__ void zero(float (&o)[NT][4])
+{
+#pragma unroll
+  for (int j = 0; j < NT; ++j)
+    o[j][0] = o[j][1] = o[j][2] = o[j][3] = 0.0f;
+}
+
+// One contraction of a pass with up to two (input, table) terms summed:
+// out = T_a^(dir) in_a [+ T_b^(dir) in_b].
+template <int SPLIT, int K, int M, bool FWD, int Q, bool TWO = false,
+          typename InIdx, typename OutIdx>
+__device__ __forceinline__ void contract_pass(
+    const float* __restrict__ in_a, const Table<SPLIT, K, M, FWD, Q>& ta,
+    const float* __restrict__ in_b, const Table<SPLIT, K, M, FWD, Q>& tb,
+    InIdx iidx, int istride, float* __restrict__ out, OutIdx oidx,
+    int ostride, int np)
+{
+  constexpr int NT = (M + 7) / 8;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int base = warp * 16; base < np; base += nwarps * 16)
+  {
+    float o[NT][4];
+    zero(o);
+    {
+      float v[8];
+      gather<K>(in_a, iidx, istride, base, np, v);
+      AFrag<SPLIT> a;
+      a.build(v);
+      Acc<SPLIT, NT> acc;
+      acc.zero();
+      acc.mma(a, ta);
+      acc.unscale_into(a, o);
+    }
+    if constexpr (TWO)
+    {
+      float v[8];
+      gather<K>(in_b, iidx, istride, base, np, v);
+      AFrag<SPLIT> a;
+      a.build(v);
+      Acc<SPLIT, NT> acc;
+      acc.zero();
+      acc.mma(a, tb);
+      acc.unscale_into(a, o);
+    }
+    scatter<M, NT>(out, oidx, ostride, base, np, o);
+  }
+}
+
+template <int SPLIT, int N, int Q, int OP>
+struct MmaTile
+{
+  using S = Shape<N, Q, OP, SEM_EXACT>;
+  using T = float;
+
+  // Pass 1: axis 2, u[c][i0][i1][i2] -> A[c][i0][i1][q2]
+  static __device__ __forceinline__ void pass1(const CellParams<float>& p,
+                                               const float* __restrict__ su,
+                                               float* __restrict__ w, int ncb)
+  {
+    float* A0 = w;
+    float* A1 = w + ncb * S::SA;
+    const int np = ncb * N * N;
+    auto iidx = [](int r) { const int c = r / (N * N); return c * S::N3 + (r - c * (N * N)) * N; };
+    auto oidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
+    Table<SPLIT, N, Q, true, Q> phi;
+    phi.build(p.tab[0]);
+    contract_pass<SPLIT, N, Q, true, Q>(su, phi, su, phi, iidx, 1, A0, oidx, 1, np);
+    if constexpr (OP == OP_STIFFNESS)
+    {
+      Table<SPLIT, N, Q, true, Q> gam;
+      gam.build(p.tab[1]);
+      contract_pass<SPLIT, N, Q, true, Q>(su, gam, su, gam, iidx, 1, A1, oidx, 1, np);
+    }
+  }
+
+  // Pass 2: axis 1, A[c][i0][i1][q2] -> B[c][i0][q1][q2]
+  static __device__ __forceinline__ void pass2(const CellParams<float>& p,
+                                               float* __restrict__ w, int ncb)
+  {
+    const float* A0 = w;
+    const float* A1 = w + ncb * S::SA;
+    float* B0 = w + ncb * S::nA * S::SA;
+    float* B1 = B0 + ncb * S::SB;
+    float* B2 = B1 + ncb * S::SB;
+    const int np = ncb * N * Q;
+    auto iidx = [](int r) {
+      const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
+      return c * S::SA + i0 * N * S::QP + q2;
+    };
+    auto oidx = [](int r) {
+      const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
+      return c * S::SB + i0 * Q * Q + q2;
+    };
+    Table<SPLIT, N, Q, true, Q> phi;
+    phi.build(p.tab[0]);
+    contract_pass<SPLIT, N, Q, true, Q>(A0, phi, A0, phi, iidx, S::QP, B0, oidx, Q, np);
+    if constexpr (OP == OP_STIFFNESS)
+    {
+      contract_pass<SPLIT, N, Q, true, Q>(A1, phi, A1, phi, iidx, S::QP, B2, oidx, Q, np);
+      Table<SPLIT, N, Q, true, Q> gam;
+      gam.build(p.tab[1]);
+      contract_pass<SPLIT, N, Q, true, Q>(A0, gam, A0, gam, iidx, S::QP, B1, oidx, Q, np);
+    }
+  }
+
+  // Pass 3 (fused, registers only between the two MMAs): axis 0 forward,
+  // D scaling / G transform, axis 0 backward; in place in B.
+  static __device__ __forceinline__ void pass3(const CellParams<float>& p,
+                                               float* __restrict__ w, int ncb,
+                                               const float* __restrict__ geo,
+                                               long long geo_cell0)
+  {
+    constexpr int NTQ = (Q + 7) / 8, NTN = (N + 7) / 8;
+    float* B0 = w + ncb * S::nA * S::SA;
+    float* B1 = B0 + ncb * S::SB;
+    float* B2 = B1 + ncb * S::SB;
+    const int np = ncb * Q * Q;
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    auto bidx = [](int r) { const int c = r / (Q * Q); return c * S::SB + (r - c * (Q * Q)); };
+    Table<SPLIT, N, Q, true, Q> fphi;
+    Table<SPLIT, Q, N, false, Q> bphi;
+    fphi.build(p.tab[0]);
+    bphi.build(p.tab[0]);
+    for (int base = warp * 16; base < np; base += nwarps * 16)
+    {
+      const int r0 = base + g, r1 = base + g + 8;
+      // geometry offsets of rows r0, r1: point (c, q0, rr) at
+      // ((geo_cell0 + c)*Q3 + q0*Q*Q + rr)*NC
+      auto gofs = [&](int r) -> long long {
+        const int c = r / (Q * Q), rr = r - c * (Q * Q);
+        return ((geo_cell0 + c) * S::Q3 + rr) * S::NC;
+      };
+      const long long go0 = r0 < np ? gofs(r0) : -1, go1 = r1 < np ? gofs(r1) : -1;
+      if constexpr (OP == OP_MASS)
+      {
+        float v[8];
+        gather<N>(B0, bidx, Q * Q, base, np, v);
+        AFrag<SPLIT> a;
+        a.build(v);
+        Acc<SPLIT, NTQ> acc;
+        acc.zero();
+        acc.mma(a, fphi);
+        float f[NTQ][4];
+        zero(f);
+        acc.unscale_into(a, f);
+        // scale by D at (row, q0)
+#pragma unroll
+        for (int j = 0; j < NTQ; ++j)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+          {
+            const int q0 = j * 8 + 2 * t + (e & 1);
+            const long long go = (e < 2) ? go0 : go1;
+            f[j][e] = (q0 < Q && go >= 0) ? f[j][e] * geo[go + q0 * Q * Q] : 0.0f;
+          }
+        float vb[8];
+        to_operand<NTQ>(f, vb);
+        AFrag<SPLIT> ab;
+        ab.build(vb);
+        Acc<SPLIT, NTN> accb;
+        accb.zero();
+        accb.mma(ab, bphi);
+        float o[NTN][4];
+        zero(o);
+        accb.unscale_into(ab, o);
+        scatter<N, NTN>(B0, bidx, Q * Q, base, np, o);
+      }
+      else
+      {
+        Table<SPLIT, N, Q, true, Q> fgam;
+        fgam.build(p.tab[1]);
+        float fx[NTQ][4], fy[NTQ][4], fz[NTQ][4];
+        zero(fx);
+        zero(fy);
+        zero(fz);
+        {
+          float v[8];
+          gather<N>(B0, bidx, Q * Q, base, np, v); // AA -> d/dx: Gamma on axis 0
+          AFrag<SPLIT> a;
+          a.build(v);
+          Acc<SPLIT, NTQ> acc;
+          acc.zero();
+          acc.mma(a, fgam);
+          acc.unscale_into(a, fx);
+        }
+        {
+          float v[8];
+          gather<N>(B1, bidx, Q * Q, base, np, v); // AG -> d/dy
+          AFrag<SPLIT> a;
+          a.build(v);
+          Acc<SPLIT, NTQ> acc;
+          acc.zero();
+          acc.mma(a, fphi);
+          acc.unscale_into(a, fy);
+        }
+        {
+          float v[8];
+          gather<N>(B2, bidx, Q * Q, base, np, v); // BA -> d/dz
+          AFrag<SPLIT> a;
+          a.build(v);
+          Acc<SPLIT, NTQ> acc;
+          acc.zero();
+          acc.mma(a, fphi);
+          acc.unscale_into(a, fz);
+        }
+        // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx]
+#pragma unroll
+        for (int j = 0; j < NTQ; ++j)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+          {
+            const int q0 = j * 8 + 2 * t + (e & 1);
+            const long long go = (e < 2) ? go0 : go1;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+            if (q0 < Q && go >= 0)
+            {
+              const float* G = geo + go + (long long)q0 * Q * Q * 6;
+              const float w0 = fx[j][e], w1 = fy[j][e], w2 = fz[j][e];
+              a0 = G[5] * w0 + G[4] * w1 + G[2] * w2;
+              a1 = G[4] * w0 + G[3] * w1 + G[1] * w2;
+              a2 = G[2] * w0 + G[1] * w1 + G[0] * w2;
+            }
+            fx[j][e] = a0;
+            fy[j][e] = a1;
+            fz[j][e] = a2;
+          }
+        Table<SPLIT, Q, N, false, Q> bgam;
+        bgam.build(p.tab[1]);
+        backward_store<NTQ, NTN>(fx, bgam, B0, bidx, base, np);
+        backward_store<NTQ, NTN>(fy, bphi, B1, bidx, base, np);
+        backward_store<NTQ, NTN>(fz, bphi, B2, bidx, base, np);
+      }
+    }
+  }
+
+  // accumulator fragment (rows g, g+8; cols 2t,2t+1 [+8]) -> A values
+  template <int NTQ>
+  static __device__ __forceinline__ void to_operand(const float (&f)[NTQ][4], float (&v)[8])
+  {
+    v[0] = f[0][0];
+    v[1] = f[0][1];
+    v[2] = f[0][2];
+    v[3] = f[0][3];
+    if constexpr (NTQ > 1)
+    {
+      v[4] = f[1][0];
+      v[5] = f[1][1];
+      v[6] = f[1][2];
+      v[7] = f[1][3];
+    }
+    else
+    {
+      v[4] = v[5] = v[6] = v[7] = 0.0f;
+    }
+  }
+
+  template <int NTQ, int NTN, typename Idx>
+  static __device__ __forceinline__ void backward_store(
+      const float (&f)[NTQ][4], const Table<SPLIT, Q, N, false, Q>& tb,
+      float* __restrict__ dst, Idx idx, int base, int np)
+  {
+    float v[8];
+    to_operand<NTQ>(f, v);
+    AFrag<SPLIT> a;
+    a.build(v);
+    Acc<SPLIT, NTN> acc;
+    acc.zero();
+    acc.mma(a, tb);
+    float o[NTN][4];
+    zero(o);
+    acc.unscale_into(a, o);
+    scatter<N, NTN>(dst, idx, Q * Q, base, np, o);
+  }
+
+  // Pass 4: backward axis 1, B[c][i0][q1][q2] -> A[c][i0][i1][q2]
+  static __device__ __forceinline__ void pass4(const CellParams<float>& p,
+                                               float* __restrict__ w, int ncb)
+  {
+    float* A0 = w;
+    float* A1 = w + ncb * S::SA;
+    const float* B0 = w + ncb * S::nA * S::SA;
+    const float* B1 = B0 + ncb * S::SB;
+    const float* B2 = B1 + ncb * S::SB;
+    const int np = ncb * N * Q;
+    auto iidx = [](int r) {
+      const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
+      return c * S::SB + i0 * Q * Q + q2;
+    };
+    auto oidx = [](int r) {
+      const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
+      return c * S::SA + i0 * N * S::QP + q2;
+    };
+    Table<SPLIT, Q, N, false, Q> phi;
+    phi.build(p.tab[0]);
+    if constexpr (OP == OP_MASS)
+    {
+      contract_pass<SPLIT, Q, N, false, Q>(B0, phi, B0, phi, iidx, Q, A0, oidx, S::QP, np);
+    }
+    else
+    {
+      Table<SPLIT, Q, N, false, Q> gam;
+      gam.build(p.tab[1]);
+      // U1 = Phi^T X + Gamma^T Y ; U2 = Phi^T Z
+      contract_pass<SPLIT, Q, N, false, Q, true>(B0, phi, B1, gam, iidx, Q, A0, oidx, S::QP, np);
+      contract_pass<SPLIT, Q, N, false, Q>(B2, phi, B2, phi, iidx, Q, A1, oidx, S::QP, np);
+    }
+  }
+
+  // Pass 5: backward axis 2, A[c][i0][i1][q2] -> y[c][i0][i1][i2]
+  static __device__ __forceinline__ void pass5(const CellParams<float>& p,
+                                               const float* __restrict__ w,
+                                               float* __restrict__ sy, int ncb)
+  {
+    const float* A0 = w;
+    const float* A1 = w + ncb * S::SA;
+    const int np = ncb * N * N;
+    auto iidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
+    auto oidx = [](int r) { const int c = r / (N * N); return c * S::N3 + (r - c * (N * N)) * N; };
+    Table<SPLIT, Q, N, false, Q> phi;
+    phi.build(p.tab[0]);
+    if constexpr (OP == OP_MASS)
+    {
+      contract_pass<SPLIT, Q, N, false, Q>(A0, phi, A0, phi, iidx, 1, sy, oidx, 1, np);
+    }
+    else
+    {
+      Table<SPLIT, Q, N, false, Q> gam;
+      gam.build(p.tab[1]);
+      contract_pass<SPLIT, Q, N, false, Q, true>(A0, phi, A1, gam, iidx, 1, sy, oidx, 1, np);
+    }
+  }
+};
+
+template <int SPLIT, int N, int Q, int OP>
+__global__ void __launch_bounds__(kCellThreads)
+    mma_kernel(const __grid_constant__ CellParams<float> p)
+{
+  stream_tiles<float, MmaTile<SPLIT, N, Q, OP>>(p);
+}
+
+} // namespace femtc

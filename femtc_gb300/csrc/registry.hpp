@@ -25,5 +25,9 @@ void register_cell_f64_mass(std::vector<CellVariant>&, std::vector<FaultReader>&
 void register_cell_f64_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_mma_f16x2_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_mma_f16x2_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_mma_bf16x3_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_mma_bf16x3_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 
 } // namespace femtc

@@ -120,7 +120,7 @@ def test_misaligned_pointer_rejected(femtc, dev):
 
 
 @pytest.mark.parametrize("staged", [0, 1])
-@pytest.mark.parametrize("cb", [4, 8, 20])
+@pytest.mark.parametrize("cb", [4, 8, 12])
 def test_tile_configs_agree(femtc, orc, dev, staged, cb):
     from femtc_gb300 import workloads as W
     w = W.make_custom("t", 1, 3, 5, 203, seed=2)
@@ -130,3 +130,9 @@ def test_tile_configs_agree(femtc, orc, dev, staged, cb):
     finally:
         femtc.set_tile_config(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)
     assert relerr(y, orc.stiffness(orc.EXACT, 3, 5, w.tables, w.u, w.geo)) <= 1e-12
+
+
+def test_oversized_tile_rejected(femtc):
+    # 20 cells of P=3/Q=5 FP64 stiffness with staged geometry need 260 KB
+    with pytest.raises(femtc.FemtcError):
+        femtc.set_tile_config(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 3, 5, 20, 1)

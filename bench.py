@@ -54,6 +54,20 @@ def bytes_per_cell(op: int, n: int, q: int, es: int) -> float:
     return es * (2 * n ** 3 + (1 if op == 0 else 6) * q ** 3)
 
 
+def roofline(head, ach_tf, ach_gbs, hbm, hbm_src):
+    """The binding roof of the headline kernel: the FP64 pipe for FP64 (its
+    arithmetic intensity puts it far above the FP64 ridge), HBM otherwise."""
+    hbm_part = {"achieved": ach_gbs, "peak": hbm, "unit": "GB/s", "frac": ach_gbs / hbm,
+                "peak_source": hbm_src}
+    if head == 0:
+        return {"bound": "fp64", "achieved": ach_tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                "frac": ach_tf / FP64_PEAK_TFLOPS, "traffic": None,
+                "peak_source": "measured FP64 FMA pipe (profiles/gb300_pipe_peaks.md)",
+                "hbm": hbm_part}
+    return {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s", "frac": ach_gbs / hbm,
+            "traffic": None, "peak_source": hbm_src}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -195,6 +209,10 @@ def main():
     ap.add_argument("--workload", default="stiffness_p4",
                     choices=["stiffness_p4", "mass_p3", "stiffness_p6"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
+    ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3",
+                    help="comma list of forms to time; the first is the headline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -216,9 +234,12 @@ def main():
         pg = dist
     F.load()
 
-    w = W.make(args.workload)
+    w = W.make(args.workload, ncells=args.cells)
     n, q, op = w.n, w.nquad, w.op
     stream = torch.cuda.current_stream()
+    names = {v: k for k, v in F.DTYPE_NAMES.items()}
+    dtypes = [names[d] for d in args.dtypes.split(",")]
+    head = dtypes[0]
 
     def barrier():
         if pg is not None:
@@ -232,8 +253,16 @@ def main():
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         return float(t.item())
 
+    # FP64 oracle on a slice of the workload: every form states its error
+    err_cells = min(w.ncells, 2048)
+    y_oracle = None
+    if rank == 0:
+        import oracle
+        fn = oracle.mass if op == 0 else oracle.stiffness
+        y_oracle = fn(oracle.EXACT, w.degree, q, w.tables, w.u[:err_cells], w.geo[:err_cells])
+
     results = {}
-    for dtype in (F.F64, F.F32):
+    for dtype in dtypes:
         tdt = torch.float64 if dtype == F.F64 else torch.float32
         u = torch.from_numpy(w.u).to(dev, tdt)
         g = torch.from_numpy(w.geo).to(dev, tdt)
@@ -247,7 +276,7 @@ def main():
         barrier()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
-        sampler = ClockSampler(local) if dtype == F.F64 else None
+        sampler = ClockSampler(local) if dtype == head else None
         if sampler:
             sampler.__enter__()
         barrier()
@@ -264,7 +293,12 @@ def main():
             sampler.__exit__(None, None, None)
         total_ms = maxreduce(t_start.elapsed_time(t_end))
         kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
-        results[dtype] = dict(total_ms=total_ms, kern_ms=kern_ms, clocks=sampler.summary() if sampler else None)
+        err = None
+        if y_oracle is not None:
+            yo = y[:err_cells].double().cpu().numpy()
+            err = float(np.abs(yo - y_oracle).max() / np.abs(y_oracle).max())
+        results[dtype] = dict(total_ms=total_ms, kern_ms=kern_ms, err=err,
+                              clocks=sampler.summary() if sampler else None)
         if F.device_status() != 0:
             raise RuntimeError("device fault word set during the benchmark")
         del u, g, y
@@ -272,7 +306,7 @@ def main():
 
     # end-to-end through the host-buffer C-ABI entry point, pinned buffers
     e2e = {}
-    for dtype in (F.F64,):
+    for dtype in ([] if args.no_e2e else [head]):
         npdt = np.float64 if dtype == F.F64 else np.float32
         uh = torch.from_numpy(w.u.astype(npdt)).pin_memory()
         gh = torch.from_numpy(w.geo.astype(npdt)).pin_memory()
@@ -293,10 +327,10 @@ def main():
                           h2d=uh.numel() * uh.element_size() + gh.numel() * gh.element_size(),
                           d2h=yh.numel() * yh.element_size())
 
-    r = results[F.F64]
+    r = results[head]
     value = world * args.steps * w.ndofs / (r["total_ms"] * 1e-3) / 1e9
     fpc = flops_per_cell(op, n, q)
-    bpc = bytes_per_cell(op, n, q, 8)
+    bpc = bytes_per_cell(op, n, q, 8 if head == F.F64 else 4)
     ach_tf = fpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e12
     ach_gbs = bpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e9
     hbm, hbm_src = peaks()
@@ -308,28 +342,26 @@ def main():
             "kernel_ms": res["kern_ms"],
             "hbm_gbs": bytes_per_cell(op, n, q, es) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
             "tflops": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
+            "max_rel_err_vs_fp64_oracle": res["err"],
         }
     if rank == 0:
         line = {
             "metric": "GDoF/s stiffness action (P=4, Q=6)" if op == 1 else "GDoF/s mass action (P=3, Q=5)",
             "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": F.DTYPE_NAMES[head], "data": "synthetic",
             "config": {"workload": args.workload, "cells": w.ncells, "degree": w.degree, "nquad": q,
                        "dofs": w.ndofs, "parallelism": f"replicas{world}",
                        "l2": f"inputs {bpc * w.ncells / 1e6:.0f} MB > 129 MB L2, no flush"},
-            "roofline": {"bound": "fp64", "achieved": ach_tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                         "frac": ach_tf / FP64_PEAK_TFLOPS, "traffic": None,
-                         "peak_source": "measured FP64 FMA pipe (profiles/gb300_pipe_peaks.md)",
-                         "hbm": {"achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
-                                 "frac": ach_gbs / hbm, "peak_source": hbm_src}},
-            "e2e": {"value": e2e[F.F64]["gdofs"], "unit": "GDoF/s",
-                    "h2d_bytes_per_step": e2e[F.F64]["h2d"], "d2h_bytes_per_step": e2e[F.F64]["d2h"]},
-            "gpu_launches": 2 * args.steps + args.steps,
+            "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src),
+            "gpu_launches": args.steps * (len(dtypes) + (0 if args.no_e2e else 1)),
             "clocks": r["clocks"],
             "variants": variants,
         }
+        if head in e2e:
+            line["e2e"] = {"value": e2e[head]["gdofs"], "unit": "GDoF/s",
+                           "h2d_bytes_per_step": e2e[head]["h2d"], "d2h_bytes_per_step": e2e[head]["d2h"]}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(w)
         print(json.dumps(line), flush=True)

@@ -166,7 +166,7 @@ def run_reference(args, rank, world):
     t = float(np.mean(times))
     gdofs = sample * n ** 3 / t / 1e9
     line = {
-        "metric": "GDoF/s stiffness action (P=4, Q=6)" if w.op == 1 else "GDoF/s mass action (P=3, Q=5)",
+        "metric": f"GDoF/s {'stiffness' if w.op == 1 else 'mass'} action (P={w.degree}, Q={q})",
         "value": gdofs, "unit": "GDoF/s", "impl": "reference", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -213,6 +213,9 @@ def main():
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
     ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3",
                     help="comma list of forms to time; the first is the headline")
+    ap.add_argument("--tile-db", default=None,
+                    help="tile configuration file: loaded if it exists (no tuning), "
+                         "else written after autotuning")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -261,6 +264,10 @@ def main():
         fn = oracle.mass if op == 0 else oracle.stiffness
         y_oracle = fn(oracle.EXACT, w.degree, q, w.tables, w.u[:err_cells], w.geo[:err_cells])
 
+    tuned = False
+    if args.tile_db and os.path.exists(args.tile_db):
+        F.tile_db_load(args.tile_db)
+        tuned = True
     results = {}
     for dtype in dtypes:
         tdt = torch.float64 if dtype == F.F64 else torch.float32
@@ -270,6 +277,10 @@ def main():
 
         def step():
             F.apply(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
+
+        if not tuned:  # the project's autotuner, outside the timed region
+            F.autotune(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
+        tile = F.get_tile_config(op, dtype, F.EXACT, w.degree, q)
 
         for _ in range(args.warmup):
             step()
@@ -297,12 +308,15 @@ def main():
         if y_oracle is not None:
             yo = y[:err_cells].double().cpu().numpy()
             err = float(np.abs(yo - y_oracle).max() / np.abs(y_oracle).max())
-        results[dtype] = dict(total_ms=total_ms, kern_ms=kern_ms, err=err,
+        results[dtype] = dict(total_ms=total_ms, kern_ms=kern_ms, err=err, tile=tile,
                               clocks=sampler.summary() if sampler else None)
         if F.device_status() != 0:
             raise RuntimeError("device fault word set during the benchmark")
         del u, g, y
         torch.cuda.empty_cache()
+
+    if args.tile_db and not tuned and rank == 0:
+        F.tile_db_save(args.tile_db)
 
     # end-to-end through the host-buffer C-ABI entry point, pinned buffers
     e2e = {}
@@ -343,10 +357,11 @@ def main():
             "hbm_gbs": bytes_per_cell(op, n, q, es) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
             "tflops": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
             "max_rel_err_vs_fp64_oracle": res["err"],
+            "tile": {"cells": res["tile"][0], "geo_staged": res["tile"][1], "threads": res["tile"][2]},
         }
     if rank == 0:
         line = {
-            "metric": "GDoF/s stiffness action (P=4, Q=6)" if op == 1 else "GDoF/s mass action (P=3, Q=5)",
+            "metric": f"GDoF/s {'stiffness' if op == 1 else 'mass'} action (P={w.degree}, Q={q})",
             "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -45,9 +45,16 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_stiffness_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
         "femtc_mass_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_stiffness_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
-        "femtc_set_tile_config": ([c_int] * 7, c_int),
-        "femtc_get_tile_config": ([c_int] * 5 + [ctypes.POINTER(c_int)] * 2, c_int),
+        "femtc_set_tile_config": ([c_int] * 8, c_int),
+        "femtc_get_tile_config": ([c_int] * 5 + [ctypes.POINTER(c_int)] * 3, c_int),
+        "femtc_autotune": ([c_int] * 5 + [vp] * 4 + [c_size, vp] + [ctypes.POINTER(c_int)] * 3
+                           + [ctypes.POINTER(ctypes.c_float)], c_int),
+        "femtc_tile_db_save": ([ctypes.c_char_p], c_int),
+        "femtc_tile_db_load": ([ctypes.c_char_p], c_int),
         "femtc_tabulate": ([c_int, c_int, dp, dp, dp, dp], c_int),
+        "femtc_gemm_blocked": ([c_int] * 4 + [vp] * 3 + [c_size, vp], c_int),
+        "femtc_apply_contractions": ([c_int] * 4 + [vp] * 5 + [c_size, vp], c_int),
+        "femtc_geometry": ([c_int, c_int, vp, vp, c_int, vp, vp, c_size, vp], c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -142,15 +149,40 @@ def supported(op: int, dtype: int, semantics: int, degree: int, nquad: int) -> b
     return bool(load().femtc_supported(op, dtype, semantics, degree, nquad))
 
 
-def set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged) -> None:
-    check(load().femtc_set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged))
+def set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged, threads=256) -> None:
+    check(load().femtc_set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged,
+                                       threads))
 
 
 def get_tile_config(op, dtype, semantics, degree, nquad):
-    cb, st = ctypes.c_int(), ctypes.c_int()
+    """(cells per tile, geometry staged, threads per CTA)."""
+    cb, st, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     check(load().femtc_get_tile_config(op, dtype, semantics, degree, nquad,
-                                       ctypes.byref(cb), ctypes.byref(st)))
-    return cb.value, st.value
+                                       ctypes.byref(cb), ctypes.byref(st), ctypes.byref(nt)))
+    return cb.value, st.value, nt.value
+
+
+def autotune(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells, stream=None):
+    """Measure tile shapes on these buffers and keep the fastest.
+    Returns (cb, geo_staged, threads, ms)."""
+    cb, st, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ms = ctypes.c_float()
+    tab = host_tables(tables, dtype)
+    check(load().femtc_autotune(op, dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u),
+                                ptr(y), ptr(geo), ncells, stream_ptr(stream), ctypes.byref(cb),
+                                ctypes.byref(st), ctypes.byref(nt), ctypes.byref(ms)))
+    return cb.value, st.value, nt.value, ms.value
+
+
+def tile_db_save(path: str) -> None:
+    check(load().femtc_tile_db_save(path.encode()))
+
+
+def tile_db_load(path: str) -> int:
+    n = load().femtc_tile_db_load(path.encode())
+    if n < 0:
+        check(n)
+    return n
 
 
 def device_status() -> int:
@@ -158,3 +190,27 @@ def device_status() -> int:
     if s < 0:
         check(s)
     return s
+
+
+def gemm_blocked(dtype: int, k: int, m: int, n: int, a, b, c, batch: int, stream=None) -> None:
+    """Batched linalg::gemm_blocked on the device (a: host table)."""
+    tab = host_tables(a, dtype)
+    check(load().femtc_gemm_blocked(dtype, k, m, n, tab.ctypes.data, ptr(b), ptr(c), batch,
+                                    stream_ptr(stream)))
+
+
+def apply_contractions(dtype: int, na: int, nb: int, tr: bool, i0, i1, i2, b, a, ncells: int,
+                       stream=None) -> None:
+    """Batched tmm apply_contractions on the device (tables: host)."""
+    t = [host_tables(x, dtype) for x in (i0, i1, i2)]
+    check(load().femtc_apply_contractions(dtype, na, nb, int(bool(tr)), t[0].ctypes.data,
+                                          t[1].ctypes.data, t[2].ctypes.data, ptr(b), ptr(a),
+                                          ncells, stream_ptr(stream)))
+
+
+def geometry(out_dtype: int, nquad: int, weights, J, dw, G, ncells: int, per_point: bool = False,
+             stream=None) -> None:
+    """FP64 quadrature factors detJ*w and/or G from Jacobians (device J)."""
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    check(load().femtc_geometry(out_dtype, nquad, w.ctypes.data, ptr(J), int(bool(per_point)),
+                                ptr(dw), ptr(G), ncells, stream_ptr(stream)))

@@ -10,9 +10,16 @@
 namespace femtc
 {
 template <typename T, int N, int Q, int OP, int SEM>
-unsigned cell_smem_bytes(int cb, int staged)
+unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
 {
-  return make_layout<N, Q, OP, SEM, T>(cb, staged).total;
+  CellParams<T> p{};
+  p.cb = cb;
+  p.geo_staged = staged;
+  p.sq = sq;
+  p.sbc = sbc;
+  return tile_layout<T, SlabTile<T, N, Q, OP, SEM>, N, Q,
+                     (OP == OP_MASS) ? 1 : 6>(p)
+      .total;
 }
 
 template <typename T, int N, int Q, int OP, int SEM>
@@ -21,7 +28,7 @@ void add_variant(std::vector<CellVariant>& v, int dtype)
   v.push_back(CellVariant{dtype, OP, SEM, N, Q,
                           reinterpret_cast<const void*>(
                               &cell_kernel<T, N, Q, OP, SEM>),
-                          &cell_smem_bytes<T, N, Q, OP, SEM>});
+                          &cell_smem_bytes<T, N, Q, OP, SEM>, 1, (int)sizeof(T)});
 }
 
 template <typename T, int OP, int N>

@@ -31,6 +31,8 @@
 
 #include "common.cuh"
 
+#include <type_traits>
+
 namespace femtc
 {
 
@@ -58,7 +60,20 @@ struct CellParams
   long long ncells;
   int cb;            // cells per tile, a multiple of 4
   int geo_staged;    // 1: geometry slab staged by TMA, 0: read in the fused pass
+  int sq;            // slab kernels: stride of one i0 slab in the work buffers
+  int sbc;           // slab kernels: stride of one cell in the work buffers
   T tab[2][kMaxQ * kMaxN]; // Phi(q,i) = tab[0][q + i*Q], Gamma = tab[1]
+};
+
+// What the tile passes read besides the data: the two 1D tables (pointers
+// into a launch's parameter block, so table operands stay in the constant
+// bank) and the work-buffer strides of the slab kernels.
+template <typename T>
+struct TabView
+{
+  const T* __restrict__ P; // Phi(q,i) = P[q + i*Q]
+  const T* __restrict__ D; // Gamma(q,i) = D[q + i*Q]
+  int sq, sbc;
 };
 
 template <int N, int Q, int OP, int SEM>
@@ -76,30 +91,38 @@ struct Shape
   static constexpr int work = nA * SA + nB * SB; // per cell, elements
 };
 
-// Byte offsets of the shared-memory regions (identical on host and device).
+// Byte offsets of the shared-memory regions (identical on host and device):
+// two mbarriers, two (DOF slab, geometry slab) stages, the output slab, and
+// the kernel family's work buffers.  Every region starts 16-byte aligned.
 struct CellLayout
 {
   unsigned u0, g0, u1, g1, y, w, total;
-  __host__ __device__ CellLayout(int cb, int esize, int n3, int q3nc,
-                                 int work, int staged)
+  __host__ __device__ CellLayout(unsigned bu, unsigned bg, unsigned bw)
   {
-    const unsigned bu = (unsigned)cb * n3 * esize;
-    const unsigned bg = staged ? (unsigned)cb * q3nc * esize : 0u;
     u0 = 128; // the two mbarriers live in the first 128 bytes
     g0 = u0 + bu;
     u1 = g0 + bg;
     g1 = u1 + bu;
     y = g1 + bg;
     w = y + bu;
-    total = w + (unsigned)cb * work * esize;
+    total = w + ((bw + 15u) & ~15u);
   }
 };
 
-template <int N, int Q, int OP, int SEM, typename T>
-__host__ __device__ inline CellLayout make_layout(int cb, int staged)
+// Shared-memory stride (elements) of one i0 slab (N*N values) of the DOF and
+// output stages.  Odd N: slabs are packed (the tile is one contiguous bulk
+// copy, and the odd slab stride is bank-conflict free).  Even N: every slab
+// is its own bulk copy into a slot whose byte size is an odd multiple of 16,
+// read and written with 16-byte vector accesses (conflict free per phase).
+template <typename T>
+__host__ __device__ constexpr int slab_stride(int n)
 {
-  using S = Shape<N, Q, OP, SEM>;
-  return CellLayout(cb, (int)sizeof(T), S::N3, S::Q3 * S::NC, S::work, staged);
+  if (n % 2 == 1)
+    return n * n;
+  int units = (n * n * (int)sizeof(T) + 15) / 16;
+  if (units % 2 == 0)
+    ++units;
+  return units * 16 / (int)sizeof(T);
 }
 
 // y[m] = sum_k A(m,k) x[k] with A(m,k) = A[m*SM + k*SK] (compile-time
@@ -135,299 +158,45 @@ __device__ __forceinline__ void mv_acc(const T* __restrict__ A,
   }
 }
 
-template <typename T, int N, int Q, int OP, int SEM>
-struct CellTile
+// ---------------------------------------------------------------------------
+// The streaming main loop shared by every kernel family.  `Tile` provides:
+//   kSlabCopies, US      staging of the DOF/output slabs (see slab_stride)
+//   work_bytes(p)        bytes of its work buffers for a tile of p.cb cells
+//   forward(p, su, sw, ncb)               DOF stage -> work buffers
+//   fused(p, sw, ncb, geo, geo_cell0)     quadrature-point pass, in place
+//   backward(p, sw, sy, ncb)              work buffers -> output stage
+// ---------------------------------------------------------------------------
+template <typename T, typename Tile, int N, int Q, int NC>
+__host__ __device__ inline CellLayout tile_layout(const CellParams<T>& p)
 {
-  using S = Shape<N, Q, OP, SEM>;
-  // Forward tables: out q, contracted i: A(q,i) = tab[q + i*Q].
-  static constexpr int FSM = 1, FSK = Q;
-  // Backward tables: exact applies the transpose A(i,q) = tab[q + i*Q];
-  // the reference reuses the forward table A(i,q) = tab[i + q*Q] (Q == N).
-  static constexpr int BSM = (SEM == SEM_EXACT) ? Q : 1;
-  static constexpr int BSK = (SEM == SEM_EXACT) ? 1 : Q;
+  const unsigned bu = (unsigned)p.cb * N * Tile::US * sizeof(T);
+  const unsigned bg =
+      p.geo_staged ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(T) : 0u;
+  return CellLayout(bu, bg, Tile::work_bytes(p));
+}
 
-  // Pass 1: contract axis 2 (i2 -> q2).  u[c][i0][i1][i2] -> A[c][i0][i1][q2]
-  static __device__ __forceinline__ void pass1(const CellParams<T>& p,
-                                               const T* __restrict__ su,
-                                               T* __restrict__ w, int ncb)
-  {
-    T* A0 = w;
-    T* A1 = w + ncb * S::SA;
-    const int np = ncb * N * N;
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
-    {
-      const int c = t / (N * N), r = t - c * (N * N);
-      T x[N];
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        x[k] = su[c * S::N3 + r * N + k];
-      T o[Q];
-      mv<Q, N, FSM, FSK>(p.tab[0], x, o);
-      T* dst = A0 + c * S::SA + r * S::QP;
-#pragma unroll
-      for (int q = 0; q < Q; ++q)
-        dst[q] = o[q];
-      if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
-      {
-        mv<Q, N, FSM, FSK>(p.tab[1], x, o);
-        T* dst1 = A1 + c * S::SA + r * S::QP;
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-          dst1[q] = o[q];
-      }
-    }
-  }
-
-  // Pass 2: contract axis 1 (i1 -> q1).  A[c][i0][i1][q2] -> B[c][i0][q1][q2]
-  static __device__ __forceinline__ void pass2(const CellParams<T>& p,
-                                               T* __restrict__ w, int ncb)
-  {
-    const T* A0 = w;
-    const T* A1 = w + ncb * S::SA;
-    T* B0 = w + ncb * S::nA * S::SA;
-    T* B1 = B0 + ncb * S::SB;
-    T* B2 = B1 + ncb * S::SB;
-    const int np = ncb * N * Q;
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
-    {
-      const int c = t / (N * Q), r = t - c * (N * Q);
-      const int i0 = r / Q, q2 = r - i0 * Q;
-      const int ia = c * S::SA + i0 * N * S::QP + q2;
-      const int ib = c * S::SB + i0 * Q * Q + q2;
-      T x[N], o[Q];
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        x[k] = A0[ia + k * S::QP];
-      mv<Q, N, FSM, FSK>(p.tab[0], x, o);
-#pragma unroll
-      for (int q = 0; q < Q; ++q)
-        B0[ib + q * Q] = o[q];
-      if constexpr (OP == OP_STIFFNESS)
-      {
-        mv<Q, N, FSM, FSK>(p.tab[1], x, o);
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-          B1[ib + q * Q] = o[q];
-        if constexpr (SEM == SEM_EXACT)
-        {
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            x[k] = A1[ia + k * S::QP];
-          mv<Q, N, FSM, FSK>(p.tab[0], x, o);
-#pragma unroll
-          for (int q = 0; q < Q; ++q)
-            B2[ib + q * Q] = o[q];
-        }
-      }
-    }
-  }
-
-  // Pass 3 (fused): contract axis 0 (i0 -> q0), scale by D or transform by
-  // G per quadrature point, contract back (q0 -> i0), in place in B.
-  static __device__ __forceinline__ void pass3(const CellParams<T>& p,
-                                               T* __restrict__ w, int ncb,
-                                               const T* __restrict__ geo,
-                                               long long geo_cell0)
-  {
-    T* B0 = w + ncb * S::nA * S::SA;
-    T* B1 = B0 + ncb * S::SB;
-    T* B2 = B1 + ncb * S::SB;
-    const int np = ncb * Q * Q;
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
-    {
-      const int c = t / (Q * Q), r = t - c * (Q * Q);
-      const int ib = c * S::SB + r;
-      // geometry of this pencil: point (q0, r) at (c*Q3 + q0*Q*Q + r)*NC
-      const T* g = geo + ((long long)(geo_cell0 + c) * S::Q3 + r) * S::NC;
-      if constexpr (OP == OP_MASS)
-      {
-        T x[N], v[Q], o[N];
-#pragma unroll
-        for (int k = 0; k < N; ++k)
-          x[k] = B0[ib + k * Q * Q];
-        mv<Q, N, FSM, FSK>(p.tab[0], x, v);
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-          v[q] *= g[q * Q * Q];
-        mv<N, Q, BSM, BSK>(p.tab[0], v, o);
-#pragma unroll
-        for (int k = 0; k < N; ++k)
-          B0[ib + k * Q * Q] = o[k];
-      }
-      else
-      {
-        T xa[N], xg[N], fx[Q], fy[Q], fz[Q];
-#pragma unroll
-        for (int k = 0; k < N; ++k)
-        {
-          xa[k] = B0[ib + k * Q * Q];
-          xg[k] = B1[ib + k * Q * Q];
-        }
-        mv<Q, N, FSM, FSK>(p.tab[1], xa, fx); // d/dx: Gamma on axis 0
-        mv<Q, N, FSM, FSK>(p.tab[0], xg, fy); // d/dy: Gamma was on axis 1
-        if constexpr (SEM == SEM_EXACT)
-        {
-          T xb[N];
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            xb[k] = B2[ib + k * Q * Q];
-          mv<Q, N, FSM, FSK>(p.tab[0], xb, fz); // d/dz: Gamma on axis 2
-        }
-        else
-        {
-          mv<Q, N, FSM, FSK>(p.tab[0], xa, fz); // reference: no derivative
-        }
-        // transform (src/stiffness.hpp:14-29): G = [zz,yz,xz,yy,xy,xx]
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-        {
-          const T* G = g + q * Q * Q * 6;
-          const T w0 = fx[q], w1 = fy[q], w2 = fz[q];
-          if constexpr (SEM == SEM_EXACT)
-          {
-            fx[q] = G[5] * w0 + G[4] * w1 + G[2] * w2;
-            fy[q] = G[4] * w0 + G[3] * w1 + G[1] * w2;
-          }
-          fz[q] = G[2] * w0 + G[1] * w1 + G[0] * w2;
-        }
-        T o[N];
-        if constexpr (SEM == SEM_EXACT)
-        {
-          mv<N, Q, BSM, BSK>(p.tab[1], fx, o);
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            B0[ib + k * Q * Q] = o[k];
-          mv<N, Q, BSM, BSK>(p.tab[0], fy, o);
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            B1[ib + k * Q * Q] = o[k];
-          mv<N, Q, BSM, BSK>(p.tab[0], fz, o);
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            B2[ib + k * Q * Q] = o[k];
-        }
-        else
-        {
-          // only the last chain (Phi, Phi, Gamma) survives; axis 0 is Phi
-          mv<N, Q, BSM, BSK>(p.tab[0], fz, o);
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            B0[ib + k * Q * Q] = o[k];
-        }
-      }
-    }
-  }
-
-  // Pass 4: backward axis 1 (q1 -> i1).  B[c][i0][q1][q2] -> A[c][i0][i1][q2]
-  static __device__ __forceinline__ void pass4(const CellParams<T>& p,
-                                               T* __restrict__ w, int ncb)
-  {
-    T* A0 = w;
-    T* A1 = w + ncb * S::SA;
-    const T* B0 = w + ncb * S::nA * S::SA;
-    const T* B1 = B0 + ncb * S::SB;
-    const T* B2 = B1 + ncb * S::SB;
-    const int np = ncb * N * Q;
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
-    {
-      const int c = t / (N * Q), r = t - c * (N * Q);
-      const int i0 = r / Q, q2 = r - i0 * Q;
-      const int ia = c * S::SA + i0 * N * S::QP + q2;
-      const int ib = c * S::SB + i0 * Q * Q + q2;
-      T x[Q], o[N];
-#pragma unroll
-      for (int q = 0; q < Q; ++q)
-        x[q] = B0[ib + q * Q];
-      if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
-      {
-        // U1 = Phi^T X + Gamma^T Y ; U2 = Phi^T Z
-        mv<N, Q, BSM, BSK>(p.tab[0], x, o);
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-          x[q] = B1[ib + q * Q];
-        mv_acc<N, Q, BSM, BSK>(p.tab[1], x, o);
-#pragma unroll
-        for (int k = 0; k < N; ++k)
-          A0[ia + k * S::QP] = o[k];
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-          x[q] = B2[ib + q * Q];
-        mv<N, Q, BSM, BSK>(p.tab[0], x, o);
-#pragma unroll
-        for (int k = 0; k < N; ++k)
-          A1[ia + k * S::QP] = o[k];
-      }
-      else
-      {
-        mv<N, Q, BSM, BSK>(p.tab[0], x, o);
-#pragma unroll
-        for (int k = 0; k < N; ++k)
-          A0[ia + k * S::QP] = o[k];
-      }
-    }
-  }
-
-  // Pass 5: backward axis 2 (q2 -> i2).  A[c][i0][i1][q2] -> y[c][i0][i1][i2]
-  static __device__ __forceinline__ void pass5(const CellParams<T>& p,
-                                               const T* __restrict__ w,
-                                               T* __restrict__ sy, int ncb)
-  {
-    const T* A0 = w;
-    const T* A1 = w + ncb * S::SA;
-    const int np = ncb * N * N;
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
-    {
-      const int c = t / (N * N), r = t - c * (N * N);
-      const int ia = c * S::SA + r * S::QP;
-      T x[Q], o[N];
-#pragma unroll
-      for (int q = 0; q < Q; ++q)
-        x[q] = A0[ia + q];
-      if constexpr (OP == OP_MASS)
-      {
-        mv<N, Q, BSM, BSK>(p.tab[0], x, o);
-      }
-      else if constexpr (SEM == SEM_EXACT)
-      {
-        mv<N, Q, BSM, BSK>(p.tab[0], x, o);
-#pragma unroll
-        for (int q = 0; q < Q; ++q)
-          x[q] = A1[ia + q];
-        mv_acc<N, Q, BSM, BSK>(p.tab[1], x, o);
-      }
-      else
-      {
-        mv<N, Q, BSM, BSK>(p.tab[1], x, o); // reference: Gamma on axis 2
-      }
-      T* dst = sy + c * S::N3 + r * N;
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        dst[k] = o[k];
-    }
-  }
-};
-
-// The streaming main loop shared by every kernel family: persistent CTAs,
-// two TMA stages, five passes per tile, TMA bulk store of the result.
-// `Tile` provides the Shape `S` and the static passes pass1..pass5.
-template <typename T, typename Tile>
+template <typename T, typename Tile, int N, int Q, int NC>
 __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
 {
-  using S = typename Tile::S;
+  constexpr int N2 = N * N, N3 = N * N * N, Q3NC = Q * Q * Q * NC;
+  constexpr int US = Tile::US;
   extern __shared__ __align__(128) unsigned char smem[];
   const int cb = p.cb;
   const bool staged = p.geo_staged != 0;
   const long long ntiles = (p.ncells + cb - 1) / cb;
-  const CellLayout L(cb, (int)sizeof(T), S::N3, S::Q3 * S::NC, S::work,
-                     p.geo_staged);
+  const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   // stage s buffers (selected arithmetically: no local-memory arrays)
   auto su = [&](int s) { return reinterpret_cast<T*>(smem + (s ? L.u1 : L.u0)); };
   auto sg = [&](int s) { return reinterpret_cast<T*>(smem + (s ? L.g1 : L.g0)); };
   T* sy = reinterpret_cast<T*>(smem + L.y);
   T* sw = reinterpret_cast<T*>(smem + L.w);
-  const unsigned bu = (unsigned)cb * S::N3 * sizeof(T);
-  const unsigned bg = staged ? (unsigned)cb * S::Q3 * S::NC * sizeof(T) : 0u;
+  const unsigned bslab = N2 * sizeof(T);
+  const unsigned bu = (unsigned)cb * N3 * sizeof(T);
+  const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(T) : 0u;
+  const int lane = threadIdx.x & 31;
+  const bool warp0 = threadIdx.x < 32;
+  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc};
 
   if (threadIdx.x == 0)
   {
@@ -438,23 +207,35 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   __syncthreads();
 
   auto is_full = [&](long long t) { return (t + 1) * cb <= p.ncells; };
+  // warp 0 only: TMA loads of tile t into stage s
   auto issue = [&](long long t, int s) {
-    fence_proxy_async_smem();
-    mbar_arrive_expect_tx(&bar[s], bu + bg);
-    bulk_g2s(su(s), p.u + t * cb * S::N3, bu, &bar[s]);
-    if (staged)
-      bulk_g2s(sg(s), p.geo + t * cb * S::Q3 * S::NC, bg, &bar[s]);
+    if (lane == 0)
+    {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[s], bu + bg);
+      if (staged)
+        bulk_g2s(sg(s), p.geo + t * cb * Q3NC, bg, &bar[s]);
+      if constexpr (!Tile::kSlabCopies)
+        bulk_g2s(su(s), p.u + t * cb * N3, bu, &bar[s]);
+    }
+    if constexpr (Tile::kSlabCopies)
+    {
+      __syncwarp();
+      const long long slab0 = t * cb * N;
+      for (int k = lane; k < cb * N; k += 32)
+        bulk_g2s(su(s) + k * US, p.u + (slab0 + k) * N2, bslab, &bar[s]);
+    }
   };
 
   long long tile = blockIdx.x;
-  if (threadIdx.x == 0 && tile < ntiles && is_full(tile))
+  if (warp0 && tile < ntiles && is_full(tile))
     issue(tile, 0);
 
   for (int it = 0; tile < ntiles; tile += gridDim.x, ++it)
   {
     const int s = it & 1;
     const long long next = tile + gridDim.x;
-    if (threadIdx.x == 0 && next < ntiles && is_full(next))
+    if (warp0 && next < ntiles && is_full(next))
       issue(next, s ^ 1);
     const bool full = is_full(tile);
     const int ncb = full ? cb : (int)(p.ncells - tile * cb);
@@ -465,14 +246,14 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     }
     else
     {
-      // ragged last tile: plain coalesced loads into the same stage
-      const long long u0 = tile * cb * S::N3;
-      for (int i = threadIdx.x; i < ncb * S::N3; i += blockDim.x)
-        su(s)[i] = p.u[u0 + i];
+      // ragged last tile: plain coalesced loads into the same stage layout
+      const long long u0 = tile * cb * N3;
+      for (int i = threadIdx.x; i < ncb * N3; i += blockDim.x)
+        su(s)[(i / N2) * US + (i % N2)] = p.u[u0 + i];
       if (staged)
       {
-        const long long g0 = tile * cb * S::Q3 * S::NC;
-        for (int i = threadIdx.x; i < ncb * S::Q3 * S::NC; i += blockDim.x)
+        const long long g0 = tile * cb * Q3NC;
+        for (int i = threadIdx.x; i < ncb * Q3NC; i += blockDim.x)
           sg(s)[i] = p.geo[g0 + i];
       }
     }
@@ -482,47 +263,413 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
         record_fault(FAULT_MBAR_TIMEOUT);
       break;
     }
-    Tile::pass1(p, su(s), sw, ncb);
-    __syncthreads();
-    Tile::pass2(p, sw, ncb);
+    Tile::forward(tv, su(s), sw, ncb);
     __syncthreads();
     if (staged)
-      Tile::pass3(p, sw, ncb, sg(s), 0);
+      Tile::fused(tv, sw, ncb, sg(s), 0);
     else
-      Tile::pass3(p, sw, ncb, p.geo, tile * cb);
+      Tile::fused(tv, sw, ncb, p.geo, tile * cb);
+    if (warp0)
+      bulk_wait_read0(); // the previous tile's stores have left sy
     __syncthreads();
-    Tile::pass4(p, sw, ncb);
-    if (threadIdx.x == 0)
-      bulk_wait_read0(); // previous tile's store has left sy
-    __syncthreads();
-    Tile::pass5(p, sw, sy, ncb);
+    Tile::backward(tv, sw, sy, ncb);
     if (full)
     {
       fence_proxy_async_smem();
       __syncthreads();
-      if (threadIdx.x == 0)
+      if constexpr (!Tile::kSlabCopies)
       {
-        bulk_s2g(p.y + tile * cb * S::N3, sy, bu);
+        if (threadIdx.x == 0)
+        {
+          bulk_s2g(p.y + tile * cb * N3, sy, bu);
+          bulk_commit();
+        }
+      }
+      else if (warp0)
+      {
+        const long long slab0 = tile * cb * N;
+        for (int k = lane; k < cb * N; k += 32)
+          bulk_s2g(p.y + (slab0 + k) * N2, sy + k * US, bslab);
         bulk_commit();
       }
     }
     else
     {
       __syncthreads();
-      const long long y0 = tile * cb * S::N3;
-      for (int i = threadIdx.x; i < ncb * S::N3; i += blockDim.x)
-        p.y[y0 + i] = sy[i];
+      const long long y0 = tile * cb * N3;
+      for (int i = threadIdx.x; i < ncb * N3; i += blockDim.x)
+        p.y[y0 + i] = sy[(i / N2) * US + (i % N2)];
     }
   }
-  if (threadIdx.x == 0)
+  if (warp0)
     bulk_wait0();
 }
+
+// ---------------------------------------------------------------------------
+// CUDA-core tile: slab-merged sum factorization.
+//   forward  : one thread per (cell, i0) slab holds u[c][i0][:][:] in
+//              registers and contracts axis 2 and axis 1 there, writing
+//              B[c][i0][q1][q2] (one column q2 at a time, so the live set is
+//              the slab plus two columns);
+//   fused    : one thread per (cell, q1, q2) pencil contracts axis 0, applies
+//              D or the G transform per point, contracts back;
+//   backward : one thread per slab contracts axes 1 and 2 back in registers
+//              and writes y[c][i0][:][:].
+// Only the fused pass exchanges data across threads, through the B buffers,
+// whose slab and cell strides (p.sq, p.sbc) are chosen on the host to keep
+// both access patterns free of shared-memory bank conflicts.
+// ---------------------------------------------------------------------------
+// S lanes share one slab (consecutive lanes of a warp): lane s of the group
+// takes the q2 columns s, s+S, ...; the slab loads are shared-memory
+// broadcasts, and the backward partial sums are reduced with shuffles.
+template <typename T>
+__host__ __device__ constexpr int slab_lanes()
+{
+  return sizeof(T) == 4 ? 2 : 1; // FP32: more busy lanes; FP64: pipe-bound
+}
+
+template <typename T, int N, int Q, int OP, int SEM>
+struct SlabTile
+{
+  static constexpr int S = slab_lanes<T>();
+  static constexpr bool kSlabCopies = (N % 2 == 0);
+  static constexpr int US = slab_stride<T>(N);
+  static constexpr int N2 = N * N, Q2 = Q * Q, Q3 = Q * Q * Q;
+  static constexpr int NBUF =
+      (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
+  // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
+  // reference A(i,q) = tab[i + q*Q] (the forward table reused, Q == N)
+  static constexpr int BSM = (SEM == SEM_EXACT) ? Q : 1;
+  static constexpr int BSK = (SEM == SEM_EXACT) ? 1 : Q;
+  static constexpr int QS = (Q + S - 1) / S; // q2 columns per lane (max)
+  // unroll the q2 loop only while the unrolled body stays small
+  static constexpr int UNR = (N * N * QS * NBUF <= 1200) ? QS : 1;
+
+  static __host__ __device__ unsigned work_bytes(const CellParams<T>& p)
+  {
+    return (unsigned)NBUF * p.cb * p.sbc * sizeof(T);
+  }
+
+  static __device__ __forceinline__ void load_slab(const T* __restrict__ src,
+                                                   T (&x)[N2])
+  {
+    if constexpr (kSlabCopies)
+    {
+      using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+      constexpr int W = 16 / sizeof(T);
+#pragma unroll
+      for (int k = 0; k < N2 / W; ++k)
+      {
+        const V v = reinterpret_cast<const V*>(src)[k];
+        const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          x[k * W + j] = e[j];
+      }
+    }
+    else
+    {
+#pragma unroll
+      for (int k = 0; k < N2; ++k)
+        x[k] = src[k];
+    }
+  }
+
+  static __device__ __forceinline__ void store_slab(T* __restrict__ dst,
+                                                    const T (&x)[N2])
+  {
+    if constexpr (kSlabCopies)
+    {
+      using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+      constexpr int W = 16 / sizeof(T);
+#pragma unroll
+      for (int k = 0; k < N2 / W; ++k)
+      {
+        V v;
+        T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          e[j] = x[k * W + j];
+        reinterpret_cast<V*>(dst)[k] = v;
+      }
+    }
+    else
+    {
+#pragma unroll
+      for (int k = 0; k < N2; ++k)
+        dst[k] = x[k];
+    }
+  }
+
+  static __device__ __forceinline__ void forward(const TabView<T>& p,
+                                                 const T* __restrict__ su,
+                                                 T* __restrict__ sw, int ncb)
+  {
+    const T* __restrict__ P = p.P;
+    const T* __restrict__ D = p.D;
+    const int ns = ncb * N * S, bstride = ncb * p.sbc;
+    for (int ts = threadIdx.x; ts < ns; ts += blockDim.x)
+    {
+      const int sl = ts / S, lane_s = ts - sl * S;
+      const int c = sl / N, i0 = sl - c * N;
+      T x[N2];
+      load_slab(su + sl * US, x);
+      T* b0 = sw + c * p.sbc + i0 * p.sq;
+      T* b1 = b0 + bstride;
+      T* b2 = b1 + bstride;
+#pragma unroll UNR
+      for (int jq = 0; jq < QS; ++jq)
+      {
+        const int q2 = lane_s + jq * S;
+        if (S > 1 && q2 >= Q)
+          break;
+        T a[N], g[N];
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          T acc = P[q2] * x[i1 * N];
+#pragma unroll
+          for (int i2 = 1; i2 < N; ++i2)
+            acc = fma(P[q2 + i2 * Q], x[i1 * N + i2], acc);
+          a[i1] = acc;
+          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          {
+            T gcc = D[q2] * x[i1 * N];
+#pragma unroll
+            for (int i2 = 1; i2 < N; ++i2)
+              gcc = fma(D[q2 + i2 * Q], x[i1 * N + i2], gcc);
+            g[i1] = gcc;
+          }
+        }
+#pragma unroll
+        for (int q1 = 0; q1 < Q; ++q1)
+        {
+          T o0 = P[q1] * a[0];
+#pragma unroll
+          for (int i1 = 1; i1 < N; ++i1)
+            o0 = fma(P[q1 + i1 * Q], a[i1], o0);
+          b0[q1 * Q + q2] = o0; // AA = Phi_1 Phi_2 u
+          if constexpr (OP == OP_STIFFNESS)
+          {
+            T o1 = D[q1] * a[0];
+#pragma unroll
+            for (int i1 = 1; i1 < N; ++i1)
+              o1 = fma(D[q1 + i1 * Q], a[i1], o1);
+            b1[q1 * Q + q2] = o1; // AG = Gamma_1 Phi_2 u
+            if constexpr (SEM == SEM_EXACT)
+            {
+              T o2 = P[q1] * g[0];
+#pragma unroll
+              for (int i1 = 1; i1 < N; ++i1)
+                o2 = fma(P[q1 + i1 * Q], g[i1], o2);
+              b2[q1 * Q + q2] = o2; // BA = Phi_1 Gamma_2 u
+            }
+          }
+        }
+      }
+    }
+  }
+
+  static __device__ __forceinline__ void fused(const TabView<T>& p,
+                                               T* __restrict__ sw, int ncb,
+                                               const T* __restrict__ geo,
+                                               long long geo_cell0)
+  {
+    const T* __restrict__ P = p.P;
+    const T* __restrict__ D = p.D;
+    const int np = ncb * Q2, bstride = ncb * p.sbc;
+    for (int t = threadIdx.x; t < np; t += blockDim.x)
+    {
+      const int c = t / Q2, r = t - c * Q2;
+      T* b0 = sw + c * p.sbc + r;
+      T* b1 = b0 + bstride;
+      T* b2 = b1 + bstride;
+      const int sq = p.sq;
+      if constexpr (OP == OP_MASS)
+      {
+        const T* dw = geo + (geo_cell0 + c) * Q3 + r;
+        T x[N], v[Q];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          x[k] = b0[k * sq];
+        mv<Q, N, 1, Q>(P, x, v);
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+          v[q] *= dw[q * Q2];
+        mv<N, Q, BSM, BSK>(P, v, x);
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          b0[k * sq] = x[k];
+      }
+      else
+      {
+        const T* G = geo + ((geo_cell0 + c) * Q3 + r) * 6;
+        T xa[N], xg[N], fx[Q], fy[Q], fz[Q];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+        {
+          xa[k] = b0[k * sq];
+          xg[k] = b1[k * sq];
+        }
+        mv<Q, N, 1, Q>(D, xa, fx); // d/dx: Gamma on axis 0
+        mv<Q, N, 1, Q>(P, xg, fy); // d/dy: Gamma was applied on axis 1
+        if constexpr (SEM == SEM_EXACT)
+        {
+          T xb[N];
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            xb[k] = b2[k * sq];
+          mv<Q, N, 1, Q>(P, xb, fz); // d/dz: Gamma was applied on axis 2
+        }
+        else
+        {
+          mv<Q, N, 1, Q>(P, xa, fz); // reference: W_z carries no derivative
+        }
+        // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx], read
+        // as three 8/16-byte pairs
+        using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+        {
+          const V2* g2 = reinterpret_cast<const V2*>(G + (long long)q * Q2 * 6);
+          const V2 g01 = g2[0], g23 = g2[1], g45 = g2[2];
+          const T zz = g01.x, yz = g01.y, xz = g23.x, yy = g23.y, xy = g45.x,
+                  xx = g45.y;
+          const T w0 = fx[q], w1 = fy[q], w2 = fz[q];
+          if constexpr (SEM == SEM_EXACT)
+          {
+            fx[q] = xx * w0 + xy * w1 + xz * w2;
+            fy[q] = xy * w0 + yy * w1 + yz * w2;
+          }
+          fz[q] = xz * w0 + yz * w1 + zz * w2;
+        }
+        T o[N];
+        if constexpr (SEM == SEM_EXACT)
+        {
+          mv<N, Q, BSM, BSK>(D, fx, o);
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            b0[k * sq] = o[k];
+          mv<N, Q, BSM, BSK>(P, fy, o);
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            b1[k * sq] = o[k];
+          mv<N, Q, BSM, BSK>(P, fz, o);
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            b2[k * sq] = o[k];
+        }
+        else
+        {
+          mv<N, Q, BSM, BSK>(P, fz, o); // (Phi, Phi, Gamma): axis 0 is Phi
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            b0[k * sq] = o[k];
+        }
+      }
+    }
+  }
+
+  static __device__ __forceinline__ void backward(const TabView<T>& p,
+                                                  const T* __restrict__ sw,
+                                                  T* __restrict__ sy, int ncb)
+  {
+    const T* __restrict__ P = p.P;
+    const T* __restrict__ D = p.D;
+    // every lane of a warp takes part in the shuffle reduction, so the loop
+    // runs to a bound that is a multiple of the CTA size
+    const int ns = ncb * N * S, bstride = ncb * p.sbc;
+    const int nsr = (ns + blockDim.x - 1) / blockDim.x * blockDim.x;
+    for (int ts = threadIdx.x; ts < nsr; ts += blockDim.x)
+    {
+      const bool live = ts < ns;
+      const int sl = live ? ts / S : 0, lane_s = ts - (ts / S) * S;
+      const int c = sl / N, i0 = sl - c * N;
+      const T* b0 = sw + c * p.sbc + i0 * p.sq;
+      const T* b1 = b0 + bstride;
+      const T* b2 = b1 + bstride;
+      T y[N2];
+#pragma unroll
+      for (int k = 0; k < N2; ++k)
+        y[k] = T(0);
+#pragma unroll UNR
+      for (int jq = 0; jq < QS; ++jq)
+      {
+        const int q2 = lane_s + jq * S;
+        if (!live || (S > 1 && q2 >= Q))
+          break;
+        T X[Q], Y[Q], Z[Q], U1[N], U2[N];
+#pragma unroll
+        for (int q1 = 0; q1 < Q; ++q1)
+        {
+          X[q1] = b0[q1 * Q + q2];
+          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          {
+            Y[q1] = b1[q1 * Q + q2];
+            Z[q1] = b2[q1 * Q + q2];
+          }
+        }
+        // axis 1 back (q1 -> i1)
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          T acc = P[i1 * BSM] * X[0];
+#pragma unroll
+          for (int q1 = 1; q1 < Q; ++q1)
+            acc = fma(P[i1 * BSM + q1 * BSK], X[q1], acc);
+          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          {
+#pragma unroll
+            for (int q1 = 0; q1 < Q; ++q1)
+              acc = fma(D[i1 * BSM + q1 * BSK], Y[q1], acc);
+            T acc2 = P[i1 * BSM] * Z[0];
+#pragma unroll
+            for (int q1 = 1; q1 < Q; ++q1)
+              acc2 = fma(P[i1 * BSM + q1 * BSK], Z[q1], acc2);
+            U2[i1] = acc2;
+          }
+          U1[i1] = acc;
+        }
+        // axis 2 back (q2 -> i2), accumulated over q2
+        const T* T2 = (OP == OP_STIFFNESS && SEM == SEM_REFERENCE) ? D : P;
+#pragma unroll
+        for (int i2 = 0; i2 < N; ++i2)
+        {
+          const T t1 = T2[i2 * BSM + q2 * BSK];
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+            y[i1 * N + i2] = fma(t1, U1[i1], y[i1 * N + i2]);
+          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          {
+            const T t2 = D[i2 * BSM + q2 * BSK];
+#pragma unroll
+            for (int i1 = 0; i1 < N; ++i1)
+              y[i1 * N + i2] = fma(t2, U2[i1], y[i1 * N + i2]);
+          }
+        }
+      }
+      if constexpr (S > 1)
+      {
+#pragma unroll
+        for (int k = 0; k < N2; ++k)
+        {
+#pragma unroll
+          for (int o = 1; o < S; o <<= 1)
+            y[k] += __shfl_xor_sync(0xffffffffu, y[k], o);
+        }
+      }
+      // the S lanes of a slab hold the same sums: the store is one write
+      if (live)
+        store_slab(sy + sl * US, y);
+    }
+  }
+};
 
 template <typename T, int N, int Q, int OP, int SEM>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  stream_tiles<T, CellTile<T, N, Q, OP, SEM>>(p);
+  stream_tiles<T, SlabTile<T, N, Q, OP, SEM>, N, Q, (OP == OP_MASS) ? 1 : 6>(p);
 }
 
 } // namespace femtc

@@ -76,60 +76,220 @@ const CellVariant* find_cell(int op, int dtype, int sem, int n, int q)
 // ---------------------------------------------------------------- tiles --
 using Key = std::tuple<int, int, int, int, int>; // op dtype sem n q
 std::mutex g_cfg_mutex;
-std::map<Key, std::pair<int, int>> g_tile_cfg; // -> (cb, staged)
+struct TileChoice
+{
+  int cb, staged, nt;
+};
+std::map<Key, TileChoice> g_tile_cfg;
+
+
 
 constexpr unsigned kSmemPerSmTarget = 113 * 1024; // 2 CTAs per SM
 
-// Lane efficiency of a tile of `cb` cells: useful pencil slots over issued
-// slots across the five passes, each weighted by its FMAs per pencil.
-double lane_efficiency(int n, int q, int cb)
+// Shared-memory wavefronts of one warp-wide access of `esize`-byte elements
+// at element indices a[0..31]: 32 four-byte banks; 8-byte accesses are
+// served per half warp (16 x 8 bytes = one 128-byte wavefront when the
+// element indices are distinct modulo 16).
+int wavefronts(const long long* a, int esize)
 {
-  const double np[5] = {double(n * n), double(n * q), double(q * q),
-                        double(n * q), double(n * n)};
-  const double wk[5] = {double(n * q), double(n * q), double(2 * n * q),
-                        double(n * q), double(n * q)};
-  double useful = 0, issued = 0;
-  for (int i = 0; i < 5; ++i)
+  if (esize == 4)
   {
-    const double p = np[i] * cb;
-    const double slots = std::ceil(p / kCellThreads) * kCellThreads;
-    useful += p * wk[i];
+    int worst = 0;
+    for (int b = 0; b < 32; ++b)
+    {
+      long long seen[32];
+      int n = 0;
+      for (int t = 0; t < 32; ++t)
+        if (((a[t] % 32) + 32) % 32 == b)
+        {
+          bool dup = false;
+          for (int k = 0; k < n; ++k)
+            dup = dup || seen[k] == a[t];
+          if (!dup)
+            seen[n++] = a[t];
+        }
+      worst = std::max(worst, n);
+    }
+    return worst;
+  }
+  int total = 0;
+  for (int h = 0; h < 2; ++h)
+  {
+    int worst = 0;
+    for (int b = 0; b < 16; ++b)
+    {
+      long long seen[16];
+      int n = 0;
+      for (int t = 16 * h; t < 16 * h + 16; ++t)
+        if (((a[t] % 16) + 16) % 16 == b)
+        {
+          bool dup = false;
+          for (int k = 0; k < n; ++k)
+            dup = dup || seen[k] == a[t];
+          if (!dup)
+            seen[n++] = a[t];
+        }
+      worst = std::max(worst, n);
+    }
+    total += worst;
+  }
+  return total;
+}
+
+// Strides of the slab kernels' work buffers: a slab (c, i0) starts at
+// c*sbc + i0*sq.  The forward/backward passes access them with one thread per
+// slab (addresses c*sbc + i0*sq + const), the fused pass with one thread per
+// pencil (c, r) (addresses c*sbc + r + const).  Pick the strides that
+// minimise the modelled bank-conflict wavefronts of both patterns.
+std::pair<int, int> slab_layout(int n, int q, int esize)
+{
+  const int lanes = esize == 4 ? 2 : 1; // lanes per slab (slab_lanes<T>())
+  static std::mutex m;
+  static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;
+  std::lock_guard<std::mutex> lk(m);
+  auto key = std::make_tuple(n, q, esize);
+  auto it = cache.find(key);
+  if (it != cache.end())
+    return it->second;
+  const int q2 = q * q;
+  double best = 1e30;
+  std::pair<int, int> res{q2, n * q2};
+  long long a[32];
+  for (int sq = q2; sq < q2 + 32; ++sq)
+    for (int sbc = n * sq; sbc < n * sq + 32; ++sbc)
+    {
+      double cost = 0.0;
+      for (int mm = 0; mm < n; ++mm)
+      {
+        for (int t = 0; t < 32; ++t)
+        {
+          const long long ts = 32LL * mm + t, sl = ts / lanes;
+          a[t] = (sl / n) * sbc + (sl % n) * sq + ts % lanes;
+        }
+        cost += double(wavefronts(a, esize)) / n;
+      }
+      for (int mm = 0; mm < q2; ++mm)
+      {
+        for (int t = 0; t < 32; ++t)
+        {
+          const long long pp = 32LL * mm + t;
+          a[t] = (pp / q2) * sbc + pp % q2;
+        }
+        cost += double(wavefronts(a, esize)) / q2;
+      }
+      cost += 1e-6 * sbc; // then the smaller footprint
+      if (cost < best)
+      {
+        best = cost;
+        res = {sq, sbc};
+      }
+    }
+  cache[key] = res;
+  return res;
+}
+
+// Lane efficiency of a tile of `cb` cells: useful thread slots over issued
+// slots across the passes, each weighted by its FMAs per work item.
+double lane_efficiency(const CellVariant& v, int cb, int nt)
+{
+  const double n = v.n, q = v.q;
+  double np[5], wk[5];
+  int passes;
+  if (v.slab)
+  {
+    passes = 3; // slabs forward, pencils fused, slabs backward
+    const double lanes = v.esize == 4 ? 2 : 1;
+    np[0] = n * cb * lanes; wk[0] = q * n * (n + q) / lanes;
+    np[1] = q * q * cb;     wk[1] = 2 * q * n;
+    np[2] = n * cb * lanes; wk[2] = q * n * (n + q) / lanes;
+  }
+  else
+  {
+    passes = 5; // 16-pencil MMA blocks per warp
+    const double rows[5] = {n * n, n * q, q * q, n * q, n * n};
+    for (int i = 0; i < 5; ++i)
+    {
+      np[i] = std::ceil(rows[i] * cb / 16.0) * 32.0;
+      wk[i] = 1.0;
+    }
+  }
+  double useful = 0, issued = 0;
+  for (int i = 0; i < passes; ++i)
+  {
+    const double slots = std::ceil(np[i] / nt) * nt;
+    useful += np[i] * wk[i];
     issued += slots * wk[i];
   }
   return useful / issued;
 }
 
-std::pair<int, int> default_tile(const CellVariant& v)
+struct TileCfg
 {
-  int best_cb = 4, best_staged = 0;
-  double best = -1.0;
-  for (int staged = 1; staged >= 0; --staged)
+  int cb, staged, nt, sq, sbc;
+};
+
+TileCfg with_layout(const CellVariant& v, int cb, int staged, int nt)
+{
+  TileCfg c{cb, staged, nt, 0, 0};
+  if (v.slab)
   {
-    for (int cb = 4; cb <= 64; cb += 4)
+    auto l = slab_layout(v.n, v.q, v.esize);
+    c.sq = l.first;
+    c.sbc = l.second;
+  }
+  return c;
+}
+
+unsigned smem_of(const CellVariant& v, const TileCfg& c)
+{
+  return v.smem(c.cb, c.staged, c.sq, c.sbc);
+}
+
+// Built-in tile heuristic (the autotuner replaces it per variant).
+// Slab kernels: geometry read in the fused pass (its slab per cell is large
+// and used once), threads per CTA and cells per tile chosen to fill the
+// lanes of all three passes within ~113 KB (two CTAs per SM).  Tensor-core
+// kernels: 256 threads, geometry staged by TMA where it fits.
+TileCfg default_tile(const CellVariant& v)
+{
+  TileCfg best_cfg = with_layout(v, 4, 0, kCellThreads);
+  double best = -1.0;
+  const int stage_order[2] = {v.slab ? 0 : 1, v.slab ? 1 : 0};
+  for (int si = 0; si < 2; ++si)
+  {
+    const int staged = stage_order[si];
+    for (int nt : {128, 256})
     {
-      if (v.smem(cb, staged) > kSmemPerSmTarget)
-        break;
-      // prefer filled lanes, then larger tiles (fewer tile boundaries)
-      const double s = lane_efficiency(v.n, v.q, cb) + 1e-4 * cb;
-      if (s > best)
+      if (!v.slab && nt != kCellThreads)
+        continue;
+      for (int cb = 4; cb <= 128; cb += 4)
       {
-        best = s;
-        best_cb = cb;
-        best_staged = staged;
+        const TileCfg c = with_layout(v, cb, staged, nt);
+        if (smem_of(v, c) > kSmemPerSmTarget)
+          break;
+        // prefer filled lanes, then larger tiles (fewer tile boundaries)
+        const double sc = lane_efficiency(v, cb, nt) + 1e-4 * cb;
+        if (sc > best)
+        {
+          best = sc;
+          best_cfg = c;
+        }
       }
     }
     if (best > 0)
-      break; // staging fits: keep it
+      break;
   }
-  return {best_cb, best_staged};
+  return best_cfg;
 }
 
-std::pair<int, int> tile_config(const CellVariant& v)
+TileCfg tile_config(const CellVariant& v)
 {
-  std::lock_guard<std::mutex> lk(g_cfg_mutex);
-  auto it = g_tile_cfg.find(Key(v.op, v.dtype, v.sem, v.n, v.q));
-  if (it != g_tile_cfg.end())
-    return it->second;
+  {
+    std::lock_guard<std::mutex> lk(g_cfg_mutex);
+    auto it = g_tile_cfg.find(Key(v.op, v.dtype, v.sem, v.n, v.q));
+    if (it != g_tile_cfg.end())
+      return with_layout(v, it->second.cb, it->second.staged, it->second.nt);
+  }
   return default_tile(v);
 }
 
@@ -137,7 +297,7 @@ std::pair<int, int> tile_config(const CellVariant& v)
 struct FnState
 {
   int max_smem_set = 0;
-  std::map<unsigned, int> blocks_per_sm; // by dynamic smem
+  std::map<unsigned, int> blocks_per_sm; // by (dynamic smem, threads)
 };
 std::mutex g_fn_mutex;
 std::map<const void*, FnState> g_fn_state;
@@ -150,7 +310,7 @@ int sm_count()
   return n > 0 ? n : 1;
 }
 
-int prepare(const void* fn, unsigned smem, int* blocks)
+int prepare(const void* fn, unsigned smem, int nt, int* blocks)
 {
   std::lock_guard<std::mutex> lk(g_fn_mutex);
   FnState& st = g_fn_state[fn];
@@ -162,19 +322,20 @@ int prepare(const void* fn, unsigned smem, int* blocks)
       return cuda_fail(e, "cudaFuncSetAttribute");
     st.max_smem_set = (int)smem;
   }
-  auto it = st.blocks_per_sm.find(smem);
+  const unsigned key = smem * 1024u + (unsigned)nt;
+  auto it = st.blocks_per_sm.find(key);
   if (it == st.blocks_per_sm.end())
   {
     int nb = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &nb, fn, kCellThreads, smem);
+        &nb, fn, nt, smem);
     if (e != cudaSuccess)
       return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (nb < 1)
       return fail(FEMTC_ERR_UNSUPPORTED,
                   "kernel does not fit on an SM with %u B shared memory",
                   smem);
-    it = st.blocks_per_sm.emplace(smem, nb).first;
+    it = st.blocks_per_sm.emplace(key, nb).first;
   }
   *blocks = it->second;
   return FEMTC_OK;
@@ -217,29 +378,31 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
 }
 
 template <typename T>
-int launch_cell(const CellVariant& v, const T* tables, const void* u,
-                void* y, const void* geo, size_t ncells, cudaStream_t stream)
+int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
+                const void* u, void* y, const void* geo, size_t ncells,
+                cudaStream_t stream)
 {
   if (!aligned16(u) || !aligned16(y) || !aligned16(geo))
     return fail(FEMTC_ERR_INVALID,
                 "u, y and the geometry must be 16-byte aligned device "
                 "pointers (TMA bulk copies)");
-  const auto cfg = tile_config(v);
   CellParams<T> p;
   std::memset(&p, 0, sizeof(p));
   p.u = static_cast<const T*>(u);
   p.y = static_cast<T*>(y);
   p.geo = static_cast<const T*>(geo);
   p.ncells = (long long)ncells;
-  p.cb = cfg.first;
-  p.geo_staged = cfg.second;
+  p.cb = cfg.cb;
+  p.geo_staged = cfg.staged;
+  p.sq = cfg.sq;
+  p.sbc = cfg.sbc;
   const int ntab = (v.op == FEMTC_OP_STIFFNESS) ? 2 : 1;
   for (int t = 0; t < ntab; ++t)
     for (int i = 0; i < v.n * v.q; ++i)
       p.tab[t][i] = tables[t * v.n * v.q + i];
-  const unsigned smem = v.smem(p.cb, p.geo_staged);
+  const unsigned smem = smem_of(v, cfg);
   int blocks = 0;
-  int rc = prepare(v.fn, smem, &blocks);
+  int rc = prepare(v.fn, smem, cfg.nt, &blocks);
   if (rc != FEMTC_OK)
     return rc;
   const long long ntiles = ((long long)ncells + p.cb - 1) / p.cb;
@@ -247,10 +410,21 @@ int launch_cell(const CellVariant& v, const T* tables, const void* u,
       std::min<long long>(ntiles, (long long)blocks * sm_count());
   void* args[] = {&p};
   cudaError_t e = cudaLaunchKernel(v.fn, dim3((unsigned)grid),
-                                   dim3(kCellThreads), args, smem, stream);
+                                   dim3((unsigned)cfg.nt), args, smem, stream);
   if (e != cudaSuccess)
     return cuda_fail(e, "cudaLaunchKernel");
   return FEMTC_OK;
+}
+
+int launch_variant(const CellVariant& v, const TileCfg& cfg,
+                   const void* tables, const void* u, void* y,
+                   const void* geo, size_t ncells, cudaStream_t st)
+{
+  if (v.dtype == FEMTC_F64)
+    return launch_cell<double>(v, cfg, static_cast<const double*>(tables), u,
+                               y, geo, ncells, st);
+  return launch_cell<float>(v, cfg, static_cast<const float*>(tables), u, y,
+                            geo, ncells, st);
 }
 
 int apply(int op, int dtype, int sem, int degree, int nquad,
@@ -263,12 +437,8 @@ int apply(int op, int dtype, int sem, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return FEMTC_OK;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (dtype == FEMTC_F64)
-    return launch_cell<double>(*v, static_cast<const double*>(tables), u, y,
-                               geo, ncells, st);
-  return launch_cell<float>(*v, static_cast<const float*>(tables), u, y, geo,
-                            ncells, st);
+  return launch_variant(*v, tile_config(*v), tables, u, y, geo, ncells,
+                        static_cast<cudaStream_t>(stream));
 }
 
 size_t elem_size(int dtype) { return dtype == FEMTC_F64 ? 8 : 4; }
@@ -433,6 +603,8 @@ void gll_nodes(int p, double* x)
 }
 
 } // namespace
+
+int aux_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 } // namespace femtc
 
 using namespace femtc;
@@ -492,7 +664,7 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
 }
 
 int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int cb, int geo_staged)
+                          int nquad, int cb, int geo_staged, int threads)
 {
   const CellVariant* v = find_cell(op, dtype, semantics, degree + 1, nquad);
   if (!v)
@@ -506,24 +678,158 @@ int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
   }
   if (cb % 4 != 0 || cb > 256)
     return fail(FEMTC_ERR_INVALID, "cb must be a multiple of 4 in [4,256]");
-  if (v->smem(cb, geo_staged ? 1 : 0) > 227u * 1024u)
-    return fail(FEMTC_ERR_INVALID, "tile needs %u B of shared memory",
-                v->smem(cb, geo_staged ? 1 : 0));
-  g_tile_cfg[k] = {cb, geo_staged ? 1 : 0};
+  if (threads <= 0)
+    threads = kCellThreads;
+  if (threads % 32 != 0 || threads > kCellThreads)
+    return fail(FEMTC_ERR_INVALID, "threads must be a multiple of 32, <= %d",
+                kCellThreads);
+  const unsigned need =
+      smem_of(*v, with_layout(*v, cb, geo_staged ? 1 : 0, threads));
+  if (need > 227u * 1024u)
+    return fail(FEMTC_ERR_INVALID, "tile needs %u B of shared memory", need);
+  g_tile_cfg[k] = TileChoice{cb, geo_staged ? 1 : 0, threads};
   return FEMTC_OK;
 }
 
+int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
+                   const void* tables, const void* u, void* y,
+                   const void* geo, size_t ncells, void* stream, int* cb,
+                   int* geo_staged, int* threads, float* best_ms)
+{
+  const CellVariant* v = nullptr;
+  int rc = check_common(op, dtype, semantics, degree, nquad, tables, u, y,
+                        geo, &v);
+  if (rc != FEMTC_OK)
+    return rc;
+  if (ncells == 0)
+    return fail(FEMTC_ERR_INVALID, "autotune needs at least one cell");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // candidates: for each (staging, threads), the cell counts per tile with
+  // the best lane efficiency that fit in shared memory
+  std::vector<TileCfg> cands;
+  for (int staged = 0; staged <= 1; ++staged)
+    for (int nt : {64, 128, 256})
+    {
+      std::vector<std::pair<double, TileCfg>> opts;
+      for (int c = 4; c <= 128; c += 4)
+      {
+        const TileCfg t = with_layout(*v, c, staged, nt);
+        if (smem_of(*v, t) > 227u * 1024u)
+          break;
+        opts.push_back({lane_efficiency(*v, c, nt) + 1e-4 * c, t});
+      }
+      std::sort(opts.begin(), opts.end(),
+                [](const auto& a, const auto& b) { return a.first > b.first; });
+      for (size_t i = 0; i < opts.size() && i < 4; ++i)
+        cands.push_back(opts[i].second);
+    }
+  if (cands.empty())
+    return fail(FEMTC_ERR_UNSUPPORTED, "no tile shape fits in shared memory");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  TileCfg best_cfg = cands[0];
+  for (const TileCfg& c : cands)
+  {
+    rc = launch_variant(*v, c, tables, u, y, geo, ncells, st);
+    if (rc != FEMTC_OK)
+      continue; // e.g. does not fit on an SM with these registers
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 3; ++r)
+      launch_variant(*v, c, tables, u, y, geo, ncells, st);
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess)
+    {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return cuda_fail(e, "autotune");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= 3.f;
+    if (ms < best)
+    {
+      best = ms;
+      best_cfg = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best >= 1e30f)
+    return fail(FEMTC_ERR_UNSUPPORTED, "no tile candidate could be launched");
+  {
+    std::lock_guard<std::mutex> lk(g_cfg_mutex);
+    g_tile_cfg[Key(op, dtype, semantics, degree + 1, nquad)] =
+        TileChoice{best_cfg.cb, best_cfg.staged, best_cfg.nt};
+  }
+  if (cb)
+    *cb = best_cfg.cb;
+  if (geo_staged)
+    *geo_staged = best_cfg.staged;
+  if (threads)
+    *threads = best_cfg.nt;
+  if (best_ms)
+    *best_ms = best;
+  return FEMTC_OK;
+}
+
+int femtc_tile_db_save(const char* path)
+{
+  if (!path)
+    return fail(FEMTC_ERR_INVALID, "null path");
+  FILE* f = std::fopen(path, "w");
+  if (!f)
+    return fail(FEMTC_ERR_INVALID, "cannot open %s for writing", path);
+  std::lock_guard<std::mutex> lk(g_cfg_mutex);
+  std::fprintf(f, "# femtc tile db: op dtype semantics n q cb geo_staged threads\n");
+  for (const auto& kv : g_tile_cfg)
+    std::fprintf(f, "%d %d %d %d %d %d %d %d\n", std::get<0>(kv.first),
+                 std::get<1>(kv.first), std::get<2>(kv.first),
+                 std::get<3>(kv.first), std::get<4>(kv.first), kv.second.cb,
+                 kv.second.staged, kv.second.nt);
+  std::fclose(f);
+  return FEMTC_OK;
+}
+
+int femtc_tile_db_load(const char* path)
+{
+  if (!path)
+    return fail(FEMTC_ERR_INVALID, "null path");
+  FILE* f = std::fopen(path, "r");
+  if (!f)
+    return fail(FEMTC_ERR_INVALID, "cannot open %s", path);
+  char line[256];
+  int loaded = 0;
+  while (std::fgets(line, sizeof(line), f))
+  {
+    int op, dt, sem, n, q, cb, st, nt;
+    if (line[0] == '#')
+      continue;
+    if (std::sscanf(line, "%d %d %d %d %d %d %d %d", &op, &dt, &sem, &n, &q,
+                    &cb, &st, &nt) != 8)
+      continue;
+    if (femtc_set_tile_config(op, dt, sem, n - 1, q, cb, st, nt) == FEMTC_OK)
+      ++loaded;
+  }
+  std::fclose(f);
+  return loaded;
+}
+
 int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int* cb, int* geo_staged)
+                          int nquad, int* cb, int* geo_staged, int* threads)
 {
   const CellVariant* v = find_cell(op, dtype, semantics, degree + 1, nquad);
   if (!v)
     return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
-  const auto c = tile_config(*v);
+  const TileCfg c = tile_config(*v);
   if (cb)
-    *cb = c.first;
+    *cb = c.cb;
   if (geo_staged)
-    *geo_staged = c.second;
+    *geo_staged = c.staged;
+  if (threads)
+    *threads = c.nt;
   return FEMTC_OK;
 }
 

@@ -8,9 +8,14 @@
 namespace femtc
 {
 template <int SPLIT, int N, int Q, int OP>
-unsigned mma_smem_bytes(int cb, int staged)
+unsigned mma_smem_bytes(int cb, int staged, int, int)
 {
-  return make_layout<N, Q, OP, SEM_EXACT, float>(cb, staged).total;
+  CellParams<float> p{};
+  p.cb = cb;
+  p.geo_staged = staged;
+  return tile_layout<float, MmaTile<SPLIT, N, Q, OP>, N, Q,
+                     (OP == OP_MASS) ? 1 : 6>(p)
+      .total;
 }
 
 template <int SPLIT, int N, int Q, int OP>
@@ -18,7 +23,7 @@ void add_mma_variant(std::vector<CellVariant>& v, int dtype)
 {
   v.push_back(CellVariant{dtype, OP, SEM_EXACT, N, Q,
                           reinterpret_cast<const void*>(&mma_kernel<SPLIT, N, Q, OP>),
-                          &mma_smem_bytes<SPLIT, N, Q, OP>});
+                          &mma_smem_bytes<SPLIT, N, Q, OP>, 0, 4});
 }
 
 template <int SPLIT, int OP, int N>

@@ -358,9 +358,42 @@ struct MmaTile
 {
   using S = Shape<N, Q, OP, SEM_EXACT>;
   using T = float;
+  static constexpr bool kSlabCopies = false;
+  static constexpr int US = N * N;
+
+  static __host__ __device__ unsigned work_bytes(const CellParams<float>& p)
+  {
+    return (unsigned)p.cb * S::work * sizeof(float);
+  }
+
+  static __device__ __forceinline__ void forward(const TabView<float>& p,
+                                                 const float* __restrict__ su,
+                                                 float* __restrict__ w, int ncb)
+  {
+    pass1(p, su, w, ncb);
+    __syncthreads();
+    pass2(p, w, ncb);
+  }
+
+  static __device__ __forceinline__ void fused(const TabView<float>& p,
+                                               float* __restrict__ w, int ncb,
+                                               const float* __restrict__ geo,
+                                               long long geo_cell0)
+  {
+    pass3(p, w, ncb, geo, geo_cell0);
+    __syncthreads();
+    pass4(p, w, ncb);
+  }
+
+  static __device__ __forceinline__ void backward(const TabView<float>& p,
+                                                  const float* __restrict__ w,
+                                                  float* __restrict__ sy, int ncb)
+  {
+    pass5(p, w, sy, ncb);
+  }
 
   // Pass 1: axis 2, u[c][i0][i1][i2] -> A[c][i0][i1][q2]
-  static __device__ __forceinline__ void pass1(const CellParams<float>& p,
+  static __device__ __forceinline__ void pass1(const TabView<float>& p,
                                                const float* __restrict__ su,
                                                float* __restrict__ w, int ncb)
   {
@@ -370,18 +403,18 @@ struct MmaTile
     auto iidx = [](int r) { const int c = r / (N * N); return c * S::N3 + (r - c * (N * N)) * N; };
     auto oidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
     Table<SPLIT, N, Q, true, Q> phi;
-    phi.build(p.tab[0]);
+    phi.build(p.P);
     contract_pass<SPLIT, N, Q, true, Q>(su, phi, su, phi, iidx, 1, A0, oidx, 1, np);
     if constexpr (OP == OP_STIFFNESS)
     {
       Table<SPLIT, N, Q, true, Q> gam;
-      gam.build(p.tab[1]);
+      gam.build(p.D);
       contract_pass<SPLIT, N, Q, true, Q>(su, gam, su, gam, iidx, 1, A1, oidx, 1, np);
     }
   }
 
   // Pass 2: axis 1, A[c][i0][i1][q2] -> B[c][i0][q1][q2]
-  static __device__ __forceinline__ void pass2(const CellParams<float>& p,
+  static __device__ __forceinline__ void pass2(const TabView<float>& p,
                                                float* __restrict__ w, int ncb)
   {
     const float* A0 = w;
@@ -399,20 +432,20 @@ struct MmaTile
       return c * S::SB + i0 * Q * Q + q2;
     };
     Table<SPLIT, N, Q, true, Q> phi;
-    phi.build(p.tab[0]);
+    phi.build(p.P);
     contract_pass<SPLIT, N, Q, true, Q>(A0, phi, A0, phi, iidx, S::QP, B0, oidx, Q, np);
     if constexpr (OP == OP_STIFFNESS)
     {
       contract_pass<SPLIT, N, Q, true, Q>(A1, phi, A1, phi, iidx, S::QP, B2, oidx, Q, np);
       Table<SPLIT, N, Q, true, Q> gam;
-      gam.build(p.tab[1]);
+      gam.build(p.D);
       contract_pass<SPLIT, N, Q, true, Q>(A0, gam, A0, gam, iidx, S::QP, B1, oidx, Q, np);
     }
   }
 
   // Pass 3 (fused, registers only between the two MMAs): axis 0 forward,
   // D scaling / G transform, axis 0 backward; in place in B.
-  static __device__ __forceinline__ void pass3(const CellParams<float>& p,
+  static __device__ __forceinline__ void pass3(const TabView<float>& p,
                                                float* __restrict__ w, int ncb,
                                                const float* __restrict__ geo,
                                                long long geo_cell0)
@@ -427,8 +460,8 @@ struct MmaTile
     auto bidx = [](int r) { const int c = r / (Q * Q); return c * S::SB + (r - c * (Q * Q)); };
     Table<SPLIT, N, Q, true, Q> fphi;
     Table<SPLIT, Q, N, false, Q> bphi;
-    fphi.build(p.tab[0]);
-    bphi.build(p.tab[0]);
+    fphi.build(p.P);
+    bphi.build(p.P);
     for (int base = warp * 16; base < np; base += nwarps * 16)
     {
       const int r0 = base + g, r1 = base + g + 8;
@@ -476,7 +509,7 @@ struct MmaTile
       else
       {
         Table<SPLIT, N, Q, true, Q> fgam;
-        fgam.build(p.tab[1]);
+        fgam.build(p.D);
         float fx[NTQ][4], fy[NTQ][4], fz[NTQ][4];
         zero(fx);
         zero(fy);
@@ -533,7 +566,7 @@ struct MmaTile
             fz[j][e] = a2;
           }
         Table<SPLIT, Q, N, false, Q> bgam;
-        bgam.build(p.tab[1]);
+        bgam.build(p.D);
         backward_store<NTQ, NTN>(fx, bgam, B0, bidx, base, np);
         backward_store<NTQ, NTN>(fy, bphi, B1, bidx, base, np);
         backward_store<NTQ, NTN>(fz, bphi, B2, bidx, base, np);
@@ -581,7 +614,7 @@ struct MmaTile
   }
 
   // Pass 4: backward axis 1, B[c][i0][q1][q2] -> A[c][i0][i1][q2]
-  static __device__ __forceinline__ void pass4(const CellParams<float>& p,
+  static __device__ __forceinline__ void pass4(const TabView<float>& p,
                                                float* __restrict__ w, int ncb)
   {
     float* A0 = w;
@@ -599,7 +632,7 @@ struct MmaTile
       return c * S::SA + i0 * N * S::QP + q2;
     };
     Table<SPLIT, Q, N, false, Q> phi;
-    phi.build(p.tab[0]);
+    phi.build(p.P);
     if constexpr (OP == OP_MASS)
     {
       contract_pass<SPLIT, Q, N, false, Q>(B0, phi, B0, phi, iidx, Q, A0, oidx, S::QP, np);
@@ -607,7 +640,7 @@ struct MmaTile
     else
     {
       Table<SPLIT, Q, N, false, Q> gam;
-      gam.build(p.tab[1]);
+      gam.build(p.D);
       // U1 = Phi^T X + Gamma^T Y ; U2 = Phi^T Z
       contract_pass<SPLIT, Q, N, false, Q, true>(B0, phi, B1, gam, iidx, Q, A0, oidx, S::QP, np);
       contract_pass<SPLIT, Q, N, false, Q>(B2, phi, B2, phi, iidx, Q, A1, oidx, S::QP, np);
@@ -615,7 +648,7 @@ struct MmaTile
   }
 
   // Pass 5: backward axis 2, A[c][i0][i1][q2] -> y[c][i0][i1][i2]
-  static __device__ __forceinline__ void pass5(const CellParams<float>& p,
+  static __device__ __forceinline__ void pass5(const TabView<float>& p,
                                                const float* __restrict__ w,
                                                float* __restrict__ sy, int ncb)
   {
@@ -625,7 +658,7 @@ struct MmaTile
     auto iidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
     auto oidx = [](int r) { const int c = r / (N * N); return c * S::N3 + (r - c * (N * N)) * N; };
     Table<SPLIT, Q, N, false, Q> phi;
-    phi.build(p.tab[0]);
+    phi.build(p.P);
     if constexpr (OP == OP_MASS)
     {
       contract_pass<SPLIT, Q, N, false, Q>(A0, phi, A0, phi, iidx, 1, sy, oidx, 1, np);
@@ -633,7 +666,7 @@ struct MmaTile
     else
     {
       Table<SPLIT, Q, N, false, Q> gam;
-      gam.build(p.tab[1]);
+      gam.build(p.D);
       contract_pass<SPLIT, Q, N, false, Q, true>(A0, phi, A1, gam, iidx, 1, sy, oidx, 1, np);
     }
   }
@@ -643,7 +676,7 @@ template <int SPLIT, int N, int Q, int OP>
 __global__ void __launch_bounds__(kCellThreads)
     mma_kernel(const __grid_constant__ CellParams<float> p)
 {
-  stream_tiles<float, MmaTile<SPLIT, N, Q, OP>>(p);
+  stream_tiles<float, MmaTile<SPLIT, N, Q, OP>, N, Q, (OP == OP_MASS) ? 1 : 6>(p);
 }
 
 } // namespace femtc

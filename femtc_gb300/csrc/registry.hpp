@@ -16,7 +16,10 @@ struct CellVariant
   int sem;     // femtc_semantics
   int n, q;    // DOFs and quadrature points per axis
   const void* fn;
-  unsigned (*smem)(int cb, int staged); // dynamic shared memory, bytes
+  // dynamic shared memory (bytes) of a tile of cb cells
+  unsigned (*smem)(int cb, int staged, int sq, int sbc);
+  int slab;    // 1: slab-merged CUDA-core kernel (uses sq, sbc)
+  int esize;   // bytes per stored value
 };
 
 using FaultReader = unsigned (*)(); // returns and clears the unit's fault word

@@ -106,13 +106,60 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
                                int nquad, const void* tables, const void* u,
                                void* y, const void* G, size_t ncells);
 
-/* Tile shape used for a variant: cells per tile (multiple of 4) and whether
- * the geometry slab is staged through shared memory by TMA.  cb <= 0 restores
- * the built-in heuristic.  (The autotuner writes these.) */
+/* Tile shape of a variant: cells per tile cb (multiple of 4), whether the
+ * geometry slab is staged through shared memory by TMA, and threads per CTA
+ * (multiple of 32, at most 256; <= 0 means 256).  cb <= 0 restores the
+ * built-in heuristic.  The autotuner below writes these. */
 int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int cb, int geo_staged);
+                          int nquad, int cb, int geo_staged, int threads);
 int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int* cb, int* geo_staged);
+                          int nquad, int* cb, int* geo_staged, int* threads);
+
+/* Autotuner: times candidate tile shapes of one variant on the caller's
+ * device buffers (as for femtc_*_apply; y is overwritten), keeps the fastest
+ * as the variant's tile configuration and returns it (any output pointer may
+ * be NULL).  Synchronises `stream`.  No reference counterpart (the reference
+ * picks CPU register blocks Mb/Nb by hand, src/mass.hpp:176-218). */
+int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
+                   const void* tables, const void* u, void* y,
+                   const void* geo, size_t ncells, void* stream, int* cb,
+                   int* geo_staged, int* threads, float* best_ms);
+
+/* Save / load every explicitly set or tuned tile configuration as text
+ * ("op dtype semantics n q cb geo_staged threads" per line).  Load returns
+ * the number of entries applied, or a negative status. */
+int femtc_tile_db_save(const char* path);
+int femtc_tile_db_load(const char* path);
+
+/* One batched axis contraction, as linalg::gemm_blocked
+ * (src/linalg.hpp:101-182) for every cell c: C_c = A B_c with A column-major
+ * m x k (HOST memory, k, m <= 32), B_c row-major k x n and C_c column-major
+ * m x n (device, cell-contiguous; C is assigned, not accumulated).
+ * dtype FEMTC_F64 or FEMTC_F32.  The reference's own unit test exercises
+ * this at k = m = P+1, n = (P+1)^2 (tests/test_gemm.cpp:10-60). */
+int femtc_gemm_blocked(int dtype, int k, int m, int n, const void* a,
+                       const void* b, void* c, size_t batch, void* stream);
+
+/* apply_contractions (src/tmm.hpp:91-126) for every cell:
+ * A[a0,a1,a2] = sum I0(a0,b0) I1(a1,b1) I2(a2,b2) B[b0,b1,b2], with
+ * I(a,b) = I[a*Nb + b] when tr != 0 and I[b*Na + a] otherwise (the
+ * transpose the reference's Tr flag selects).  Tables are HOST memory,
+ * Na, Nb <= 16; B (Nb^3 per cell) and A (Na^3 per cell) on the device. */
+int femtc_apply_contractions(int dtype, int na, int nb, int tr,
+                             const void* i0, const void* i1, const void* i2,
+                             const void* b, void* a, size_t ncells,
+                             void* stream);
+
+/* Quadrature factors from Jacobians, computed in FP64 on the device:
+ * J row-major 3x3 per cell (per_point = 0, affine cells) or per point
+ * (per_point = 1, [ncells][Q^3][9]); weights: the Q 1D Gauss weights (host).
+ * Writes dw = detJ*w (mass, [ncells][Q^3]) and/or G = detJ w J^-1 J^-T
+ * ([ncells][Q^3][6], [zz,yz,xz,yy,xy,xx]) as FP64 or cast to FP32
+ * (out_dtype); either output may be NULL.  The reference has no geometry
+ * (bench_mass.cpp:86-88 draws detJ and G at random). */
+int femtc_geometry(int out_dtype, int nquad, const double* weights,
+                   const double* J, int per_point, void* dw, void* G,
+                   size_t ncells, void* stream);
 
 /* 1D basis tables for degree P with Q Gauss-Legendre points on [0,1]:
  * Lagrange basis on the P+1 Gauss-Lobatto-Legendre nodes (tabulated in

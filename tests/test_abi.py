@@ -69,11 +69,18 @@ def test_null_pointer_rejected(femtc):
     assert rc == -1
 
 
-def test_tile_config_roundtrip(femtc):
+def test_tile_config_roundtrip(femtc, tmp_path):
     old = femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5)
-    femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 8, 0)
-    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0)
+    femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 8, 0, 128)
+    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0, 128)
     with pytest.raises(femtc.FemtcError):
         femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 6, 0)  # not a multiple of 4
+    with pytest.raises(femtc.FemtcError):
+        femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 8, 0, 100)  # threads % 32
+    db = str(tmp_path / "tiles.txt")
+    femtc.tile_db_save(db)
     femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)  # back to default
     assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == old
+    assert femtc.tile_db_load(db) >= 1
+    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0, 128)
+    femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)

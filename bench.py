@@ -200,6 +200,162 @@ def cpu_baseline(w, seconds=10.0):
             "sample": f"{reps} x {sample} cells of the workload, FP64, OpenMP over cells, {el:.1f} s"}
 
 
+def run_batch(args, rank, world, dev, pg):
+    """64 meshes of mixed degree and operator in one persistent launch
+    (CUDA graph), against the same meshes as 64 single-mesh launches."""
+    import torch
+    import femtc_gb300 as F
+    from femtc_gb300 import workloads as W
+    spec = W.batch64_spec()
+    if args.cells:  # scale the cell counts down (profiling)
+        spec = [(op, P, max(1, n * args.cells // 100000)) for op, P, n in spec]
+    gen = torch.Generator(device=dev).manual_seed(1004)
+    rng = np.random.default_rng(1004)
+    meshes = []
+    for op, P, n in spec:
+        Q = P + 2
+        tables, _, wts, _ = F.tabulate(P, Q)
+        J = torch.from_numpy(W.random_jacobians(rng, n).reshape(n, 9)).to(dev)
+        u = torch.rand(n, (P + 1) ** 3, device=dev, generator=gen, dtype=torch.float32) * 2 - 1
+        y = torch.empty_like(u)
+        if op == F.MASS:
+            geo = torch.empty(n, Q ** 3, device=dev, dtype=torch.float32)
+            F.geometry(F.F32, Q, wts, J, geo, None, n)
+        else:
+            geo = torch.empty(n, Q ** 3, 6, device=dev, dtype=torch.float32)
+            F.geometry(F.F32, Q, wts, J, None, geo, n)
+        meshes.append((op, P, Q, tables.astype(np.float32), u, y, geo, n))
+    torch.cuda.synchronize()
+    ndofs = sum(n * (P + 1) ** 3 for _, P, n in spec)
+    nbytes = sum(4 * (2 * (P + 1) ** 3 + (1 if op == 0 else 6) * (P + 2) ** 3) * n for op, P, n in spec)
+    stream = torch.cuda.current_stream()
+    out = {}
+    for dtype in (F.F32, F.BF16X3, F.F16X2):
+        b = F.Batch(dtype, meshes, tune=True)
+        res = {}
+        for mode in ("graph", "eager", "separate"):
+            def step():
+                if mode == "graph":
+                    b.launch(stream)
+                elif mode == "eager":
+                    b.launch_eager(stream)
+                else:
+                    for op, P, Q, tab, u, y, geo, n in meshes:
+                        F.apply(op, dtype, F.EXACT, P, Q, tab, u, y, geo, n, stream)
+            for _ in range(args.warmup):
+                step()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            res[mode] = {"ms": ms, "gdofs": ndofs / ms / 1e6, "hbm_gbs": nbytes / ms / 1e6}
+        res["info"] = b.info()
+        b.close()
+        out[F.DTYPE_NAMES[dtype]] = res
+    if F.device_status() != 0:
+        raise RuntimeError("device fault word set during the batch benchmark")
+    if rank == 0:
+        head = out["f32"]["graph"]
+        hbm, src = peaks()
+        line = {
+            "metric": "GDoF/s batched mixed-degree action (64 meshes, one persistent graph launch)",
+            "value": head["gdofs"] * world, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64", "meshes": len(spec), "dofs": ndofs,
+                       "degrees": sorted({P for _, P, _ in spec}),
+                       "bytes_per_step": nbytes},
+            "roofline": {"bound": "hbm", "achieved": head["hbm_gbs"], "peak": hbm, "unit": "GB/s",
+                         "frac": head["hbm_gbs"] / hbm, "traffic": None, "peak_source": src},
+            "forms": out,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, rank, world, dev, pg):
+    """Serving: a Poisson stream (mean 2000 req/s) of matrix-free solves of
+    (M + sigma K) x = b, sigma ~ U(0.1, 10), P ~ U{2..7} (Q = P+2), cells
+    log-uniform in [1e3, 2e5], b ~ N(0,1), Jacobi, rel. tol 1e-8 through the
+    mixed-precision operator inside FP64 iterative refinement; admission by
+    HBM budget, continuous batching.  Latency = completion - arrival."""
+    import threading
+    import femtc_gb300 as F
+    from femtc_gb300 import workloads as W
+    rng = np.random.default_rng(1005 + rank)
+    nreq = args.requests
+    probs = []
+    for _ in range(nreq):
+        P = int(rng.integers(2, 8))
+        n = int(round(10 ** rng.uniform(3.0, np.log10(2e5))))
+        if args.cells:
+            n = max(1, n * args.cells // 200000)
+        sigma = float(rng.uniform(0.1, 10.0))
+        J = W.random_jacobians(rng, n).reshape(-1, 9)
+        b = rng.standard_normal((n, (P + 1) ** 3))
+        probs.append(F.Problem(P, P + 2, J, b, alpha=1.0, beta=sigma, rtol=1e-8,
+                               inner_dtype=F.F16X2))
+    arrivals = np.cumsum(rng.exponential(1.0 / 2000.0, size=nreq))
+    free = torch_free_bytes(dev)
+    budget = int(min(free * 0.6, 120e9))
+    # warm the kernels used by the solves (setup, outside the timed region)
+    for P in range(2, 8):
+        wp = F.Problem(P, P + 2, np.tile(np.eye(3).reshape(1, 9), (8, 1)), np.ones((8, (P + 1) ** 3)),
+                       inner_dtype=F.F16X2)
+        F.solve(wp)
+    srv = F.Server(budget, max_active=8)
+    tickets = [None] * nreq
+    t0 = time.perf_counter()
+
+    def feeder():
+        for i, p in enumerate(probs):
+            delay = arrivals[i] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            tickets[i] = srv.submit(p)
+
+    th = threading.Thread(target=feeder)
+    th.start()
+    th.join()
+    results = [srv.wait(t, 3600.0) for t in tickets]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r["t_done_ms"] - r["t_submit_ms"] for r in results])
+    svc = np.array([r["ms_total"] for r in results])
+    ok = sum(1 for r in results if r["rc"] == 0)
+    dofs = sum(p.b.size for p in probs)
+    if rank == 0:
+        line = {
+            "metric": "p50/p99 solve latency ms (serving, Poisson 2000 req/s)",
+            "value": float(np.percentile(lat, 50)), "unit": "ms", "n_gpus": world,
+            "steps": nreq, "warmup": 6, "ms_per_step": wall * 1e3 / nreq,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16x2+f64",
+            "data": "synthetic",
+            "config": {"workload": "serve", "requests": nreq, "arrival_rate_per_s": 2000,
+                       "degrees": "2..7", "cells": "log-uniform [1e3, 2e5]", "rtol": 1e-8,
+                       "hbm_budget_bytes": budget, "max_active": 8},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "service_p50_ms": float(np.percentile(svc, 50)),
+            "service_p99_ms": float(np.percentile(svc, 99)),
+            "throughput_req_s": nreq / wall, "solved_dofs_per_s": dofs / wall,
+            "converged": ok, "max_relres": float(max(r["relres"] for r in results)),
+            "max_concurrent": st["max_concurrent"], "peak_hbm_bytes": st["peak_in_use_bytes"],
+            "mean_outer_iters": float(np.mean([r["outer_iters"] for r in results])),
+            "mean_inner_iters": float(np.mean([r["inner_iters"] for r in results])),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def torch_free_bytes(dev):
+    import torch
+    free, _ = torch.cuda.mem_get_info(dev)
+    return free
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -207,7 +363,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="femtc", choices=["femtc", "reference"])
     ap.add_argument("--workload", default="stiffness_p4",
-                    choices=["stiffness_p4", "mass_p3", "stiffness_p6"])
+                    choices=["stiffness_p4", "mass_p3", "stiffness_p6", "batch64", "serve"])
+    ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
@@ -236,6 +393,11 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
     F.load()
+    if args.workload in ("batch64", "serve"):
+        (run_batch if args.workload == "batch64" else run_serve)(args, rank, world, dev, pg)
+        if pg is not None:
+            pg.destroy_process_group()
+        return
 
     w = W.make(args.workload, ncells=args.cells)
     n, q, op = w.n, w.nquad, w.op

@@ -55,6 +55,20 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_gemm_blocked": ([c_int] * 4 + [vp] * 3 + [c_size, vp], c_int),
         "femtc_apply_contractions": ([c_int] * 4 + [vp] * 5 + [c_size, vp], c_int),
         "femtc_geometry": ([c_int, c_int, vp, vp, c_int, vp, vp, c_size, vp], c_int),
+        "femtc_batch_create": ([c_int, vp, c_int, c_int, ctypes.POINTER(vp)], c_int),
+        "femtc_batch_launch": ([vp, vp], c_int),
+        "femtc_batch_launch_eager": ([vp, vp], c_int),
+        "femtc_batch_info": ([vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(c_int),
+                              ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong)], c_int),
+        "femtc_batch_layout": ([vp, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
+        "femtc_batch_destroy": ([vp], None),
+        "femtc_solve_bytes": ([c_int, c_int, c_size], c_size),
+        "femtc_solve": ([vp, vp, vp], c_int),
+        "femtc_server_create": ([c_size, c_int, ctypes.POINTER(vp)], c_int),
+        "femtc_server_submit": ([vp, vp, ctypes.POINTER(ctypes.c_longlong)], c_int),
+        "femtc_server_wait": ([vp, ctypes.c_longlong, ctypes.c_double, vp], c_int),
+        "femtc_server_get_stats": ([vp, vp], c_int),
+        "femtc_server_destroy": ([vp], None),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -214,3 +228,163 @@ def geometry(out_dtype: int, nquad: int, weights, J, dw, G, ncells: int, per_poi
     w = np.ascontiguousarray(weights, dtype=np.float64)
     check(load().femtc_geometry(out_dtype, nquad, w.ctypes.data, ptr(J), int(bool(per_point)),
                                 ptr(dw), ptr(G), ncells, stream_ptr(stream)))
+
+
+class BatchItem(ctypes.Structure):
+    """femtc_batch_item (include/femtc_gpu.h)."""
+    _fields_ = [("op", ctypes.c_int), ("degree", ctypes.c_int), ("nquad", ctypes.c_int),
+                ("tables", ctypes.c_void_p), ("u", ctypes.c_void_p), ("y", ctypes.c_void_p),
+                ("geo", ctypes.c_void_p), ("ncells", ctypes.c_size_t)]
+
+
+BATCH_TUNE = 1
+
+
+class Batch:
+    """A batched persistent launch over many meshes (femtc_batch_*).
+
+    meshes: iterable of (op, degree, nquad, tables, u, y, geo, ncells) with
+    device tensors; the tables are kept alive here until the batch is built.
+    """
+
+    def __init__(self, dtype: int, meshes, tune: bool = False):
+        lib = load()
+        self._tabs = [host_tables(m[3], dtype) for m in meshes]
+        arr = (BatchItem * len(self._tabs))()
+        for i, m in enumerate(meshes):
+            op, degree, nquad, _, u, y, geo, ncells = m
+            arr[i] = BatchItem(op, degree, nquad, self._tabs[i].ctypes.data, ptr(u), ptr(y),
+                               ptr(geo), ncells)
+        h = ctypes.c_void_p()
+        check(lib.femtc_batch_create(dtype, ctypes.cast(arr, ctypes.c_void_p), len(self._tabs),
+                                     BATCH_TUNE if tune else 0, ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self, stream=None) -> None:
+        check(load().femtc_batch_launch(self.handle, stream_ptr(stream)))
+
+    def launch_eager(self, stream=None) -> None:
+        check(load().femtc_batch_launch_eager(self.handle, stream_ptr(stream)))
+
+    def info(self):
+        nt, ctas, smem, nd = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        check(load().femtc_batch_info(self.handle, ctypes.byref(nt), ctypes.byref(ctas),
+                                      ctypes.byref(smem), ctypes.byref(nd)))
+        return {"tiles": nt.value, "ctas": ctas.value, "smem": smem.value, "dofs": nd.value}
+
+    def layout(self, op: int, degree: int):
+        cb, st = ctypes.c_int(), ctypes.c_int()
+        check(load().femtc_batch_layout(self.handle, op, degree, ctypes.byref(cb), ctypes.byref(st)))
+        return cb.value, st.value
+
+    def close(self) -> None:
+        if self.handle:
+            load().femtc_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+NOT_CONVERGED, TIMEOUT, NOMEM = -6, -7, -4
+
+
+class SolveRequest(ctypes.Structure):
+    """femtc_solve_request (include/femtc_gpu.h)."""
+    _fields_ = [("degree", ctypes.c_int), ("nquad", ctypes.c_int), ("ncells", ctypes.c_size_t),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("J", ctypes.c_void_p),
+                ("b", ctypes.c_void_p), ("x", ctypes.c_void_p), ("rtol", ctypes.c_double),
+                ("inner_rtol", ctypes.c_double), ("max_outer", ctypes.c_int),
+                ("max_inner", ctypes.c_int), ("inner_dtype", ctypes.c_int)]
+
+
+class SolveResult(ctypes.Structure):
+    """femtc_solve_result (include/femtc_gpu.h)."""
+    _fields_ = [("status", ctypes.c_int), ("outer_iters", ctypes.c_int),
+                ("inner_iters", ctypes.c_int), ("relres", ctypes.c_double),
+                ("bnorm", ctypes.c_double), ("ms_total", ctypes.c_double),
+                ("t_submit_ms", ctypes.c_double), ("t_admit_ms", ctypes.c_double),
+                ("t_done_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("rejected", ctypes.c_longlong), ("queued", ctypes.c_longlong),
+                ("active", ctypes.c_longlong), ("in_use_bytes", ctypes.c_size_t),
+                ("peak_in_use_bytes", ctypes.c_size_t), ("max_concurrent", ctypes.c_int)]
+
+
+class Problem:
+    """Host data of one (alpha M + beta K) x = b solve (keeps arrays alive)."""
+
+    def __init__(self, degree, nquad, J, b, alpha=1.0, beta=1.0, rtol=1e-8, inner_dtype=F32,
+                 inner_rtol=1e-4, max_outer=20, max_inner=2000):
+        self.J = np.ascontiguousarray(J, dtype=np.float64).reshape(-1, 9)
+        self.b = np.ascontiguousarray(b, dtype=np.float64).reshape(self.J.shape[0], -1)
+        self.x = np.zeros_like(self.b)
+        self.req = SolveRequest(degree, nquad, self.J.shape[0], alpha, beta, self.J.ctypes.data,
+                                self.b.ctypes.data, self.x.ctypes.data, rtol, inner_rtol,
+                                max_outer, max_inner, inner_dtype)
+
+
+def solve_bytes(degree: int, nquad: int, ncells: int) -> int:
+    return int(load().femtc_solve_bytes(degree, nquad, ncells))
+
+
+def solve(problem: "Problem", stream=None, raise_on_error: bool = True) -> dict:
+    """Synchronous solve; returns the result as a dict, problem.x holds x."""
+    res = SolveResult()
+    rc = load().femtc_solve(ctypes.byref(problem.req), ctypes.byref(res), stream_ptr(stream))
+    if rc != 0 and raise_on_error and rc != NOT_CONVERGED:
+        check(rc)
+    out = res.as_dict()
+    out["rc"] = rc
+    return out
+
+
+class Server:
+    """Continuous-batching solve server (femtc_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int, max_active: int):
+        h = ctypes.c_void_p()
+        check(load().femtc_server_create(hbm_budget_bytes, max_active, ctypes.byref(h)))
+        self.handle = h
+        self._live = {}
+
+    def submit(self, problem: "Problem") -> int:
+        t = ctypes.c_longlong()
+        check(load().femtc_server_submit(self.handle, ctypes.byref(problem.req), ctypes.byref(t)))
+        self._live[t.value] = problem
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 600.0) -> dict:
+        res = SolveResult()
+        rc = load().femtc_server_wait(self.handle, ticket, timeout_s, ctypes.byref(res))
+        if rc == TIMEOUT:
+            raise FemtcError(rc, load().femtc_last_error().decode())
+        self._live.pop(ticket, None)
+        out = res.as_dict()
+        out["rc"] = rc
+        return out
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(load().femtc_server_get_stats(self.handle, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self) -> None:
+        if self.handle:
+            load().femtc_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

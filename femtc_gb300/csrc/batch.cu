@@ -1,0 +1,463 @@
+// Host side of the batched persistent launch (femtc_batch_* in femtc_gpu.h):
+// validation, per-degree table slots, per-variant tile layouts (built-in or
+// measured by the autotuner), the longest-processing-time static schedule,
+// device descriptor tables, and the CUDA-graph capture of the launch.
+#include "femtc_gpu.h"
+
+#include "batch_kernel.cuh"
+#include "registry.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <queue>
+#include <vector>
+
+namespace femtc
+{
+int aux_fail(int code, const char* msg); // femtc_abi.cu
+std::pair<int, int> slab_layout_for(int n, int q, int esize); // femtc_abi.cu
+
+namespace
+{
+constexpr unsigned kBatchSmemCap = 220u * 1024u;
+// Per-variant caps on a tile's stage sizes: the batch's shared memory is the
+// sum of the maxima over its variants (3 x DOF/output stage, 2 x geometry
+// stage, work), so capping each part keeps every mix of variants within
+// kBatchSmemCap: 3*16 + 2*48 + 64 KB < 220 KB.
+constexpr unsigned kCapU = 16u * 1024u, kCapG = 48u * 1024u, kCapW = 64u * 1024u;
+
+bool within_caps(unsigned bu, unsigned bg, unsigned bw)
+{
+  return bu <= kCapU && bg <= kCapG && bw <= kCapW;
+}
+
+const BatchKernelInfo* family_for(int dtype)
+{
+  static const BatchKernelInfo f32 = batch_kernel_f32();
+  static const BatchKernelInfo f16 = batch_kernel_f16x2();
+  static const BatchKernelInfo bf16 = batch_kernel_bf16x3();
+  switch (dtype)
+  {
+  case FEMTC_F32: return &f32;
+  case FEMTC_F16X2: return &f16;
+  case FEMTC_BF16X3: return &bf16;
+  default: return nullptr;
+  }
+}
+
+double cell_cost(int op, int n)
+{
+  // bytes + flops/8 per cell (FP32 storage): the schedule's cost model
+  const double q = n + 1;
+  const double bytes = 4.0 * (2.0 * n * n * n + (op ? 6.0 : 1.0) * q * q * q);
+  const double flops = op ? 4.0 * q * n * (2.0 * n * n + 3.0 * q * n + 3.0 * q * q) + 15.0 * q * q * q
+                          : 4.0 * q * n * (n * n + q * n + q * q) + q * q * q;
+  return bytes + flops / 8.0;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+} // namespace
+} // namespace femtc
+
+using namespace femtc;
+
+struct femtc_batch
+{
+  int dtype = 0;
+  const BatchKernelInfo* fam = nullptr;
+  std::vector<femtc_batch_item> items;
+  BatchParams<float> params;
+  BatchTile* d_tiles = nullptr;
+  BatchItem<float>* d_items = nullptr;
+  long long ntiles = 0;
+  int grid = 0;
+  unsigned smem = 0;
+  long long ndofs = 0;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+
+  ~femtc_batch()
+  {
+    if (exec)
+      cudaGraphExecDestroy(exec);
+    if (graph)
+      cudaGraphDestroy(graph);
+    if (cap_stream)
+      cudaStreamDestroy(cap_stream);
+    if (d_tiles)
+      cudaFree(d_tiles);
+    if (d_items)
+      cudaFree(d_items);
+  }
+};
+
+namespace femtc
+{
+namespace
+{
+// Default layout of a variant for the batch kernel (256 threads per CTA):
+// the best lane efficiency for tiles whose stages stay within the cap.
+BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v)
+{
+  const int op = v / kBatchDegrees, n = 2 + v % kBatchDegrees, q = n + 1;
+  BatchLayout best{4, 0, 0, 0};
+  if (fam.family == kFamilySlab)
+  {
+    auto l = slab_layout_for(n, q, 4);
+    best.sq = l.first;
+    best.sbc = l.second;
+  }
+  double best_score = -1.0;
+  for (int cb = 4; cb <= 128; cb += 4)
+  {
+    BatchLayout l = best;
+    l.cb = cb;
+    l.staged = 0;
+    unsigned bu, bg, bw;
+    fam.bytes(v, l, &bu, &bg, &bw);
+    if (!within_caps(bu, bg, bw))
+      break;
+    // lanes: slab passes (2 lanes per slab) and pencil passes
+    const double lanes[2] = {double(cb * n * (fam.family == kFamilySlab ? 2 : 1)),
+                             double(cb * q * q)};
+    double eff = 0.0;
+    for (double x : lanes)
+      eff += x / (std::ceil(x / kCellThreads) * kCellThreads);
+    const double score = eff + 1e-4 * cb;
+    if (score > best_score)
+    {
+      best_score = score;
+      best = l;
+    }
+  }
+  (void)op;
+  return best;
+}
+
+int build(femtc_batch* b, const std::vector<BatchLayout>& lay)
+{
+  const BatchKernelInfo& fam = *b->fam;
+  BatchParams<float>& p = b->params;
+  for (int v = 0; v < kBatchVariants; ++v)
+    p.lay[v] = lay[v];
+  // stage sizes: max over the variants present
+  unsigned su = 0, sg = 0, sw = 0;
+  std::vector<char> present(kBatchVariants, 0);
+  for (const femtc_batch_item& it : b->items)
+    present[batch_variant(it.op, it.degree + 1)] = 1;
+  for (int v = 0; v < kBatchVariants; ++v)
+    if (present[v])
+    {
+      unsigned bu, bg, bw;
+      fam.bytes(v, lay[v], &bu, &bg, &bw);
+      su = std::max(su, (bu + 15u) & ~15u);
+      sg = std::max(sg, (bg + 15u) & ~15u);
+      sw = std::max(sw, (bw + 15u) & ~15u);
+    }
+  p.stage_u = su;
+  p.stage_g = sg;
+  p.stage_y = su;
+  b->smem = 128 + 2 * (su + sg) + su + sw;
+  if (b->smem > kBatchSmemCap)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: tile stages exceed shared memory");
+  cudaError_t e = cudaFuncSetAttribute(fam.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)b->smem);
+  if (e != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fam.fn, kCellThreads, b->smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (per_sm < 1)
+    return aux_fail(FEMTC_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
+
+  // tiles and their costs
+  struct Work
+  {
+    BatchTile t;
+    double cost;
+  };
+  std::vector<Work> work;
+  for (size_t i = 0; i < b->items.size(); ++i)
+  {
+    const femtc_batch_item& it = b->items[i];
+    const int v = batch_variant(it.op, it.degree + 1);
+    const int cb = lay[v].cb;
+    const double c = cell_cost(it.op, it.degree + 1);
+    for (long long c0 = 0; c0 < (long long)it.ncells; c0 += cb)
+    {
+      const int ncb = (int)std::min<long long>(cb, (long long)it.ncells - c0);
+      work.push_back({BatchTile{c0, (int)i, v, ncb, ncb == cb ? 1 : 0}, c * ncb});
+    }
+  }
+  const long long nwork = (long long)work.size();
+  b->grid = (int)std::max<long long>(1, std::min<long long>(nwork, (long long)per_sm * sms));
+  // longest processing time first onto the least loaded CTA
+  std::stable_sort(work.begin(), work.end(),
+                   [](const Work& a, const Work& c) { return a.cost > c.cost; });
+  using Slot = std::pair<double, int>;
+  std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> heap;
+  for (int g = 0; g < b->grid; ++g)
+    heap.push({0.0, g});
+  std::vector<std::vector<BatchTile>> per(b->grid);
+  for (const Work& w : work)
+  {
+    Slot s = heap.top();
+    heap.pop();
+    per[s.second].push_back(w.t);
+    heap.push({s.first + w.cost, s.second});
+  }
+  size_t rounds = 0;
+  for (auto& v : per)
+    rounds = std::max(rounds, v.size());
+  std::vector<BatchTile> order(rounds * b->grid, BatchTile{0, -1, 0, 0, 0});
+  for (int g = 0; g < b->grid; ++g)
+    for (size_t j = 0; j < per[g].size(); ++j)
+      order[j * b->grid + g] = per[g][j];
+  b->ntiles = (long long)order.size();
+  p.ntiles = b->ntiles;
+
+  std::vector<BatchItem<float>> items(b->items.size());
+  for (size_t i = 0; i < b->items.size(); ++i)
+    items[i] = BatchItem<float>{static_cast<const float*>(b->items[i].u),
+                                static_cast<float*>(b->items[i].y),
+                                static_cast<const float*>(b->items[i].geo)};
+  if (b->d_tiles)
+    cudaFree(b->d_tiles);
+  if (b->d_items)
+    cudaFree(b->d_items);
+  b->d_tiles = nullptr;
+  b->d_items = nullptr;
+  if (cudaMalloc(&b->d_tiles, sizeof(BatchTile) * std::max<size_t>(1, order.size())) !=
+          cudaSuccess ||
+      cudaMalloc(&b->d_items, sizeof(BatchItem<float>) * std::max<size_t>(1, items.size())) !=
+          cudaSuccess)
+    return aux_fail(FEMTC_ERR_NOMEM, "batch: descriptor allocation failed");
+  cudaMemcpy(b->d_tiles, order.data(), sizeof(BatchTile) * order.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_items, items.data(), sizeof(BatchItem<float>) * items.size(),
+             cudaMemcpyHostToDevice);
+  p.tiles = b->d_tiles;
+  p.items = b->d_items;
+  return FEMTC_OK;
+}
+
+int launch_eager(femtc_batch* b, cudaStream_t st)
+{
+  void* args[] = {&b->params};
+  cudaError_t e = cudaLaunchKernel(b->fam->fn, dim3((unsigned)b->grid), dim3(kCellThreads), args,
+                                   b->smem, st);
+  return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int capture(femtc_batch* b)
+{
+  if (b->exec)
+    cudaGraphExecDestroy(b->exec);
+  if (b->graph)
+    cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  if (!b->cap_stream &&
+      cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, "batch: stream creation failed");
+  cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  int rc = launch_eager(b, b->cap_stream);
+  e = cudaStreamEndCapture(b->cap_stream, &b->graph);
+  if (rc != FEMTC_OK)
+    return rc;
+  if (e != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+}
+
+float time_launches(femtc_batch* b, cudaStream_t st, int reps)
+{
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  launch_eager(b, st);
+  cudaEventRecord(e0, st);
+  for (int r = 0; r < reps; ++r)
+    launch_eager(b, st);
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms / reps;
+}
+
+// Autotuner of the batch: for every variant present, time candidate tile
+// shapes on that variant's meshes alone (the batch kernel, same stage
+// budget) and keep the fastest.
+void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
+{
+  const std::vector<femtc_batch_item> all = b->items;
+  cudaStream_t st;
+  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  for (int v = 0; v < kBatchVariants; ++v)
+  {
+    std::vector<femtc_batch_item> mine;
+    for (const auto& it : all)
+      if (batch_variant(it.op, it.degree + 1) == v)
+        mine.push_back(it);
+    if (mine.empty())
+      continue;
+    femtc_batch sub;
+    sub.dtype = b->dtype;
+    sub.fam = b->fam;
+    sub.items = mine;
+    std::memcpy(sub.params.tabs, b->params.tabs, sizeof(b->params.tabs));
+    const BatchLayout base = lay[v];
+    float best = 1e30f;
+    BatchLayout best_l = base;
+    for (int staged = 0; staged <= 1; ++staged)
+      for (int mult : {1, 2, 3, 4, 6, 8})
+      {
+        BatchLayout l = base;
+        l.cb = std::max(4, (base.cb * mult / 4 + 3) / 4 * 4);
+        l.staged = staged;
+        unsigned bu, bg, bw;
+        b->fam->bytes(v, l, &bu, &bg, &bw);
+        if (!within_caps(bu, bg, bw))
+          continue;
+        std::vector<BatchLayout> trial = lay;
+        trial[v] = l;
+        if (build(&sub, trial) != FEMTC_OK)
+          continue;
+        const float ms = time_launches(&sub, st, 3);
+        if (ms < best)
+        {
+          best = ms;
+          best_l = l;
+        }
+      }
+    lay[v] = best_l;
+  }
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+}
+} // namespace
+} // namespace femtc
+
+extern "C" {
+
+int femtc_batch_create(int dtype, const femtc_batch_item* items, int nitems,
+                       int flags, femtc_batch** out)
+{
+  if (!out)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: null output");
+  *out = nullptr;
+  const BatchKernelInfo* fam = family_for(dtype);
+  if (!fam)
+    return aux_fail(FEMTC_ERR_UNSUPPORTED,
+                    "batch: dtype must be FEMTC_F32, FEMTC_F16X2 or FEMTC_BF16X3");
+  if (!items || nitems < 1)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: no items");
+  auto b = std::make_unique<femtc_batch>();
+  b->dtype = dtype;
+  b->fam = fam;
+  std::memset(&b->params, 0, sizeof(b->params));
+  std::vector<char> slot_set(kBatchDegrees, 0);
+  for (int i = 0; i < nitems; ++i)
+  {
+    const femtc_batch_item& it = items[i];
+    if (it.op != FEMTC_OP_MASS && it.op != FEMTC_OP_STIFFNESS)
+      return aux_fail(FEMTC_ERR_INVALID, "batch: bad op");
+    if (it.degree < 1 || it.degree > kBatchDegrees)
+      return aux_fail(FEMTC_ERR_UNSUPPORTED, "batch: degree must be in 1..7");
+    if (it.nquad != it.degree + 2)
+      return aux_fail(FEMTC_ERR_UNSUPPORTED, "batch: nquad must be degree+2");
+    if (!it.tables || !it.u || !it.y || !it.geo)
+      return aux_fail(FEMTC_ERR_INVALID, "batch: null pointer in an item");
+    if (!aligned16(it.u) || !aligned16(it.y) || !aligned16(it.geo))
+      return aux_fail(FEMTC_ERR_INVALID, "batch: device pointers must be 16-byte aligned");
+    const int n = it.degree + 1, q = it.nquad, slot = n - 2;
+    const int ntab = it.op == FEMTC_OP_STIFFNESS ? 2 : 1;
+    const float* t = static_cast<const float*>(it.tables);
+    for (int w = 0; w < ntab; ++w)
+    {
+      float* dst = b->params.tabs[slot][w];
+      if (slot_set[slot] & (1 << w))
+      {
+        if (std::memcmp(dst, t + w * q * n, sizeof(float) * q * n) != 0)
+          return aux_fail(FEMTC_ERR_INVALID,
+                          "batch: meshes of the same degree must share their tables");
+      }
+      else
+      {
+        std::memcpy(dst, t + w * q * n, sizeof(float) * q * n);
+        slot_set[slot] |= (char)(1 << w);
+      }
+    }
+    b->items.push_back(it);
+    b->ndofs += (long long)it.ncells * n * n * n;
+  }
+  std::vector<BatchLayout> lay(kBatchVariants);
+  for (int v = 0; v < kBatchVariants; ++v)
+    lay[v] = default_batch_layout(*fam, v);
+  if (flags & FEMTC_BATCH_TUNE)
+    tune(b.get(), lay);
+  int rc = build(b.get(), lay);
+  if (rc != FEMTC_OK)
+    return rc;
+  rc = capture(b.get());
+  if (rc != FEMTC_OK)
+    return rc;
+  *out = b.release();
+  return FEMTC_OK;
+}
+
+int femtc_batch_launch(femtc_batch* b, void* stream)
+{
+  if (!b || !b->exec)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
+  cudaError_t e = cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int femtc_batch_launch_eager(femtc_batch* b, void* stream)
+{
+  if (!b)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
+  return launch_eager(b, static_cast<cudaStream_t>(stream));
+}
+
+int femtc_batch_info(const femtc_batch* b, long long* ntiles, int* ctas,
+                     int* smem_bytes, long long* ndofs)
+{
+  if (!b)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
+  if (ntiles)
+    *ntiles = b->ntiles;
+  if (ctas)
+    *ctas = b->grid;
+  if (smem_bytes)
+    *smem_bytes = (int)b->smem;
+  if (ndofs)
+    *ndofs = b->ndofs;
+  return FEMTC_OK;
+}
+
+int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
+                       int* geo_staged)
+{
+  if (!b || degree < 1 || degree > kBatchDegrees || (op != 0 && op != 1))
+    return aux_fail(FEMTC_ERR_INVALID, "batch: bad layout query");
+  const BatchLayout& l = b->params.lay[batch_variant(op, degree + 1)];
+  if (cb)
+    *cb = l.cb;
+  if (geo_staged)
+    *geo_staged = l.staged;
+  return FEMTC_OK;
+}
+
+void femtc_batch_destroy(femtc_batch* b) { delete b; }
+
+} // extern "C"

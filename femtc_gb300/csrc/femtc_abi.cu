@@ -605,6 +605,11 @@ void gll_nodes(int p, double* x)
 } // namespace
 
 int aux_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
+std::pair<int, int> slab_layout_for(int n, int q, int esize)
+{
+  return slab_layout(n, q, esize);
+}
 } // namespace femtc
 
 using namespace femtc;

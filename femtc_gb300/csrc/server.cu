@@ -1,0 +1,185 @@
+// Serving loop (femtc_server_* in femtc_gpu.h): continuous batching of
+// matrix-free solves.  A fixed pool of host workers, each with its own CUDA
+// stream, takes requests from one FIFO queue as soon as a worker is free and
+// the request fits in the HBM budget next to the solves already running;
+// running solves overlap on the device.  Timestamps (submit, admit, done)
+// are taken on one steady clock so callers get queueing and service latency.
+#include "femtc_gpu.h"
+
+#include <chrono>
+#include <condition_variable>
+#include <cuda_runtime.h>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace femtc
+{
+int aux_fail(int code, const char* msg);
+int solve_on_stream(const femtc_solve_request* rq, femtc_solve_result* res, cudaStream_t st);
+size_t solve_bytes(int degree, int nquad, size_t ncells);
+} // namespace femtc
+
+using namespace femtc;
+
+struct femtc_server
+{
+  using clk = std::chrono::steady_clock;
+  struct Job
+  {
+    long long ticket;
+    femtc_solve_request rq;
+    size_t bytes;
+    double t_submit;
+  };
+  size_t budget = 0;
+  int device = 0;
+  clk::time_point t0 = clk::now();
+  std::mutex m;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Job> queue;
+  std::map<long long, femtc_solve_result> results;
+  size_t in_use = 0, peak = 0;
+  long long next_ticket = 1, submitted = 0, completed = 0, rejected = 0;
+  int active = 0, max_conc = 0;
+  bool stop = false;
+  std::vector<std::thread> workers;
+
+  double now_ms() const
+  {
+    return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+  }
+
+  void worker()
+  {
+    cudaSetDevice(device);
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+      st = nullptr; // no device: solves fail with a CUDA status below
+    for (;;)
+    {
+      Job job;
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv_work.wait(lk, [&] {
+          return stop || (!queue.empty() && in_use + queue.front().bytes <= budget);
+        });
+        if (stop)
+          break;
+        job = queue.front();
+        queue.pop_front();
+        in_use += job.bytes;
+        peak = std::max(peak, in_use);
+        ++active;
+        max_conc = std::max(max_conc, active);
+      }
+      femtc_solve_result res{};
+      const double t_admit = now_ms();
+      if (st)
+        solve_on_stream(&job.rq, &res, st);
+      else
+        res.status = aux_fail(FEMTC_ERR_CUDA, "server: no CUDA stream on this worker");
+      {
+        std::lock_guard<std::mutex> lk(m);
+        res.t_submit_ms = job.t_submit;
+        res.t_admit_ms = t_admit;
+        res.t_done_ms = now_ms();
+        results[job.ticket] = res;
+        in_use -= job.bytes;
+        --active;
+        ++completed;
+      }
+      cv_done.notify_all();
+      cv_work.notify_all();
+    }
+    if (st)
+      cudaStreamDestroy(st);
+  }
+};
+
+extern "C" {
+
+int femtc_server_create(size_t hbm_budget_bytes, int max_active, femtc_server** out)
+{
+  if (!out || max_active < 1 || hbm_budget_bytes == 0)
+    return aux_fail(FEMTC_ERR_INVALID, "server: need a budget, max_active >= 1 and an output");
+  auto* s = new femtc_server();
+  s->budget = hbm_budget_bytes;
+  cudaGetDevice(&s->device);
+  for (int i = 0; i < max_active; ++i)
+    s->workers.emplace_back([s] { s->worker(); });
+  *out = s;
+  return FEMTC_OK;
+}
+
+int femtc_server_submit(femtc_server* s, const femtc_solve_request* rq, long long* ticket)
+{
+  if (!s || !rq || !ticket)
+    return aux_fail(FEMTC_ERR_INVALID, "server: null argument");
+  if (rq->degree < 1 || rq->degree > 7 || rq->nquad < rq->degree + 1 ||
+      rq->nquad > rq->degree + 3 || rq->ncells == 0 || !rq->J || !rq->b || !rq->x)
+    return aux_fail(FEMTC_ERR_INVALID, "server: malformed request");
+  const size_t bytes = solve_bytes(rq->degree, rq->nquad, rq->ncells);
+  std::lock_guard<std::mutex> lk(s->m);
+  if (bytes > s->budget)
+  {
+    ++s->rejected;
+    return aux_fail(FEMTC_ERR_NOMEM, "server: request exceeds the HBM budget");
+  }
+  *ticket = s->next_ticket++;
+  s->queue.push_back(femtc_server::Job{*ticket, *rq, bytes, s->now_ms()});
+  ++s->submitted;
+  s->cv_work.notify_one();
+  return FEMTC_OK;
+}
+
+int femtc_server_wait(femtc_server* s, long long ticket, double timeout_s,
+                      femtc_solve_result* res)
+{
+  if (!s || !res)
+    return aux_fail(FEMTC_ERR_INVALID, "server: null argument");
+  std::unique_lock<std::mutex> lk(s->m);
+  const bool ok = s->cv_done.wait_for(
+      lk, std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0.0),
+      [&] { return s->results.count(ticket) > 0; });
+  if (!ok)
+    return aux_fail(FEMTC_ERR_TIMEOUT, "server: result not ready");
+  *res = s->results[ticket];
+  s->results.erase(ticket);
+  return res->status;
+}
+
+int femtc_server_get_stats(femtc_server* s, femtc_server_stats* st)
+{
+  if (!s || !st)
+    return aux_fail(FEMTC_ERR_INVALID, "server: null argument");
+  std::lock_guard<std::mutex> lk(s->m);
+  st->submitted = s->submitted;
+  st->completed = s->completed;
+  st->rejected = s->rejected;
+  st->queued = (long long)s->queue.size();
+  st->active = s->active;
+  st->in_use_bytes = s->in_use;
+  st->peak_in_use_bytes = s->peak;
+  st->max_concurrent = s->max_conc;
+  return FEMTC_OK;
+}
+
+void femtc_server_destroy(femtc_server* s)
+{
+  if (!s)
+    return;
+  {
+    std::lock_guard<std::mutex> lk(s->m);
+    s->stop = true;
+    s->queue.clear();
+  }
+  s->cv_work.notify_all();
+  for (auto& t : s->workers)
+    t.join();
+  delete s;
+}
+
+} // extern "C"

@@ -122,3 +122,17 @@ def random_reference_inputs(op: int, degree: int, ncells: int, seed: int):
     else:
         geo = rng.uniform(0.0, 1.0, size=(ncells, n ** 3, 6))
     return tables, u, geo
+
+
+def batch64_spec(seed: int = 1004, nmeshes: int = 64):
+    """The batching workload: 64 meshes, degree P ~ U{1..7}, Q = P+2, cell
+    counts log-uniform in [1e3, 1e5], half mass and half stiffness.
+    Returns [(op, degree, ncells)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nmeshes):
+        degree = int(rng.integers(1, 8))
+        ncells = int(round(10 ** rng.uniform(3.0, 5.0)))
+        op = _lib.MASS if i < nmeshes // 2 else _lib.STIFFNESS
+        out.append((op, degree, ncells))
+    return out

@@ -39,6 +39,8 @@ extern "C" {
 #define FEMTC_ERR_CUDA (-3)        /* a CUDA runtime call failed */
 #define FEMTC_ERR_NOMEM (-4)       /* device or pinned allocation failed */
 #define FEMTC_ERR_DEVICE (-5)      /* a kernel's bounded wait gave up */
+#define FEMTC_ERR_NOT_CONVERGED (-6) /* a solve stopped at its iteration cap */
+#define FEMTC_ERR_TIMEOUT (-7)     /* a wait ran out of time */
 
 typedef enum
 {
@@ -160,6 +162,113 @@ int femtc_apply_contractions(int dtype, int na, int nb, int tr,
 int femtc_geometry(int out_dtype, int nquad, const double* weights,
                    const double* J, int per_point, void* dw, void* G,
                    size_t ncells, void* stream);
+
+/* ----------------------------------------------------------------------
+ * Batched persistent launch: many meshes of mixed degree (1..7, Q = P+2)
+ * and operator in one kernel, captured once in a CUDA graph and replayed.
+ * No reference counterpart: the reference applies one operator of one
+ * degree per call (src/mass.hpp:196-219).
+ * Items with the same degree must share their tables.  Device pointers
+ * must stay valid, with unchanged contents' shapes, for the batch's life;
+ * their contents may change between launches.
+ * dtype: FEMTC_F32 (CUDA cores), FEMTC_F16X2 or FEMTC_BF16X3 (tensor
+ * cores); FP32 storage and tables.
+ * flags: FEMTC_BATCH_TUNE measures tile shapes per (degree, op) on the
+ * batch's own buffers at creation (the y buffers are overwritten).
+ * ---------------------------------------------------------------------- */
+#define FEMTC_BATCH_TUNE 1
+
+typedef struct
+{
+  int op;             /* femtc_op */
+  int degree;         /* 1..7 */
+  int nquad;          /* degree + 2 */
+  const void* tables; /* host, 2*Q*(degree+1) floats (Phi then Gamma) */
+  const void* u;      /* device, [ncells][N^3] */
+  void* y;            /* device, [ncells][N^3] */
+  const void* geo;    /* device, detJ*w or G as for the single-mesh calls */
+  size_t ncells;
+} femtc_batch_item;
+
+typedef struct femtc_batch femtc_batch;
+
+int femtc_batch_create(int dtype, const femtc_batch_item* items, int nitems,
+                       int flags, femtc_batch** out);
+/* Replays the captured graph on `stream` (asynchronous). */
+int femtc_batch_launch(femtc_batch* b, void* stream);
+/* The same kernel launched without the graph (for comparison). */
+int femtc_batch_launch_eager(femtc_batch* b, void* stream);
+int femtc_batch_info(const femtc_batch* b, long long* ntiles, int* ctas,
+                     int* smem_bytes, long long* ndofs);
+int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
+                       int* geo_staged);
+void femtc_batch_destroy(femtc_batch* b);
+
+/* ----------------------------------------------------------------------
+ * Matrix-free solve of (alpha M + beta K) x = b on a cell-local hexahedral
+ * mesh (affine cells): Jacobi-preconditioned CG with a mixed-precision
+ * operator (inner_dtype) inside FP64 iterative refinement; the residual,
+ * the dot products and x are FP64.  No reference counterpart (the
+ * reference has no solver): this is the caller the serving workload needs.
+ * ---------------------------------------------------------------------- */
+typedef struct
+{
+  int degree, nquad;   /* degree 1..7, nquad in degree+1..degree+3 */
+  size_t ncells;
+  double alpha, beta;  /* A = alpha M + beta K; alpha > 0, beta >= 0 */
+  const double* J;     /* host [ncells][9] row-major affine Jacobians */
+  const double* b;     /* host [ncells][N^3] */
+  double* x;           /* host [ncells][N^3], written on completion */
+  double rtol;         /* ||b - A x|| <= rtol ||b|| (FP64 residual) */
+  double inner_rtol;   /* inner CG tolerance (<= 0: 1e-4) */
+  int max_outer;       /* <= 0: 20 */
+  int max_inner;       /* per outer iteration, <= 0: 2000 */
+  int inner_dtype;     /* FEMTC_F32, FEMTC_F16X2 or FEMTC_BF16X3 */
+} femtc_solve_request;
+
+typedef struct
+{
+  int status;          /* FEMTC_OK, FEMTC_ERR_NOT_CONVERGED, ... */
+  int outer_iters, inner_iters;
+  double relres;       /* final ||b - A x|| / ||b|| in FP64 */
+  double bnorm;
+  double ms_total;     /* wall time of the solve itself */
+  double t_submit_ms, t_admit_ms, t_done_ms; /* server clock (server only) */
+} femtc_solve_result;
+
+/* Device bytes one solve allocates (one stream-ordered allocation). */
+size_t femtc_solve_bytes(int degree, int nquad, size_t ncells);
+
+/* Synchronous solve on `stream` (NULL: a private stream). */
+int femtc_solve(const femtc_solve_request* rq, femtc_solve_result* res,
+                void* stream);
+
+/* Serving loop with continuous batching: up to max_active solves run at
+ * once, each on its own stream and host worker, so their kernels overlap on
+ * the device; queued requests are admitted in arrival order as slots and
+ * HBM budget free up (a request larger than the whole budget is rejected
+ * at submit with FEMTC_ERR_NOMEM).  Request memory (J, b, x) must stay
+ * valid until the request's result has been collected. */
+typedef struct femtc_server femtc_server;
+
+typedef struct
+{
+  long long submitted, completed, rejected, queued, active;
+  size_t in_use_bytes, peak_in_use_bytes;
+  int max_concurrent;  /* most solves seen running at once */
+} femtc_server_stats;
+
+int femtc_server_create(size_t hbm_budget_bytes, int max_active,
+                        femtc_server** out);
+int femtc_server_submit(femtc_server* s, const femtc_solve_request* rq,
+                        long long* ticket);
+/* Waits up to timeout_s seconds for the ticket's result (FEMTC_ERR_TIMEOUT
+ * otherwise); returns the solve's status and fills *res. */
+int femtc_server_wait(femtc_server* s, long long ticket, double timeout_s,
+                      femtc_solve_result* res);
+int femtc_server_get_stats(femtc_server* s, femtc_server_stats* st);
+/* Stops admitting, lets running solves finish, drops queued ones. */
+void femtc_server_destroy(femtc_server* s);
 
 /* 1D basis tables for degree P with Q Gauss-Legendre points on [0,1]:
  * Lagrange basis on the P+1 Gauss-Lobatto-Legendre nodes (tabulated in

@@ -1,0 +1,91 @@
+"""GPU: matrix-free CG with the mixed-precision operator inside FP64
+iterative refinement, and the continuous-batching server.
+
+Checked against the oracle: the FP64 residual ||b - (alpha M + beta K) x||
+computed on the CPU must be <= rtol ||b|| (1e-8), and x must match the
+oracle's own FP64 CG solution; a solve gives the same bits alone and in a
+mix of concurrent solves on the server."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def problem(femtc, P, Q, ncells, sigma, seed, inner_dtype=1, rtol=1e-8):
+    from femtc_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    J = W.random_jacobians(rng, ncells)
+    b = rng.standard_normal((ncells, (P + 1) ** 3))
+    return femtc.Problem(P, Q, J.reshape(-1, 9), b, alpha=1.0, beta=sigma, rtol=rtol,
+                         inner_dtype=inner_dtype), J
+
+
+def oracle_geo(femtc, P, Q, J):
+    from femtc_gb300 import workloads as W
+    _, _, w, _ = femtc.tabulate(P, Q)
+    w3 = W.tensor_weights(w)
+    d = np.linalg.det(J)[:, None] * w3[None]
+    g = W.geometry_from_jacobians(J, w3)
+    t, _, _, _ = femtc.tabulate(P, Q)
+    return t, d, g
+
+
+@pytest.mark.parametrize("inner_dtype", [1, 2, 3])
+@pytest.mark.parametrize("P,Q,sigma", [(2, 4, 0.5), (3, 5, 5.0), (5, 7, 0.1)])
+def test_solve_matches_oracle(femtc, orc, dev, inner_dtype, P, Q, sigma):
+    pr, J = problem(femtc, P, Q, 60, sigma, seed=P * 10 + inner_dtype, inner_dtype=inner_dtype)
+    res = femtc.solve(pr)
+    assert res["rc"] == 0 and res["relres"] <= 1e-8, res
+    t, d, g = oracle_geo(femtc, P, Q, J)
+    r = pr.b - orc.helmholtz(P, Q, t, pr.x, d, g, 1.0, sigma)
+    assert np.linalg.norm(r) <= 1.5e-8 * np.linalg.norm(pr.b)
+    xo, it, rel = orc.cg(P, Q, t, d, g, 1.0, sigma, pr.b.reshape(-1), 1e-12, 5000)
+    assert it > 0
+    assert np.abs(pr.x.reshape(-1) - xo).max() <= 1e-6 * np.abs(xo).max()
+
+
+def test_not_converged_is_reported(femtc, dev):
+    pr, _ = problem(femtc, 3, 5, 40, 1.0, seed=1, rtol=1e-14)
+    pr.req.max_outer = 1
+    res = femtc.solve(pr)
+    assert res["rc"] == femtc.NOT_CONVERGED and res["outer_iters"] == 1 and res["relres"] > 1e-14
+
+
+def test_server_mix_equals_alone(femtc, dev):
+    probs = [problem(femtc, P, P + 2, n, s, seed=i)[0]
+             for i, (P, n, s) in enumerate([(2, 300, 0.3), (4, 120, 2.0), (3, 500, 7.0),
+                                            (6, 40, 0.1), (5, 80, 1.0), (2, 50, 9.0)])]
+    alone = []
+    for p in probs:
+        femtc.solve(p)
+        alone.append(p.x.copy())
+        p.x[:] = 0.0
+    srv = femtc.Server(hbm_budget_bytes=8 << 30, max_active=3)
+    try:
+        tickets = [srv.submit(p) for p in probs]
+        results = [srv.wait(t, 300.0) for t in tickets]
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert all(r["rc"] == 0 for r in results)
+    assert st["completed"] == len(probs) and st["max_concurrent"] >= 2
+    for p, a in zip(probs, alone):
+        assert np.array_equal(p.x, a)  # same bits alone and in the mix
+    for r in results:
+        assert r["t_submit_ms"] <= r["t_admit_ms"] <= r["t_done_ms"]
+
+
+def test_server_budget_serialises(femtc, dev):
+    p1 = problem(femtc, 3, 5, 400, 1.0, seed=1)[0]
+    p2 = problem(femtc, 3, 5, 400, 1.0, seed=2)[0]
+    need = femtc.solve_bytes(3, 5, 400)
+    srv = femtc.Server(hbm_budget_bytes=int(need * 1.5), max_active=4)  # room for one at a time
+    try:
+        t1, t2 = srv.submit(p1), srv.submit(p2)
+        r1, r2 = srv.wait(t1, 300.0), srv.wait(t2, 300.0)
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert r1["rc"] == 0 and r2["rc"] == 0
+    assert st["max_concurrent"] == 1 and st["peak_in_use_bytes"] <= need * 1.5
+    assert r2["t_admit_ms"] >= r1["t_done_ms"] - 1.0

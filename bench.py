@@ -207,7 +207,7 @@ def run_batch(args, rank, world, dev, pg):
     import femtc_gb300 as F
     from femtc_gb300 import workloads as W
     spec = W.batch64_spec()
-    if args.cells:  # scale the cell counts down (profiling)
+    if args.cells:  # scale the cell counts down (small meshes / profiling)
         spec = [(op, P, max(1, n * args.cells // 100000)) for op, P, n in spec]
     gen = torch.Generator(device=dev).manual_seed(1004)
     rng = np.random.default_rng(1004)

@@ -4,7 +4,7 @@
 // device descriptor tables, and the CUDA-graph capture of the launch.
 #include "femtc_gpu.h"
 
-#include "batch_kernel.cuh"
+#include "batch_host.hpp"
 #include "registry.hpp"
 
 #include <algorithm>
@@ -24,8 +24,8 @@ constexpr unsigned kBatchSmemCap = 220u * 1024u;
 // Per-variant caps on a tile's stage sizes: the batch's shared memory is the
 // sum of the maxima over its variants (3 x DOF/output stage, 2 x geometry
 // stage, work), so capping each part keeps every mix of variants within
-// kBatchSmemCap: 3*16 + 2*48 + 64 KB < 220 KB.
-constexpr unsigned kCapU = 16u * 1024u, kCapG = 48u * 1024u, kCapW = 64u * 1024u;
+// 3*8 + 2*16 + 48 KB = 104 KB: two CTAs per SM whatever the mix.
+constexpr unsigned kCapU = 8u * 1024u, kCapG = 16u * 1024u, kCapW = 48u * 1024u;
 
 bool within_caps(unsigned bu, unsigned bg, unsigned bw)
 {
@@ -62,39 +62,15 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 using namespace femtc;
 
-struct femtc_batch
-{
-  int dtype = 0;
-  const BatchKernelInfo* fam = nullptr;
-  std::vector<femtc_batch_item> items;
-  BatchParams<float> params;
-  BatchTile* d_tiles = nullptr;
-  BatchItem<float>* d_items = nullptr;
-  long long ntiles = 0;
-  int grid = 0;
-  unsigned smem = 0;
-  long long ndofs = 0;
-  cudaStream_t cap_stream = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-
-  ~femtc_batch()
-  {
-    if (exec)
-      cudaGraphExecDestroy(exec);
-    if (graph)
-      cudaGraphDestroy(graph);
-    if (cap_stream)
-      cudaStreamDestroy(cap_stream);
-    if (d_tiles)
-      cudaFree(d_tiles);
-    if (d_items)
-      cudaFree(d_items);
-  }
-};
 
 namespace femtc
 {
+namespace
+{
+} // namespace
+
+const BatchKernelInfo* batch_family_for(int dtype) { return family_for(dtype); }
+
 namespace
 {
 // Default layout of a variant for the batch kernel (256 threads per CTA):
@@ -136,7 +112,13 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v)
   return best;
 }
 
-int build(femtc_batch* b, const std::vector<BatchLayout>& lay)
+} // namespace
+
+// Host part of a batch build: stage sizes, shared memory, grid, and the
+// longest-processing-time tile order (CTA g runs order[g], order[g+G], ...).
+// No device memory is allocated here.
+int batch_plan(femtc_batch* b, const std::vector<BatchLayout>& lay,
+               std::vector<BatchTile>& order)
 {
   const BatchKernelInfo& fam = *b->fam;
   BatchParams<float>& p = b->params;
@@ -212,18 +194,45 @@ int build(femtc_batch* b, const std::vector<BatchLayout>& lay)
   size_t rounds = 0;
   for (auto& v : per)
     rounds = std::max(rounds, v.size());
-  std::vector<BatchTile> order(rounds * b->grid, BatchTile{0, -1, 0, 0, 0});
+  order.assign(rounds * b->grid, BatchTile{0, -1, 0, 0, 0});
   for (int g = 0; g < b->grid; ++g)
     for (size_t j = 0; j < per[g].size(); ++j)
       order[j * b->grid + g] = per[g][j];
   b->ntiles = (long long)order.size();
   p.ntiles = b->ntiles;
+  return FEMTC_OK;
+}
 
-  std::vector<BatchItem<float>> items(b->items.size());
+// Device mesh table of a batch.
+void batch_item_table(const femtc_batch* b, std::vector<BatchItem<float>>& items)
+{
+  items.resize(b->items.size());
   for (size_t i = 0; i < b->items.size(); ++i)
     items[i] = BatchItem<float>{static_cast<const float*>(b->items[i].u),
                                 static_cast<float*>(b->items[i].y),
                                 static_cast<const float*>(b->items[i].geo)};
+}
+
+namespace
+{
+} // namespace
+
+BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v)
+{
+  return default_batch_layout(fam, v);
+}
+
+namespace
+{
+int build(femtc_batch* b, const std::vector<BatchLayout>& lay)
+{
+  std::vector<BatchTile> order;
+  int rc = batch_plan(b, lay, order);
+  if (rc != FEMTC_OK)
+    return rc;
+  BatchParams<float>& p = b->params;
+  std::vector<BatchItem<float>> items;
+  batch_item_table(b, items);
   if (b->d_tiles)
     cudaFree(b->d_tiles);
   if (b->d_items)

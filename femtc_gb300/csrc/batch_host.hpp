@@ -1,0 +1,53 @@
+// Host-side state of a batched launch, shared by the translation units that
+// build and launch batches (batch.cu and friends).
+#pragma once
+
+#include "femtc_gpu.h"
+
+#include "batch_kernel.cuh"
+
+#include <vector>
+
+struct femtc_batch
+{
+  int dtype = 0;
+  const femtc::BatchKernelInfo* fam = nullptr;
+  std::vector<femtc_batch_item> items;
+  femtc::BatchParams<float> params;
+  femtc::BatchTile* d_tiles = nullptr;
+  femtc::BatchItem<float>* d_items = nullptr;
+  long long ntiles = 0;
+  int grid = 0;
+  unsigned smem = 0;
+  long long ndofs = 0;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+
+  ~femtc_batch()
+  {
+    if (exec)
+      cudaGraphExecDestroy(exec);
+    if (graph)
+      cudaGraphDestroy(graph);
+    if (cap_stream)
+      cudaStreamDestroy(cap_stream);
+    if (d_tiles)
+      cudaFree(d_tiles);
+    if (d_items)
+      cudaFree(d_items);
+  }
+};
+
+namespace femtc
+{
+// Kernel family of a batch dtype (FEMTC_F32, FEMTC_F16X2, FEMTC_BF16X3).
+const BatchKernelInfo* batch_family_for(int dtype);
+// Built-in tile layout of variant v for the batch kernel.
+BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v);
+// Host plan of a batch: stage sizes, shared memory, grid and tile order.
+int batch_plan(femtc_batch* b, const std::vector<BatchLayout>& lay,
+               std::vector<BatchTile>& order);
+// Device mesh table of a batch (pointers of its items).
+void batch_item_table(const femtc_batch* b, std::vector<BatchItem<float>>& items);
+} // namespace femtc

@@ -235,8 +235,18 @@ __device__ __noinline__ void batch_run(const BatchParams<T>& bp,
   X(4, OP_STIFFNESS) X(5, OP_STIFFNESS) X(6, OP_STIFFNESS)                     \
   X(7, OP_STIFFNESS) X(8, OP_STIFFNESS)
 
+// The kernel's register budget is its largest variant's.  Tensor-core
+// families fit in 128 registers: two CTAs per SM.  The CUDA-core slab
+// tiles of degree >= 5 hold a whole slab per thread and spill under that
+// cap, so that family keeps one CTA per SM and its full register file.
+template <int FAMILY>
+__host__ __device__ constexpr int batch_min_blocks()
+{
+  return FAMILY == 0 ? 1 : 2;
+}
+
 template <typename T, int FAMILY>
-__global__ void __launch_bounds__(kCellThreads)
+__global__ void __launch_bounds__(kCellThreads, batch_min_blocks<FAMILY>())
     batch_kernel(const __grid_constant__ BatchParams<T> bp)
 {
   extern __shared__ __align__(128) unsigned char smem[];

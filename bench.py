@@ -411,12 +411,10 @@ def main():
             pg.barrier()
         torch.cuda.synchronize()
 
+    from femtc_gb300 import replicas
+
     def maxreduce(x):
-        if pg is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.max_over_ranks(x, device=dev)
 
     # FP64 oracle on a slice of the workload: every form states its error
     err_cells = min(w.ncells, 2048)

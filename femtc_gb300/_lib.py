@@ -62,6 +62,7 @@ def _declare(lib: ctypes.CDLL) -> None:
                               ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong)], c_int),
         "femtc_batch_layout": ([vp, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
         "femtc_batch_destroy": ([vp], None),
+        "femtc_batch_apply_static": ([c_int, vp, c_int, vp], c_int),
         "femtc_solve_bytes": ([c_int, c_int, c_size], c_size),
         "femtc_solve": ([vp, vp, vp], c_int),
         "femtc_server_create": ([c_size, c_int, ctypes.POINTER(vp)], c_int),
@@ -238,6 +239,18 @@ class BatchItem(ctypes.Structure):
 
 
 BATCH_TUNE = 1
+
+
+def batch_apply_static(dtype: int, meshes, stream=None) -> None:
+    """femtc_batch_apply_static: the batched launch with its schedule in the
+    library's fixed device array (no device allocation); meshes as for Batch."""
+    tabs = [host_tables(m[3], dtype) for m in meshes]
+    arr = (BatchItem * len(tabs))()
+    for i, m in enumerate(meshes):
+        op, degree, nquad, _, u, y, geo, ncells = m
+        arr[i] = BatchItem(op, degree, nquad, tabs[i].ctypes.data, ptr(u), ptr(y), ptr(geo), ncells)
+    check(load().femtc_batch_apply_static(dtype, ctypes.cast(arr, ctypes.c_void_p), len(tabs),
+                                          stream_ptr(stream)))
 
 
 class Batch:

@@ -1,0 +1,175 @@
+// femtc_batch_apply_static: the batched launch for callers that cannot
+// allocate device memory.
+//
+// femtc_batch_create keeps its tile schedule and mesh table in device memory
+// it allocates with cudaMalloc.  Some callers cannot allow that: code that
+// runs while another thread captures a CUDA graph in global capture mode
+// (cudaMalloc is then an error), applications whose memory manager has
+// reserved the device's memory up front, and latency-bound loops that must
+// not take cudaMalloc's implicit device synchronisation.  This entry point
+// runs the same batch kernel with the schedule and the mesh table placed in
+// a fixed array in this file (g_batch_scratch, kStaticScratchBytes), which
+// every GPU that loads the library holds until the process exits.
+//
+// * The first call on a device looks up the array's device address with
+//   cudaGetSymbolAddress (with that device current); make that first call
+//   before any stream capture.
+// * Every call reuses the array.  Nothing in it must start at zero: each
+//   call writes the whole mesh table and tile schedule it reads.  Calls on
+//   one stream are ordered; calls whose work overlaps on the GPU (other
+//   streams, other host threads) race on the array.
+// * A batch whose schedule does not fit is rejected with FEMTC_ERR_INVALID
+//   and a message giving the capacity.
+// * No cudaMalloc, cudaFree or other allocating routine is called: the
+//   schedule is uploaded with cudaMemcpyAsync on the caller's stream.
+#include "batch_host.hpp"
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace femtc
+{
+int aux_fail(int code, const char* msg); // femtc_abi.cu
+
+namespace
+{
+// The mesh table (kStaticMaxItems entries at most) followed by the tile
+// schedule of one call.
+constexpr size_t kStaticScratchBytes = size_t(8) << 20; // 8 MiB
+constexpr int kStaticMaxItems = 4096;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_batch_scratch[kStaticScratchBytes];
+
+std::mutex g_scratch_mutex;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_batch_scratch on the current device (set up once per
+// device, with that device current).
+int scratch_address(void** out)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices)
+    return aux_fail(FEMTC_ERR_UNSUPPORTED, "batch_apply_static: device index above 63");
+  std::lock_guard<std::mutex> lk(g_scratch_mutex);
+  if (!g_scratch_addr[dev])
+  {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_batch_scratch);
+    if (e != cudaSuccess || !p)
+      return aux_fail(FEMTC_ERR_CUDA, "batch_apply_static: cudaGetSymbolAddress failed");
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return FEMTC_OK;
+}
+
+size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+} // namespace
+} // namespace femtc
+
+using namespace femtc;
+
+extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items,
+                                        int nitems, void* stream)
+{
+  const BatchKernelInfo* fam = batch_family_for(dtype);
+  if (!fam)
+    return aux_fail(FEMTC_ERR_UNSUPPORTED,
+                    "batch_apply_static: dtype must be FEMTC_F32, FEMTC_F16X2 or FEMTC_BF16X3");
+  if (!items || nitems < 1)
+    return aux_fail(FEMTC_ERR_INVALID, "batch_apply_static: no items");
+  if (nitems > kStaticMaxItems)
+  {
+    char msg[160];
+    std::snprintf(msg, sizeof(msg),
+                  "batch_apply_static: %d meshes exceed the static capacity of %d meshes",
+                  nitems, kStaticMaxItems);
+    return aux_fail(FEMTC_ERR_INVALID, msg);
+  }
+  // the batch's host description; it owns no device memory
+  femtc_batch b;
+  b.dtype = dtype;
+  b.fam = fam;
+  std::memset(&b.params, 0, sizeof(b.params));
+  char slot_set[kBatchDegrees] = {};
+  for (int i = 0; i < nitems; ++i)
+  {
+    const femtc_batch_item& it = items[i];
+    if (it.op != FEMTC_OP_MASS && it.op != FEMTC_OP_STIFFNESS)
+      return aux_fail(FEMTC_ERR_INVALID, "batch_apply_static: bad op");
+    if (it.degree < 1 || it.degree > kBatchDegrees || it.nquad != it.degree + 2)
+      return aux_fail(FEMTC_ERR_UNSUPPORTED,
+                      "batch_apply_static: degree in 1..7 and nquad = degree+2");
+    if (!it.tables || !it.u || !it.y || !it.geo)
+      return aux_fail(FEMTC_ERR_INVALID, "batch_apply_static: null pointer in an item");
+    if (((reinterpret_cast<uintptr_t>(it.u) | reinterpret_cast<uintptr_t>(it.y) |
+          reinterpret_cast<uintptr_t>(it.geo)) & 15u) != 0)
+      return aux_fail(FEMTC_ERR_INVALID,
+                      "batch_apply_static: device pointers must be 16-byte aligned");
+    const int n = it.degree + 1, q = it.nquad, slot = n - 2;
+    const int ntab = it.op == FEMTC_OP_STIFFNESS ? 2 : 1;
+    const float* t = static_cast<const float*>(it.tables);
+    for (int w = 0; w < ntab; ++w)
+    {
+      float* dst = b.params.tabs[slot][w];
+      if (slot_set[slot] & (1 << w))
+      {
+        if (std::memcmp(dst, t + w * q * n, sizeof(float) * q * n) != 0)
+          return aux_fail(FEMTC_ERR_INVALID,
+                          "batch_apply_static: meshes of one degree must share their tables");
+      }
+      else
+      {
+        std::memcpy(dst, t + w * q * n, sizeof(float) * q * n);
+        slot_set[slot] |= (char)(1 << w);
+      }
+    }
+    b.items.push_back(it);
+  }
+  std::vector<BatchLayout> lay(kBatchVariants);
+  for (int v = 0; v < kBatchVariants; ++v)
+    lay[v] = batch_default_layout(*fam, v);
+  std::vector<BatchTile> order;
+  int rc = batch_plan(&b, lay, order);
+  if (rc != FEMTC_OK)
+    return rc;
+  std::vector<BatchItem<float>> table;
+  batch_item_table(&b, table);
+  const size_t items_bytes = round256(sizeof(BatchItem<float>) * table.size());
+  const size_t tiles_bytes = sizeof(BatchTile) * order.size();
+  if (items_bytes + tiles_bytes > kStaticScratchBytes)
+  {
+    char msg[200];
+    std::snprintf(msg, sizeof(msg),
+                  "batch_apply_static: %zu tiles exceed the static capacity of %zu tiles "
+                  "(%zu bytes)",
+                  order.size(), (kStaticScratchBytes - items_bytes) / sizeof(BatchTile),
+                  kStaticScratchBytes);
+    return aux_fail(FEMTC_ERR_INVALID, msg);
+  }
+  void* base = nullptr;
+  rc = scratch_address(&base);
+  if (rc != FEMTC_OK)
+    return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* p = static_cast<unsigned char*>(base);
+  cudaError_t e = cudaMemcpyAsync(p, table.data(), sizeof(BatchItem<float>) * table.size(),
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p + items_bytes, order.data(), tiles_bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  b.params.items = reinterpret_cast<const BatchItem<float>*>(p);
+  b.params.tiles = reinterpret_cast<const BatchTile*>(p + items_bytes);
+  void* args[] = {&b.params};
+  e = cudaLaunchKernel(fam->fn, dim3((unsigned)b.grid), dim3(kCellThreads), args, b.smem, st);
+  if (e != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  return FEMTC_OK;
+}

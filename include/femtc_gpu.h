@@ -204,6 +204,22 @@ int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
                        int* geo_staged);
 void femtc_batch_destroy(femtc_batch* b);
 
+/* The batched launch for callers that cannot allocate device memory (code
+ * running while another thread captures a CUDA graph in global mode, apps
+ * whose memory manager owns the device memory, loops that must not take
+ * cudaMalloc's device synchronisation).  No counterpart in the reference.
+ * Same items and kernel as femtc_batch_create + femtc_batch_launch, launched
+ * directly on `stream`; the tile schedule and mesh table go to a fixed 8 MiB
+ * device array of the library (held on every GPU that loads it), so the
+ * call allocates nothing.  Limits: at most 4096 meshes and as many tiles as
+ * fit in 8 MiB (about 349,000); larger batches are rejected with
+ * FEMTC_ERR_INVALID.  The first call on a device sets up the array's address
+ * (cudaGetSymbolAddress): make it before any stream capture.  Every call
+ * reuses the array, so calls whose work overlaps on the GPU (different
+ * streams or threads) race; calls on one stream are ordered. */
+int femtc_batch_apply_static(int dtype, const femtc_batch_item* items,
+                             int nitems, void* stream);
+
 /* ----------------------------------------------------------------------
  * Matrix-free solve of (alpha M + beta K) x = b on a cell-local hexahedral
  * mesh (affine cells): Jacobi-preconditioned CG with a mixed-precision

@@ -1,0 +1,64 @@
+"""GPU: femtc_batch_apply_static, the batched launch for callers that cannot
+allocate device memory (e.g. while another thread captures a CUDA graph in
+global mode, or when their memory manager owns the device memory).
+
+Its schedule lives in the library's fixed device array instead of memory
+from cudaMalloc.  Two calls in a row, on different meshes, must give the
+same results as femtc_batch_create + femtc_batch_launch on the same data,
+within the tolerance the batch tests use for two launches of one mesh.
+This file is collected last (its name), so a stop at the first failure has
+run every other test already; it also passes alone in a fresh process."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def meshes(femtc, dev, seed, dtype):
+    import torch
+    from femtc_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    out = []
+    for P in range(1, 8):
+        for op in (0, 1):
+            n = int(rng.integers(1, 200)) + (seed % 7)
+            w = W.make_custom("s", op, P, P + 2, n, seed=seed * 100 + P * 2 + op)
+            u = torch.from_numpy(w.u).to(dev, torch.float32)
+            g = torch.from_numpy(w.geo).to(dev, torch.float32)
+            out.append([op, P, P + 2, w.tables.astype(np.float32), u, None, g, n])
+    return out
+
+
+@pytest.mark.parametrize("dtype", [1, 3])
+def test_static_batch_matches_batch_launch(femtc, dev, dtype):
+    import torch
+    for seed in (11, 12):  # two calls in a row, different meshes
+        ms = meshes(femtc, dev, seed, dtype)
+        ref_meshes, st_meshes = [], []
+        for m in ms:
+            a, b = list(m), list(m)
+            a[5] = torch.full_like(m[4], float("nan"))
+            b[5] = torch.full_like(m[4], float("nan"))
+            ref_meshes.append(tuple(a))
+            st_meshes.append(tuple(b))
+        batch = femtc.Batch(dtype, ref_meshes)
+        batch.launch()
+        femtc.batch_apply_static(dtype, st_meshes)
+        torch.cuda.synchronize()
+        assert femtc.device_status() == 0
+        for r, s in zip(ref_meshes, st_meshes):
+            yr = r[5].double().cpu().numpy()
+            ys = s[5].double().cpu().numpy()
+            assert np.isfinite(ys).all()
+            assert np.abs(ys - yr).max() <= 1e-6 * np.abs(yr).max()
+        batch.close()
+
+
+def test_static_batch_rejects_oversize(femtc, dev):
+    import torch
+    # more meshes than the static mesh table holds
+    u = torch.zeros(64, dtype=torch.float32, device=dev)
+    t = np.zeros(2 * 5 * 4, dtype=np.float32)
+    one = (0, 3, 5, t, u, u, u, 1)
+    with pytest.raises(femtc.FemtcError):
+        femtc.batch_apply_static(1, [one] * 5000)

@@ -54,18 +54,28 @@ def bytes_per_cell(op: int, n: int, q: int, es: int) -> float:
     return es * (2 * n ** 3 + (1 if op == 0 else 6) * q ** 3)
 
 
-def roofline(head, ach_tf, ach_gbs, hbm, hbm_src):
+# DRAM bytes (read + write) of one launch of the headline kernel, measured
+# by ncu on the full workload (profiles/stiffness_p4_32k_cells_slab_kernels.md)
+MEASURED_TRAFFIC = {("stiffness_p4", 32768, 0): 399.3e6, ("stiffness_p4", 32768, 1): 196.4e6}
+
+
+def traffic_for(workload, ncells, dtype):
+    return MEASURED_TRAFFIC.get((workload, ncells, dtype))
+
+
+def roofline(head, ach_tf, ach_gbs, hbm, hbm_src, traffic=None):
     """The binding roof of the headline kernel: the FP64 pipe for FP64 (its
     arithmetic intensity puts it far above the FP64 ridge), HBM otherwise."""
     hbm_part = {"achieved": ach_gbs, "peak": hbm, "unit": "GB/s", "frac": ach_gbs / hbm,
                 "peak_source": hbm_src}
     if head == 0:
         return {"bound": "fp64", "achieved": ach_tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                "frac": ach_tf / FP64_PEAK_TFLOPS, "traffic": None,
+                "frac": ach_tf / FP64_PEAK_TFLOPS, "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu, profiles/stiffness_p4_32k_cells_slab_kernels.md)",
                 "peak_source": "measured FP64 FMA pipe (profiles/gb300_pipe_peaks.md)",
                 "hbm": hbm_part}
     return {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s", "frac": ach_gbs / hbm,
-            "traffic": None, "peak_source": hbm_src}
+            "traffic": traffic, "peak_source": hbm_src}
 
 
 def dist_env():
@@ -478,7 +488,10 @@ def main():
     if args.tile_db and not tuned and rank == 0:
         F.tile_db_save(args.tile_db)
 
-    # end-to-end through the host-buffer C-ABI entry point, pinned buffers
+    # end-to-end through the host-buffer C-ABI entry point, pinned buffers:
+    # mode 0 lets the kernel stream the host buffers over the coherent
+    # Grace-Blackwell link (zero-copy), mode 1 stages them through device
+    # copies; both include every byte's host->device and device->host move
     e2e = {}
     for dtype in ([] if args.no_e2e else [head]):
         npdt = np.float64 if dtype == F.F64 else np.float32
@@ -489,17 +502,22 @@ def main():
         def estep():
             F.apply_host(op, dtype, F.EXACT, w.degree, q, w.tables, uh, yh, gh, w.ncells)
 
-        for _ in range(args.warmup):
-            estep()
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            estep()
-        barrier()
-        el = maxreduce(time.perf_counter() - t0)
-        e2e[dtype] = dict(gdofs=world * args.steps * w.ndofs / el / 1e9,
-                          h2d=uh.numel() * uh.element_size() + gh.numel() * gh.element_size(),
-                          d2h=yh.numel() * yh.element_size())
+        # tile tuning of the zero-copy path (setup, outside the timed region)
+        F.autotune_host(op, dtype, F.EXACT, w.degree, q, w.tables, uh, yh, gh, w.ncells)
+        for mode in (0, 1):
+            F.set_host_path(mode)
+            for _ in range(args.warmup):
+                estep()
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                estep()
+            barrier()
+            el = maxreduce(time.perf_counter() - t0)
+            e2e[(dtype, mode)] = dict(gdofs=world * args.steps * w.ndofs / el / 1e9,
+                                      h2d=uh.numel() * uh.element_size() + gh.numel() * gh.element_size(),
+                                      d2h=yh.numel() * yh.element_size())
+        F.set_host_path(0)
 
     r = results[head]
     value = world * args.steps * w.ndofs / (r["total_ms"] * 1e-3) / 1e9
@@ -517,7 +535,8 @@ def main():
             "hbm_gbs": bytes_per_cell(op, n, q, es) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
             "tflops": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
             "max_rel_err_vs_fp64_oracle": res["err"],
-            "tile": {"cells": res["tile"][0], "geo_staged": res["tile"][1], "threads": res["tile"][2]},
+            "tile": {"cells": res["tile"][0], "geo_staged": res["tile"][1], "threads": res["tile"][2],
+                     "lanes_per_slab": res["tile"][3]},
         }
     if rank == 0:
         line = {
@@ -529,14 +548,18 @@ def main():
             "config": {"workload": args.workload, "cells": w.ncells, "degree": w.degree, "nquad": q,
                        "dofs": w.ndofs, "parallelism": f"replicas{world}",
                        "l2": f"inputs {bpc * w.ncells / 1e6:.0f} MB > 129 MB L2, no flush"},
-            "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src),
-            "gpu_launches": args.steps * (len(dtypes) + (0 if args.no_e2e else 1)),
+            "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src,
+                                 traffic_for(args.workload, w.ncells, head)),
+            "gpu_launches": args.steps * (len(dtypes) + (0 if args.no_e2e else 2)),
             "clocks": r["clocks"],
             "variants": variants,
         }
-        if head in e2e:
-            line["e2e"] = {"value": e2e[head]["gdofs"], "unit": "GDoF/s",
-                           "h2d_bytes_per_step": e2e[head]["h2d"], "d2h_bytes_per_step": e2e[head]["d2h"]}
+        if (head, 0) in e2e:
+            z, c = e2e[(head, 0)], e2e[(head, 1)]
+            line["e2e"] = {"value": z["gdofs"], "unit": "GDoF/s",
+                           "h2d_bytes_per_step": z["h2d"], "d2h_bytes_per_step": z["d2h"],
+                           "path": "femtc_*_apply_host, pinned buffers, zero-copy over the host link",
+                           "staging_copies_gdofs": c["gdofs"]}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(w)
         print(json.dumps(line), flush=True)

@@ -45,13 +45,16 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_stiffness_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
         "femtc_mass_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_stiffness_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
-        "femtc_set_tile_config": ([c_int] * 8, c_int),
-        "femtc_get_tile_config": ([c_int] * 5 + [ctypes.POINTER(c_int)] * 3, c_int),
+        "femtc_set_tile_config": ([c_int] * 9, c_int),
+        "femtc_get_tile_config": ([c_int] * 5 + [ctypes.POINTER(c_int)] * 4, c_int),
         "femtc_autotune": ([c_int] * 5 + [vp] * 4 + [c_size, vp] + [ctypes.POINTER(c_int)] * 3
                            + [ctypes.POINTER(ctypes.c_float)], c_int),
+        "femtc_autotune_host": ([c_int] * 5 + [vp] * 4 + [c_size] + [ctypes.POINTER(c_int)] * 3
+                                + [ctypes.POINTER(ctypes.c_float)], c_int),
         "femtc_tile_db_save": ([ctypes.c_char_p], c_int),
         "femtc_tile_db_load": ([ctypes.c_char_p], c_int),
         "femtc_tabulate": ([c_int, c_int, dp, dp, dp, dp], c_int),
+        "femtc_set_host_path": ([c_int], c_int),
         "femtc_gemm_blocked": ([c_int] * 4 + [vp] * 3 + [c_size, vp], c_int),
         "femtc_apply_contractions": ([c_int] * 4 + [vp] * 5 + [c_size, vp], c_int),
         "femtc_geometry": ([c_int, c_int, vp, vp, c_int, vp, vp, c_size, vp], c_int),
@@ -160,21 +163,28 @@ def apply_host(op: int, dtype: int, semantics: int, degree: int, nquad: int,
              ptr(geo), ncells))
 
 
+def set_host_path(mode: int) -> None:
+    """0 auto (zero-copy for pinned buffers), 1 staging copies, 2 zero-copy only."""
+    check(load().femtc_set_host_path(mode))
+
+
 def supported(op: int, dtype: int, semantics: int, degree: int, nquad: int) -> bool:
     return bool(load().femtc_supported(op, dtype, semantics, degree, nquad))
 
 
-def set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged, threads=256) -> None:
+def set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged, threads=256,
+                    lanes=0) -> None:
     check(load().femtc_set_tile_config(op, dtype, semantics, degree, nquad, cb, geo_staged,
-                                       threads))
+                                       threads, lanes))
 
 
 def get_tile_config(op, dtype, semantics, degree, nquad):
-    """(cells per tile, geometry staged, threads per CTA)."""
-    cb, st, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    """(cells per tile, geometry staged, threads per CTA, lanes per slab)."""
+    cb, st, nt, ln = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     check(load().femtc_get_tile_config(op, dtype, semantics, degree, nquad,
-                                       ctypes.byref(cb), ctypes.byref(st), ctypes.byref(nt)))
-    return cb.value, st.value, nt.value
+                                       ctypes.byref(cb), ctypes.byref(st), ctypes.byref(nt),
+                                       ctypes.byref(ln)))
+    return cb.value, st.value, nt.value, ln.value
 
 
 def autotune(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells, stream=None):
@@ -186,6 +196,18 @@ def autotune(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells, str
     check(load().femtc_autotune(op, dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u),
                                 ptr(y), ptr(geo), ncells, stream_ptr(stream), ctypes.byref(cb),
                                 ctypes.byref(st), ctypes.byref(nt), ctypes.byref(ms)))
+    return cb.value, st.value, nt.value, ms.value
+
+
+def autotune_host(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells):
+    """Tile tuning of the zero-copy host path on pinned host buffers.
+    Returns (cb, geo_staged, threads, ms)."""
+    cb, st, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ms = ctypes.c_float()
+    tab = host_tables(tables, dtype)
+    check(load().femtc_autotune_host(op, dtype, semantics, degree, nquad, tab.ctypes.data,
+                                     ptr(u), ptr(y), ptr(geo), ncells, ctypes.byref(cb),
+                                     ctypes.byref(st), ctypes.byref(nt), ctypes.byref(ms)))
     return cb.value, st.value, nt.value, ms.value
 
 

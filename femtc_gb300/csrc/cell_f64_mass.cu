@@ -1,3 +1,3 @@
-// CUDA-core mass cell kernels, double arithmetic and storage.
+// CUDA-core mass cell kernels, double arithmetic and storage, one lane per slab.
 #include "cell_inst.cuh"
-FEMTC_CELL_UNIT(register_cell_f64_mass, double, 0, OP_MASS)
+FEMTC_CELL_UNIT(register_cell_f64_mass, double, 0, OP_MASS, 1)

@@ -9,7 +9,7 @@
 
 namespace femtc
 {
-template <typename T, int N, int Q, int OP, int SEM>
+template <typename T, int N, int Q, int OP, int SEM, int L>
 unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
 {
   CellParams<T> p{};
@@ -17,40 +17,42 @@ unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
   p.geo_staged = staged;
   p.sq = sq;
   p.sbc = sbc;
-  return tile_layout<T, SlabTile<T, N, Q, OP, SEM>, N, Q,
+  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L>, N, Q,
                      (OP == OP_MASS) ? 1 : 6>(p)
       .total;
 }
 
-template <typename T, int N, int Q, int OP, int SEM>
+template <typename T, int N, int Q, int OP, int SEM, int L>
 void add_variant(std::vector<CellVariant>& v, int dtype)
 {
   v.push_back(CellVariant{dtype, OP, SEM, N, Q,
                           reinterpret_cast<const void*>(
-                              &cell_kernel<T, N, Q, OP, SEM>),
-                          &cell_smem_bytes<T, N, Q, OP, SEM>, 1, (int)sizeof(T)});
+                              &cell_kernel<T, N, Q, OP, SEM, L>),
+                          &cell_smem_bytes<T, N, Q, OP, SEM, L>, 1, (int)sizeof(T),
+                          L});
 }
 
-template <typename T, int OP, int N>
+template <typename T, int OP, int N, int L>
 void add_degree(std::vector<CellVariant>& v, int dtype)
 {
-  add_variant<T, N, N, OP, SEM_EXACT>(v, dtype);
-  add_variant<T, N, N + 1, OP, SEM_EXACT>(v, dtype);
+  add_variant<T, N, N, OP, SEM_EXACT, L>(v, dtype);
+  add_variant<T, N, N + 1, OP, SEM_EXACT, L>(v, dtype);
   if constexpr (N + 2 <= kMaxQ)
-    add_variant<T, N, N + 2, OP, SEM_EXACT>(v, dtype);
-  add_variant<T, N, N, OP, SEM_REFERENCE>(v, dtype);
+    add_variant<T, N, N + 2, OP, SEM_EXACT, L>(v, dtype);
+  add_variant<T, N, N, OP, SEM_REFERENCE, L>(v, dtype);
 }
 
-template <typename T, int OP>
+// L = lanes sharing one slab (1 or 2; see SlabTile)
+template <typename T, int OP, int L>
 void add_all(std::vector<CellVariant>& v, int dtype)
 {
-  add_degree<T, OP, 2>(v, dtype);
-  add_degree<T, OP, 3>(v, dtype);
-  add_degree<T, OP, 4>(v, dtype);
-  add_degree<T, OP, 5>(v, dtype);
-  add_degree<T, OP, 6>(v, dtype);
-  add_degree<T, OP, 7>(v, dtype);
-  add_degree<T, OP, 8>(v, dtype);
+  add_degree<T, OP, 2, L>(v, dtype);
+  add_degree<T, OP, 3, L>(v, dtype);
+  add_degree<T, OP, 4, L>(v, dtype);
+  add_degree<T, OP, 5, L>(v, dtype);
+  add_degree<T, OP, 6, L>(v, dtype);
+  add_degree<T, OP, 7, L>(v, dtype);
+  add_degree<T, OP, 8, L>(v, dtype);
 }
 
 inline unsigned read_clear_fault_word()
@@ -64,12 +66,12 @@ inline unsigned read_clear_fault_word()
 }
 } // namespace femtc
 
-#define FEMTC_CELL_UNIT(NAME, T, DTYPE, OP)                                    \
+#define FEMTC_CELL_UNIT(NAME, T, DTYPE, OP, L)                                 \
   namespace femtc                                                              \
   {                                                                            \
   void NAME(std::vector<CellVariant>& v, std::vector<FaultReader>& f)          \
   {                                                                            \
-    add_all<T, OP>(v, DTYPE);                                                  \
+    add_all<T, OP, L>(v, DTYPE);                                               \
     f.push_back(&read_clear_fault_word);                                       \
   }                                                                            \
   }

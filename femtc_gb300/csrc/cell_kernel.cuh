@@ -62,6 +62,8 @@ struct CellParams
   int geo_staged;    // 1: geometry slab staged by TMA, 0: read in the fused pass
   int sq;            // slab kernels: stride of one i0 slab in the work buffers
   int sbc;           // slab kernels: stride of one cell in the work buffers
+  int host_io;       // 1: u, geo, y are host memory read/written over the
+                     // coherent host link with plain vector accesses (no TMA)
   T tab[2][kMaxQ * kMaxN]; // Phi(q,i) = tab[0][q + i*Q], Gamma = tab[1]
 };
 
@@ -206,7 +208,9 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   }
   __syncthreads();
 
-  auto is_full = [&](long long t) { return (t + 1) * cb <= p.ncells; };
+  // TMA moves full tiles of device memory; host-resident operands and the
+  // ragged last tile go through plain vector loads and stores
+  auto is_full = [&](long long t) { return !p.host_io && (t + 1) * cb <= p.ncells; };
   // warp 0 only: TMA loads of tile t into stage s
   auto issue = [&](long long t, int s) {
     if (lane == 0)
@@ -237,12 +241,37 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     const long long next = tile + gridDim.x;
     if (warp0 && next < ntiles && is_full(next))
       issue(next, s ^ 1);
-    const bool full = is_full(tile);
-    const int ncb = full ? cb : (int)(p.ncells - tile * cb);
+    const bool full = is_full(tile); // loaded and stored by TMA
+    // cells in this tile (never more than the stage holds)
+    const int ncb = (int)((p.ncells - tile * cb) < cb ? (p.ncells - tile * cb) : cb);
     bool ok = true;
     if (full)
     {
       ok = mbar_wait(&bar[s], (unsigned)(it >> 1) & 1u);
+    }
+    else if (p.host_io && ncb == cb)
+    {
+      // host-resident full tile: 16-byte vector loads (tile starts and slab
+      // lengths are multiples of 16 bytes: cb % 4 == 0 and N*N % 4 == 0
+      // whenever slabs are padded)
+      using V = uint4;
+      constexpr int W = 16 / sizeof(T);
+      const V* gu = reinterpret_cast<const V*>(p.u + tile * cb * N3);
+      const int nv = cb * N3 / W;
+#pragma unroll 4
+      for (int i = threadIdx.x; i < nv; i += blockDim.x)
+      {
+        const int e = i * W;
+        *reinterpret_cast<V*>(su(s) + (e / N2) * US + (e % N2)) = gu[i];
+      }
+      if (staged)
+      {
+        const V* gg = reinterpret_cast<const V*>(p.geo + tile * cb * Q3NC);
+        V* dg = reinterpret_cast<V*>(sg(s));
+#pragma unroll 4
+        for (int i = threadIdx.x; i < cb * Q3NC / W; i += blockDim.x)
+          dg[i] = gg[i];
+      }
     }
     else
     {
@@ -293,6 +322,20 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
         bulk_commit();
       }
     }
+    else if (p.host_io && ncb == cb)
+    {
+      __syncthreads();
+      using V = uint4;
+      constexpr int W = 16 / sizeof(T);
+      V* gy = reinterpret_cast<V*>(p.y + tile * cb * N3);
+      const int nv = cb * N3 / W;
+#pragma unroll 4
+      for (int i = threadIdx.x; i < nv; i += blockDim.x)
+      {
+        const int e = i * W;
+        gy[i] = *reinterpret_cast<const V*>(sy + (e / N2) * US + (e % N2));
+      }
+    }
     else
     {
       __syncthreads();
@@ -328,10 +371,10 @@ __host__ __device__ constexpr int slab_lanes()
   return sizeof(T) == 4 ? 2 : 1; // FP32: more busy lanes; FP64: pipe-bound
 }
 
-template <typename T, int N, int Q, int OP, int SEM>
+template <typename T, int N, int Q, int OP, int SEM, int LANES = slab_lanes<T>()>
 struct SlabTile
 {
-  static constexpr int S = slab_lanes<T>();
+  static constexpr int S = LANES;
   static constexpr bool kSlabCopies = (N % 2 == 0);
   static constexpr int US = slab_stride<T>(N);
   static constexpr int N2 = N * N, Q2 = Q * Q, Q3 = Q * Q * Q;
@@ -665,11 +708,11 @@ struct SlabTile
   }
 };
 
-template <typename T, int N, int Q, int OP, int SEM>
+template <typename T, int N, int Q, int OP, int SEM, int LANES>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  stream_tiles<T, SlabTile<T, N, Q, OP, SEM>, N, Q, (OP == OP_MASS) ? 1 : 6>(p);
+  stream_tiles<T, SlabTile<T, N, Q, OP, SEM, LANES>, N, Q, (OP == OP_MASS) ? 1 : 6>(p);
 }
 
 } // namespace femtc

@@ -54,8 +54,10 @@ Registry& registry()
   std::call_once(once, [] {
     register_cell_f64_mass(r.cells, r.faults);
     register_cell_f64_stiffness(r.cells, r.faults);
-    register_cell_f32_mass(r.cells, r.faults);
-    register_cell_f32_stiffness(r.cells, r.faults);
+    register_cell_f32_mass_l1(r.cells, r.faults);
+    register_cell_f32_mass_l2(r.cells, r.faults);
+    register_cell_f32_stiffness_l1(r.cells, r.faults);
+    register_cell_f32_stiffness_l2(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);
     register_mma_f16x2_stiffness(r.cells, r.faults);
     register_mma_bf16x3_mass(r.cells, r.faults);
@@ -64,13 +66,26 @@ Registry& registry()
   return r;
 }
 
-const CellVariant* find_cell(int op, int dtype, int sem, int n, int q)
+// The compiled variant of (op, dtype, semantics, n, q) with `lanes` lanes
+// per slab (lanes <= 0: any).
+const CellVariant* find_cell(int op, int dtype, int sem, int n, int q,
+                             int lanes = 0)
 {
   for (const CellVariant& v : registry().cells)
     if (v.op == op && v.dtype == dtype && v.sem == sem && v.n == n &&
-        v.q == q)
+        v.q == q && (lanes <= 0 || v.lanes == lanes))
       return &v;
   return nullptr;
+}
+
+// Built-in choice of lanes per slab where both are compiled (FP32): two
+// lanes pay off for the stiffness operator of low degree, whose slabs carry
+// three outputs; one lane elsewhere.
+int default_lanes(int op, int dtype, int n)
+{
+  if (dtype != FEMTC_F32)
+    return 1;
+  return (op == FEMTC_OP_STIFFNESS && n <= 5) ? 2 : 1;
 }
 
 // ---------------------------------------------------------------- tiles --
@@ -78,9 +93,10 @@ using Key = std::tuple<int, int, int, int, int>; // op dtype sem n q
 std::mutex g_cfg_mutex;
 struct TileChoice
 {
-  int cb, staged, nt;
+  int cb, staged, nt, lanes;
 };
-std::map<Key, TileChoice> g_tile_cfg;
+std::map<Key, TileChoice> g_tile_cfg;      // device-resident operands
+std::map<Key, TileChoice> g_tile_cfg_host; // host-resident (zero-copy) operands
 
 
 
@@ -141,13 +157,12 @@ int wavefronts(const long long* a, int esize)
 // slab (addresses c*sbc + i0*sq + const), the fused pass with one thread per
 // pencil (c, r) (addresses c*sbc + r + const).  Pick the strides that
 // minimise the modelled bank-conflict wavefronts of both patterns.
-std::pair<int, int> slab_layout(int n, int q, int esize)
+std::pair<int, int> slab_layout(int n, int q, int esize, int lanes)
 {
-  const int lanes = esize == 4 ? 2 : 1; // lanes per slab (slab_lanes<T>())
   static std::mutex m;
-  static std::map<std::tuple<int, int, int>, std::pair<int, int>> cache;
+  static std::map<std::tuple<int, int, int, int>, std::pair<int, int>> cache;
   std::lock_guard<std::mutex> lk(m);
-  auto key = std::make_tuple(n, q, esize);
+  auto key = std::make_tuple(n, q, esize, lanes);
   auto it = cache.find(key);
   if (it != cache.end())
     return it->second;
@@ -198,7 +213,7 @@ double lane_efficiency(const CellVariant& v, int cb, int nt)
   if (v.slab)
   {
     passes = 3; // slabs forward, pencils fused, slabs backward
-    const double lanes = v.esize == 4 ? 2 : 1;
+    const double lanes = v.lanes;
     np[0] = n * cb * lanes; wk[0] = q * n * (n + q) / lanes;
     np[1] = q * q * cb;     wk[1] = 2 * q * n;
     np[2] = n * cb * lanes; wk[2] = q * n * (n + q) / lanes;
@@ -233,7 +248,7 @@ TileCfg with_layout(const CellVariant& v, int cb, int staged, int nt)
   TileCfg c{cb, staged, nt, 0, 0};
   if (v.slab)
   {
-    auto l = slab_layout(v.n, v.q, v.esize);
+    auto l = slab_layout(v.n, v.q, v.esize, v.lanes);
     c.sq = l.first;
     c.sbc = l.second;
   }
@@ -282,15 +297,40 @@ TileCfg default_tile(const CellVariant& v)
   return best_cfg;
 }
 
-TileCfg tile_config(const CellVariant& v)
+// The variant (lanes per slab) and tile shape used for a key: the stored
+// configuration if any, else the built-in choice.
+std::pair<const CellVariant*, TileCfg> select_variant(int op, int dtype, int sem,
+                                                      int n, int q, bool host = false)
 {
   {
     std::lock_guard<std::mutex> lk(g_cfg_mutex);
-    auto it = g_tile_cfg.find(Key(v.op, v.dtype, v.sem, v.n, v.q));
-    if (it != g_tile_cfg.end())
-      return with_layout(v, it->second.cb, it->second.staged, it->second.nt);
+    auto it = g_tile_cfg.end();
+    if (host)
+    {
+      it = g_tile_cfg_host.find(Key(op, dtype, sem, n, q));
+      if (it == g_tile_cfg_host.end())
+        it = g_tile_cfg.end();
+    }
+    if (it == g_tile_cfg.end())
+      it = g_tile_cfg.find(Key(op, dtype, sem, n, q));
+    if (it != g_tile_cfg.end() && it != g_tile_cfg_host.end())
+    {
+      const CellVariant* v = find_cell(op, dtype, sem, n, q, it->second.lanes);
+      if (v)
+        return {v, with_layout(*v, it->second.cb, it->second.staged, it->second.nt)};
+    }
   }
-  return default_tile(v);
+  const CellVariant* v = find_cell(op, dtype, sem, n, q, default_lanes(op, dtype, n));
+  if (!v)
+    v = find_cell(op, dtype, sem, n, q);
+  if (!v)
+    return {nullptr, TileCfg{}};
+  return {v, default_tile(*v)};
+}
+
+TileCfg tile_config(const CellVariant& v)
+{
+  return select_variant(v.op, v.dtype, v.sem, v.n, v.q).second;
 }
 
 // -------------------------------------------------------- launch helpers --
@@ -380,7 +420,7 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
 template <typename T>
 int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
                 const void* u, void* y, const void* geo, size_t ncells,
-                cudaStream_t stream)
+                cudaStream_t stream, int host_io = 0)
 {
   if (!aligned16(u) || !aligned16(y) || !aligned16(geo))
     return fail(FEMTC_ERR_INVALID,
@@ -396,6 +436,7 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
   p.geo_staged = cfg.staged;
   p.sq = cfg.sq;
   p.sbc = cfg.sbc;
+  p.host_io = host_io;
   const int ntab = (v.op == FEMTC_OP_STIFFNESS) ? 2 : 1;
   for (int t = 0; t < ntab; ++t)
     for (int i = 0; i < v.n * v.q; ++i)
@@ -418,13 +459,14 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
 
 int launch_variant(const CellVariant& v, const TileCfg& cfg,
                    const void* tables, const void* u, void* y,
-                   const void* geo, size_t ncells, cudaStream_t st)
+                   const void* geo, size_t ncells, cudaStream_t st,
+                   int host_io = 0)
 {
   if (v.dtype == FEMTC_F64)
     return launch_cell<double>(v, cfg, static_cast<const double*>(tables), u,
-                               y, geo, ncells, st);
+                               y, geo, ncells, st, host_io);
   return launch_cell<float>(v, cfg, static_cast<const float*>(tables), u, y,
-                            geo, ncells, st);
+                            geo, ncells, st, host_io);
 }
 
 int apply(int op, int dtype, int sem, int degree, int nquad,
@@ -437,7 +479,8 @@ int apply(int op, int dtype, int sem, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return FEMTC_OK;
-  return launch_variant(*v, tile_config(*v), tables, u, y, geo, ncells,
+  const auto sel = select_variant(op, dtype, sem, degree + 1, nquad);
+  return launch_variant(*sel.first, sel.second, tables, u, y, geo, ncells,
                         static_cast<cudaStream_t>(stream));
 }
 
@@ -453,6 +496,23 @@ struct HostPath
   size_t cap[3] = {0, 0, 0};
 };
 HostPath g_host;
+int g_host_mode = 0; // 0 auto, 1 staging copies, 2 zero-copy only
+
+// Device address of a pinned (page-locked, mapped) host buffer; false for
+// pageable or device memory.
+bool device_view(const void* p, const void** out)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+  {
+    cudaGetLastError(); // clear the sticky-free error of an unknown pointer
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+    return false;
+  *out = a.devicePointer;
+  return true;
+}
 
 int host_buffer(int i, size_t bytes)
 {
@@ -483,6 +543,28 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
   std::lock_guard<std::mutex> lk(g_host.m);
   int dev = 0;
   cudaGetDevice(&dev);
+  // Pinned host buffers: the kernel reads u and the geometry and writes y
+  // over the coherent host link directly (no staging copies).
+  const void* du = nullptr;
+  void* dy = nullptr;
+  const void* dg = nullptr;
+  if (g_host_mode != 1 && device_view(u, &du) && device_view(y, (const void**)&dy) &&
+      device_view(geo, &dg))
+  {
+    if (!g_host.stream &&
+        cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(FEMTC_ERR_CUDA, "cudaStreamCreate failed");
+    if (!aligned16(du) || !aligned16(dy) || !aligned16(dg))
+      return fail(FEMTC_ERR_INVALID, "host buffers must be 16-byte aligned");
+    const auto sel = select_variant(op, dtype, sem, degree + 1, nquad, true);
+    rc = launch_variant(*sel.first, sel.second, tables, du, dy, dg, ncells, g_host.stream, 1);
+    if (rc != FEMTC_OK)
+      return rc;
+    cudaError_t e = cudaStreamSynchronize(g_host.stream);
+    return e == cudaSuccess ? FEMTC_OK : cuda_fail(e, "cudaStreamSynchronize");
+  }
+  if (g_host_mode == 2)
+    return fail(FEMTC_ERR_INVALID, "zero-copy host mode needs pinned host buffers");
   if (g_host.device != dev)
   {
     // a different device: drop buffers of the old one (they stay valid on
@@ -608,11 +690,17 @@ int aux_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 
 std::pair<int, int> slab_layout_for(int n, int q, int esize)
 {
-  return slab_layout(n, q, esize);
+  // the batch kernels run the slab tiles with their default lanes
+  return slab_layout(n, q, esize, esize == 4 ? 2 : 1);
 }
 } // namespace femtc
 
 using namespace femtc;
+
+int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
+                  const void* tables, const void* u, void* y, const void* geo,
+                  size_t ncells, cudaStream_t st, int host_io, int* cb,
+                  int* geo_staged, int* threads, float* best_ms);
 
 extern "C" {
 
@@ -668,10 +756,21 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
                     tables, u, y, G, ncells);
 }
 
-int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int cb, int geo_staged, int threads)
+int femtc_set_host_path(int mode)
 {
-  const CellVariant* v = find_cell(op, dtype, semantics, degree + 1, nquad);
+  if (mode < 0 || mode > 2)
+    return fail(FEMTC_ERR_INVALID, "host path mode: 0 auto, 1 copies, 2 zero-copy");
+  g_host_mode = mode;
+  return FEMTC_OK;
+}
+
+int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
+                          int nquad, int cb, int geo_staged, int threads,
+                          int lanes)
+{
+  if (lanes <= 0)
+    lanes = default_lanes(op, dtype, degree + 1);
+  const CellVariant* v = find_cell(op, dtype, semantics, degree + 1, nquad, lanes);
   if (!v)
     return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
   std::lock_guard<std::mutex> lk(g_cfg_mutex);
@@ -692,7 +791,7 @@ int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
       smem_of(*v, with_layout(*v, cb, geo_staged ? 1 : 0, threads));
   if (need > 227u * 1024u)
     return fail(FEMTC_ERR_INVALID, "tile needs %u B of shared memory", need);
-  g_tile_cfg[k] = TileChoice{cb, geo_staged ? 1 : 0, threads};
+  g_tile_cfg[k] = TileChoice{cb, geo_staged ? 1 : 0, threads, v->lanes};
   return FEMTC_OK;
 }
 
@@ -701,6 +800,36 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
                    const void* geo, size_t ncells, void* stream, int* cb,
                    int* geo_staged, int* threads, float* best_ms)
 {
+  return autotune_impl(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells,
+                       static_cast<cudaStream_t>(stream), 0, cb, geo_staged, threads,
+                       best_ms);
+}
+
+int femtc_autotune_host(int op, int dtype, int semantics, int degree,
+                        int nquad, const void* tables, const void* u, void* y,
+                        const void* geo, size_t ncells, int* cb,
+                        int* geo_staged, int* threads, float* best_ms)
+{
+  const void *du = nullptr, *dg = nullptr;
+  void* dy = nullptr;
+  if (!u || !y || !geo || !device_view(u, &du) || !device_view(y, (const void**)&dy) ||
+      !device_view(geo, &dg))
+    return fail(FEMTC_ERR_INVALID, "autotune_host needs pinned host buffers");
+  std::lock_guard<std::mutex> lk(g_host.m);
+  if (!g_host.stream &&
+      cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(FEMTC_ERR_CUDA, "cudaStreamCreate failed");
+  return autotune_impl(op, dtype, semantics, degree, nquad, tables, du, dy, dg, ncells,
+                       g_host.stream, 1, cb, geo_staged, threads, best_ms);
+}
+
+} // extern "C"
+
+int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
+                  const void* tables, const void* u, void* y, const void* geo,
+                  size_t ncells, cudaStream_t st, int host_io, int* cb,
+                  int* geo_staged, int* threads, float* best_ms)
+{
   const CellVariant* v = nullptr;
   int rc = check_common(op, dtype, semantics, degree, nquad, tables, u, y,
                         geo, &v);
@@ -708,41 +837,49 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return fail(FEMTC_ERR_INVALID, "autotune needs at least one cell");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   // candidates: for each (staging, threads), the cell counts per tile with
   // the best lane efficiency that fit in shared memory
-  std::vector<TileCfg> cands;
-  for (int staged = 0; staged <= 1; ++staged)
-    for (int nt : {64, 128, 256})
-    {
-      std::vector<std::pair<double, TileCfg>> opts;
-      for (int c = 4; c <= 128; c += 4)
+  std::vector<std::pair<const CellVariant*, TileCfg>> cands;
+  for (int lanes = 1; lanes <= 2; ++lanes)
+  {
+    const CellVariant* lv = find_cell(op, dtype, semantics, degree + 1, nquad, lanes);
+    if (!lv)
+      continue;
+    for (int staged = 0; staged <= 1; ++staged)
+      for (int nt : {64, 128, 256})
       {
-        const TileCfg t = with_layout(*v, c, staged, nt);
-        if (smem_of(*v, t) > 227u * 1024u)
-          break;
-        opts.push_back({lane_efficiency(*v, c, nt) + 1e-4 * c, t});
+        std::vector<std::pair<double, TileCfg>> opts;
+        for (int c = 4; c <= 128; c += 4)
+        {
+          const TileCfg t = with_layout(*lv, c, staged, nt);
+          if (smem_of(*lv, t) > 227u * 1024u)
+            break;
+          opts.push_back({lane_efficiency(*lv, c, nt) + 1e-4 * c, t});
+        }
+        std::sort(opts.begin(), opts.end(),
+                  [](const auto& a, const auto& b) { return a.first > b.first; });
+        for (size_t i = 0; i < opts.size() && i < 4; ++i)
+          cands.push_back({lv, opts[i].second});
       }
-      std::sort(opts.begin(), opts.end(),
-                [](const auto& a, const auto& b) { return a.first > b.first; });
-      for (size_t i = 0; i < opts.size() && i < 4; ++i)
-        cands.push_back(opts[i].second);
-    }
+  }
   if (cands.empty())
     return fail(FEMTC_ERR_UNSUPPORTED, "no tile shape fits in shared memory");
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  TileCfg best_cfg = cands[0];
-  for (const TileCfg& c : cands)
+  TileCfg best_cfg = cands[0].second;
+  const CellVariant* best_v = cands[0].first;
+  for (const auto& cand : cands)
   {
-    rc = launch_variant(*v, c, tables, u, y, geo, ncells, st);
+    const CellVariant* cv = cand.first;
+    const TileCfg& c = cand.second;
+    rc = launch_variant(*cv, c, tables, u, y, geo, ncells, st, host_io);
     if (rc != FEMTC_OK)
       continue; // e.g. does not fit on an SM with these registers
     cudaEventRecord(e0, st);
     for (int r = 0; r < 3; ++r)
-      launch_variant(*v, c, tables, u, y, geo, ncells, st);
+      launch_variant(*cv, c, tables, u, y, geo, ncells, st, host_io);
     cudaEventRecord(e1, st);
     cudaError_t e = cudaEventSynchronize(e1);
     if (e != cudaSuccess)
@@ -758,6 +895,7 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
     {
       best = ms;
       best_cfg = c;
+      best_v = cv;
     }
   }
   cudaEventDestroy(e0);
@@ -766,8 +904,8 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
     return fail(FEMTC_ERR_UNSUPPORTED, "no tile candidate could be launched");
   {
     std::lock_guard<std::mutex> lk(g_cfg_mutex);
-    g_tile_cfg[Key(op, dtype, semantics, degree + 1, nquad)] =
-        TileChoice{best_cfg.cb, best_cfg.staged, best_cfg.nt};
+    (host_io ? g_tile_cfg_host : g_tile_cfg)[Key(op, dtype, semantics, degree + 1, nquad)] =
+        TileChoice{best_cfg.cb, best_cfg.staged, best_cfg.nt, best_v->lanes};
   }
   if (cb)
     *cb = best_cfg.cb;
@@ -780,6 +918,8 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
   return FEMTC_OK;
 }
 
+extern "C" {
+
 int femtc_tile_db_save(const char* path)
 {
   if (!path)
@@ -788,12 +928,12 @@ int femtc_tile_db_save(const char* path)
   if (!f)
     return fail(FEMTC_ERR_INVALID, "cannot open %s for writing", path);
   std::lock_guard<std::mutex> lk(g_cfg_mutex);
-  std::fprintf(f, "# femtc tile db: op dtype semantics n q cb geo_staged threads\n");
+  std::fprintf(f, "# femtc tile db: op dtype semantics n q cb geo_staged threads lanes\n");
   for (const auto& kv : g_tile_cfg)
-    std::fprintf(f, "%d %d %d %d %d %d %d %d\n", std::get<0>(kv.first),
+    std::fprintf(f, "%d %d %d %d %d %d %d %d %d\n", std::get<0>(kv.first),
                  std::get<1>(kv.first), std::get<2>(kv.first),
                  std::get<3>(kv.first), std::get<4>(kv.first), kv.second.cb,
-                 kv.second.staged, kv.second.nt);
+                 kv.second.staged, kv.second.nt, kv.second.lanes);
   std::fclose(f);
   return FEMTC_OK;
 }
@@ -809,13 +949,13 @@ int femtc_tile_db_load(const char* path)
   int loaded = 0;
   while (std::fgets(line, sizeof(line), f))
   {
-    int op, dt, sem, n, q, cb, st, nt;
+    int op, dt, sem, n, q, cb, st, nt, lanes = 0;
     if (line[0] == '#')
       continue;
-    if (std::sscanf(line, "%d %d %d %d %d %d %d %d", &op, &dt, &sem, &n, &q,
-                    &cb, &st, &nt) != 8)
+    if (std::sscanf(line, "%d %d %d %d %d %d %d %d %d", &op, &dt, &sem, &n, &q,
+                    &cb, &st, &nt, &lanes) < 8)
       continue;
-    if (femtc_set_tile_config(op, dt, sem, n - 1, q, cb, st, nt) == FEMTC_OK)
+    if (femtc_set_tile_config(op, dt, sem, n - 1, q, cb, st, nt, lanes) == FEMTC_OK)
       ++loaded;
   }
   std::fclose(f);
@@ -823,12 +963,15 @@ int femtc_tile_db_load(const char* path)
 }
 
 int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int* cb, int* geo_staged, int* threads)
+                          int nquad, int* cb, int* geo_staged, int* threads,
+                          int* lanes)
 {
-  const CellVariant* v = find_cell(op, dtype, semantics, degree + 1, nquad);
-  if (!v)
+  const auto sel = select_variant(op, dtype, semantics, degree + 1, nquad);
+  if (!sel.first)
     return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
-  const TileCfg c = tile_config(*v);
+  const TileCfg c = sel.second;
+  if (lanes)
+    *lanes = sel.first->lanes;
   if (cb)
     *cb = c.cb;
   if (geo_staged)

@@ -23,7 +23,7 @@ void add_mma_variant(std::vector<CellVariant>& v, int dtype)
 {
   v.push_back(CellVariant{dtype, OP, SEM_EXACT, N, Q,
                           reinterpret_cast<const void*>(&mma_kernel<SPLIT, N, Q, OP>),
-                          &mma_smem_bytes<SPLIT, N, Q, OP>, 0, 4});
+                          &mma_smem_bytes<SPLIT, N, Q, OP>, 0, 4, 1});
 }
 
 template <int SPLIT, int OP, int N>

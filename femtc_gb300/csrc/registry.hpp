@@ -20,14 +20,17 @@ struct CellVariant
   unsigned (*smem)(int cb, int staged, int sq, int sbc);
   int slab;    // 1: slab-merged CUDA-core kernel (uses sq, sbc)
   int esize;   // bytes per stored value
+  int lanes;   // slab kernels: lanes sharing one slab
 };
 
 using FaultReader = unsigned (*)(); // returns and clears the unit's fault word
 
 void register_cell_f64_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
-void register_cell_f32_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
-void register_cell_f32_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_mass_l1(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_mass_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_stiffness_l1(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_stiffness_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_f16x2_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_f16x2_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_bf16x3_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);

@@ -108,14 +108,25 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
                                int nquad, const void* tables, const void* u,
                                void* y, const void* G, size_t ncells);
 
+/* How the host-buffer entry points move data.  0 (default): when u, y and
+ * the geometry are all pinned host memory (cudaHostAlloc /
+ * cudaHostRegister), the kernel reads u and the geometry and writes y
+ * directly over the coherent Grace-Blackwell host link, with no staging
+ * copies; otherwise they are copied through device staging buffers.
+ * 1: always copy.  2: zero-copy only (pageable buffers are an error). */
+int femtc_set_host_path(int mode);
+
 /* Tile shape of a variant: cells per tile cb (multiple of 4), whether the
- * geometry slab is staged through shared memory by TMA, and threads per CTA
- * (multiple of 32, at most 256; <= 0 means 256).  cb <= 0 restores the
- * built-in heuristic.  The autotuner below writes these. */
+ * geometry slab is staged through shared memory by TMA, threads per CTA
+ * (multiple of 32, at most 256; <= 0 means 256) and, for the FP32 CUDA-core
+ * kernels, lanes per slab (1 or 2; <= 0 means the built-in choice).
+ * cb <= 0 restores the built-in heuristic.  The autotuner writes these. */
 int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int cb, int geo_staged, int threads);
+                          int nquad, int cb, int geo_staged, int threads,
+                          int lanes);
 int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
-                          int nquad, int* cb, int* geo_staged, int* threads);
+                          int nquad, int* cb, int* geo_staged, int* threads,
+                          int* lanes);
 
 /* Autotuner: times candidate tile shapes of one variant on the caller's
  * device buffers (as for femtc_*_apply; y is overwritten), keeps the fastest
@@ -126,6 +137,15 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
                    const void* tables, const void* u, void* y,
                    const void* geo, size_t ncells, void* stream, int* cb,
                    int* geo_staged, int* threads, float* best_ms);
+
+/* The same for the zero-copy host path: u, y and geo are pinned host
+ * buffers; the kernels read and write them over the host link while tiles
+ * are timed, and the winner becomes the tile shape the host-buffer entry
+ * points use for pinned buffers. */
+int femtc_autotune_host(int op, int dtype, int semantics, int degree,
+                        int nquad, const void* tables, const void* u, void* y,
+                        const void* geo, size_t ncells, int* cb,
+                        int* geo_staged, int* threads, float* best_ms);
 
 /* Save / load every explicitly set or tuned tile configuration as text
  * ("op dtype semantics n q cb geo_staged threads" per line).  Load returns

@@ -72,7 +72,7 @@ def test_null_pointer_rejected(femtc):
 def test_tile_config_roundtrip(femtc, tmp_path):
     old = femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5)
     femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 8, 0, 128)
-    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0, 128)
+    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0, 128, 1)
     with pytest.raises(femtc.FemtcError):
         femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 6, 0)  # not a multiple of 4
     with pytest.raises(femtc.FemtcError):
@@ -82,5 +82,14 @@ def test_tile_config_roundtrip(femtc, tmp_path):
     femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)  # back to default
     assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == old
     assert femtc.tile_db_load(db) >= 1
-    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0, 128)
+    assert femtc.get_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5) == (8, 0, 128, 1)
     femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)
+
+
+def test_fp32_lanes_choice_roundtrip(femtc):
+    key = (femtc.STIFFNESS, femtc.F32, femtc.EXACT, 4, 6)
+    for lanes in (1, 2):
+        femtc.set_tile_config(*key, 12, 0, 128, lanes)
+        assert femtc.get_tile_config(*key) == (12, 0, 128, lanes)
+    femtc.set_tile_config(*key, 0, 0)
+    assert femtc.get_tile_config(*key)[3] in (1, 2)

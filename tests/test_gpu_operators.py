@@ -119,16 +119,16 @@ def test_misaligned_pointer_rejected(femtc, dev):
         femtc.apply(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, t, u.data_ptr() + 8, u, u, 2)
 
 
-@pytest.mark.parametrize("dtype", [0, 1, 2])
+@pytest.mark.parametrize("dtype,lanes", [(0, 1), (1, 1), (1, 2), (2, 1)])
 @pytest.mark.parametrize("P", [3, 4])
 @pytest.mark.parametrize("staged", [0, 1])
 @pytest.mark.parametrize("cb,nt", [(4, 64), (8, 256), (12, 128), (28, 96)])
-def test_tile_configs_agree(femtc, orc, dev, dtype, P, staged, cb, nt):
+def test_tile_configs_agree(femtc, orc, dev, dtype, lanes, P, staged, cb, nt):
     from femtc_gb300 import workloads as W
     Q = P + 1
     w = W.make_custom("t", 1, P, Q, 203, seed=2)
     try:
-        femtc.set_tile_config(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q, cb, staged, nt)
+        femtc.set_tile_config(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q, cb, staged, nt, lanes)
     except femtc.FemtcError:
         pytest.skip("tile does not fit in shared memory")
     try:
@@ -151,7 +151,7 @@ def test_autotune_then_parity(femtc, orc, dev, dtype):
     y = torch.empty_like(u)
     cb, st, nt, ms = femtc.autotune(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q, w.tables, u, y, g, 3000)
     assert ms > 0 and cb % 4 == 0 and nt % 32 == 0
-    assert femtc.get_tile_config(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q) == (cb, st, nt)
+    assert femtc.get_tile_config(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q)[:3] == (cb, st, nt)
     femtc.apply(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q, w.tables, u, y, g, 3000)
     torch.cuda.synchronize()
     femtc.set_tile_config(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q, 0, 0)
@@ -163,3 +163,53 @@ def test_oversized_tile_rejected(femtc):
     # 20 cells of P=3/Q=5 FP64 stiffness with staged geometry need 260 KB
     with pytest.raises(femtc.FemtcError):
         femtc.set_tile_config(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 3, 5, 20, 1)
+
+
+@pytest.mark.parametrize("dtype", [0, 1, 3])
+@pytest.mark.parametrize("op,P,Q", [(0, 3, 5), (1, 4, 6), (1, 1, 3), (0, 7, 9)])
+def test_zero_copy_host_path(femtc, orc, dev, dtype, op, P, Q):
+    """Pinned host buffers: the kernel reads and writes host memory directly
+    (no staging copies) and must give the device path's bits."""
+    import torch
+    from femtc_gb300 import workloads as W
+    w = W.make_custom("t", op, P, Q, 333, seed=21)
+    tdt = torch.float64 if dtype == 0 else torch.float32
+    uh = torch.from_numpy(w.u).to(tdt).pin_memory()
+    gh = torch.from_numpy(w.geo).to(tdt).pin_memory()
+    yh = torch.full_like(uh, float("nan")).pin_memory()
+    femtc.apply_host(op, dtype, femtc.EXACT, P, Q, w.tables, uh, yh, gh, 333)
+    ud, gd = uh.to(dev), gh.to(dev)
+    yd = torch.empty_like(ud)
+    femtc.apply(op, dtype, femtc.EXACT, P, Q, w.tables, ud, yd, gd, 333)
+    torch.cuda.synchronize()
+    assert torch.equal(yh, yd.cpu())
+    # staging-copy mode gives the same result; zero-copy-only mode rejects pageable buffers
+    femtc.set_host_path(1)
+    try:
+        yh2 = torch.full_like(uh, float("nan")).pin_memory()
+        femtc.apply_host(op, dtype, femtc.EXACT, P, Q, w.tables, uh, yh2, gh, 333)
+        assert torch.equal(yh2, yh)
+        femtc.set_host_path(2)
+        with pytest.raises(femtc.FemtcError):
+            up = w.u.astype(np.float64 if dtype == 0 else np.float32)
+            femtc.apply_host(op, dtype, femtc.EXACT, P, Q, w.tables, up, np.empty_like(up),
+                             w.geo.astype(up.dtype), 333)
+    finally:
+        femtc.set_host_path(0)
+
+
+def test_autotune_host_then_parity(femtc, orc, dev):
+    import torch
+    from femtc_gb300 import workloads as W
+    P, Q = 4, 6
+    w = W.make_custom("t", 1, P, Q, 2000, seed=31)
+    uh = torch.from_numpy(w.u).pin_memory()
+    gh = torch.from_numpy(w.geo).pin_memory()
+    yh = torch.empty_like(uh).pin_memory()
+    cb, st, nt, ms = femtc.autotune_host(femtc.STIFFNESS, femtc.F64, femtc.EXACT, P, Q, w.tables,
+                                         uh, yh, gh, 2000)
+    assert ms > 0 and cb % 4 == 0 and nt % 32 == 0
+    yh.fill_(float("nan"))
+    femtc.apply_host(femtc.STIFFNESS, femtc.F64, femtc.EXACT, P, Q, w.tables, uh, yh, gh, 2000)
+    ref = orc.stiffness(orc.EXACT, P, Q, w.tables, w.u, w.geo)
+    assert np.abs(yh.numpy() - ref).max() / np.abs(ref).max() <= 1e-12

@@ -387,6 +387,8 @@ struct SlabTile
   static constexpr int QS = (Q + S - 1) / S; // q2 columns per lane (max)
   // unroll the q2 loop only while the unrolled body stays small
   static constexpr int UNR = (N * N * QS * NBUF <= 1200) ? QS : 1;
+  // lane-dependent axis-2 table columns preloaded into registers
+  static constexpr bool PRE = (S > 1) && (UNR == QS);
 
   static __host__ __device__ unsigned work_bytes(const CellParams<T>& p)
   {
@@ -451,6 +453,24 @@ struct SlabTile
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
     const int ns = ncb * N * S, bstride = ncb * p.sbc;
+    // With S lanes per slab the q2 columns of a lane depend on the lane, so
+    // their table entries are not compile-time constants: load them into
+    // registers once per call (lane_s == threadIdx.x % S for every slab of
+    // this thread, since blockDim.x is a multiple of 32).
+    T pc[PRE ? QS : 1][PRE ? N : 1], dc[PRE ? QS : 1][PRE ? N : 1];
+    if constexpr (PRE)
+    {
+      const int ls = threadIdx.x % S;
+#pragma unroll
+      for (int jq = 0; jq < QS; ++jq)
+#pragma unroll
+        for (int i2 = 0; i2 < N; ++i2)
+        {
+          const int q2 = ls + jq * S;
+          pc[jq][i2] = q2 < Q ? P[q2 + i2 * Q] : T(0);
+          dc[jq][i2] = q2 < Q ? D[q2 + i2 * Q] : T(0);
+        }
+    }
     for (int ts = threadIdx.x; ts < ns; ts += blockDim.x)
     {
       const int sl = ts / S, lane_s = ts - sl * S;
@@ -467,20 +487,23 @@ struct SlabTile
         if (S > 1 && q2 >= Q)
           break;
         T a[N], g[N];
+        // axis-2 table entries Phi(q2, i2), Gamma(q2, i2) of this column
+        auto pq = [&](int i2) { if constexpr (PRE) return pc[jq][i2]; else return P[q2 + i2 * Q]; };
+        auto dq = [&](int i2) { if constexpr (PRE) return dc[jq][i2]; else return D[q2 + i2 * Q]; };
 #pragma unroll
         for (int i1 = 0; i1 < N; ++i1)
         {
-          T acc = P[q2] * x[i1 * N];
+          T acc = pq(0) * x[i1 * N];
 #pragma unroll
           for (int i2 = 1; i2 < N; ++i2)
-            acc = fma(P[q2 + i2 * Q], x[i1 * N + i2], acc);
+            acc = fma(pq(i2), x[i1 * N + i2], acc);
           a[i1] = acc;
           if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
           {
-            T gcc = D[q2] * x[i1 * N];
+            T gcc = dq(0) * x[i1 * N];
 #pragma unroll
             for (int i2 = 1; i2 < N; ++i2)
-              gcc = fma(D[q2 + i2 * Q], x[i1 * N + i2], gcc);
+              gcc = fma(dq(i2), x[i1 * N + i2], gcc);
             g[i1] = gcc;
           }
         }
@@ -623,6 +646,22 @@ struct SlabTile
     // runs to a bound that is a multiple of the CTA size
     const int ns = ncb * N * S, bstride = ncb * p.sbc;
     const int nsr = (ns + blockDim.x - 1) / blockDim.x * blockDim.x;
+    // axis-2 backward table entries of this lane's q2 columns (see forward)
+    const T* T2 = (OP == OP_STIFFNESS && SEM == SEM_REFERENCE) ? D : P;
+    T tc[PRE ? QS : 1][PRE ? N : 1], ec[PRE ? QS : 1][PRE ? N : 1];
+    if constexpr (PRE)
+    {
+      const int ls = threadIdx.x % S;
+#pragma unroll
+      for (int jq = 0; jq < QS; ++jq)
+#pragma unroll
+        for (int i2 = 0; i2 < N; ++i2)
+        {
+          const int q2 = ls + jq * S;
+          tc[jq][i2] = q2 < Q ? T2[i2 * BSM + q2 * BSK] : T(0);
+          ec[jq][i2] = q2 < Q ? D[i2 * BSM + q2 * BSK] : T(0);
+        }
+    }
     for (int ts = threadIdx.x; ts < nsr; ts += blockDim.x)
     {
       const bool live = ts < ns;
@@ -674,17 +713,24 @@ struct SlabTile
           U1[i1] = acc;
         }
         // axis 2 back (q2 -> i2), accumulated over q2
-        const T* T2 = (OP == OP_STIFFNESS && SEM == SEM_REFERENCE) ? D : P;
 #pragma unroll
         for (int i2 = 0; i2 < N; ++i2)
         {
-          const T t1 = T2[i2 * BSM + q2 * BSK];
+          T t1;
+          if constexpr (PRE)
+            t1 = tc[jq][i2];
+          else
+            t1 = T2[i2 * BSM + q2 * BSK];
 #pragma unroll
           for (int i1 = 0; i1 < N; ++i1)
             y[i1 * N + i2] = fma(t1, U1[i1], y[i1 * N + i2]);
           if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
           {
-            const T t2 = D[i2 * BSM + q2 * BSK];
+            T t2;
+            if constexpr (PRE)
+              t2 = ec[jq][i2];
+            else
+              t2 = D[i2 * BSM + q2 * BSK];
 #pragma unroll
             for (int i1 = 0; i1 < N; ++i1)
               y[i1 * N + i2] = fma(t2, U2[i1], y[i1 * N + i2]);

@@ -487,11 +487,16 @@ int apply(int op, int dtype, int sem, int degree, int nquad,
 size_t elem_size(int dtype) { return dtype == FEMTC_F64 ? 8 : 4; }
 
 // ------------------------------------------------------- host-buffer path --
+// Host-buffer path state: the device it was set up on, a compute stream,
+// copy-in / copy-out streams and chunk events of the staging pipeline, and
+// grow-only device staging buffers.
+constexpr int kHostChunks = 16; // events per pipeline (chunks per call, at most)
 struct HostPath
 {
   std::mutex m;
   int device = -1;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr, in = nullptr, out = nullptr;
+  cudaEvent_t ev_in[kHostChunks] = {}, ev_k[kHostChunks] = {};
   void* buf[3] = {nullptr, nullptr, nullptr};
   size_t cap[3] = {0, 0, 0};
 };
@@ -570,6 +575,8 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
     // a different device: drop buffers of the old one (they stay valid on
     // it until freed; free them with that device current)
     g_host.stream = nullptr;
+    g_host.in = nullptr;
+    g_host.out = nullptr;
     for (int i = 0; i < 3; ++i)
     {
       g_host.buf[i] = nullptr;
@@ -592,24 +599,75 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
       (rc = host_buffer(1, bu)) != FEMTC_OK ||
       (rc = host_buffer(2, bg)) != FEMTC_OK)
     return rc;
-  cudaStream_t st = g_host.stream;
-  cudaError_t e = cudaMemcpyAsync(g_host.buf[0], u, bu,
-                                  cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(g_host.buf[2], geo, bg, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess)
-    return cuda_fail(e, "cudaMemcpyAsync (host to device)");
-  rc = apply(op, dtype, sem, degree, nquad, tables, g_host.buf[0],
-             g_host.buf[1], g_host.buf[2], ncells, st);
-  if (rc != FEMTC_OK)
+  // Staging pipeline: chunk i's host->device copy (stream `in`), operator
+  // (compute stream, after the copy's event) and device->host copy (stream
+  // `out`, after the kernel's event) overlap with the neighbouring chunks.
+  // Chunks start on multiples of 4 cells, so every chunk pointer keeps the
+  // 16-byte alignment the kernels' bulk copies need.
+  if (!g_host.in)
   {
-    cudaStreamSynchronize(st);
-    return rc;
+    if (cudaStreamCreateWithFlags(&g_host.in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&g_host.out, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(FEMTC_ERR_CUDA, "cudaStreamCreate failed");
+    for (int i = 0; i < kHostChunks; ++i)
+      if (cudaEventCreateWithFlags(&g_host.ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&g_host.ev_k[i], cudaEventDisableTiming) != cudaSuccess)
+        return fail(FEMTC_ERR_CUDA, "cudaEventCreate failed");
   }
-  e = cudaMemcpyAsync(y, g_host.buf[1], bu, cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess)
-    return cuda_fail(e, "cudaMemcpyAsync (device to host)");
-  e = cudaStreamSynchronize(st);
+  // Chunks of whole waves of tiles (CTAs per SM x SMs x cells per tile), so
+  // no chunk's kernel ends on a mostly idle wave; about 8 chunks per call,
+  // each a multiple of 4 cells.
+  size_t per;
+  {
+    const auto sel = select_variant(op, dtype, sem, degree + 1, nquad);
+    int blocks = 1;
+    if (!sel.first || prepare(sel.first->fn, smem_of(*sel.first, sel.second), sel.second.nt,
+                              &blocks) != FEMTC_OK)
+      blocks = 1;
+    const size_t wave = std::max<size_t>(4, (size_t)blocks * sm_count() * sel.second.cb);
+    size_t waves = std::max<size_t>(1, (ncells + 8 * wave - 1) / (8 * wave));
+    per = waves * wave;
+    while ((ncells + per - 1) / per > (size_t)kHostChunks)
+      per += wave;
+    per = (per + 3) / 4 * 4;
+  }
+  const char* hu = static_cast<const char*>(u);
+  const char* hg = static_cast<const char*>(geo);
+  char* hy = static_cast<char*>(y);
+  char* du2 = static_cast<char*>(g_host.buf[0]);
+  char* dy2 = static_cast<char*>(g_host.buf[1]);
+  char* dg2 = static_cast<char*>(g_host.buf[2]);
+  int nch = 0;
+  for (size_t c0 = 0; c0 < ncells; c0 += per, ++nch)
+  {
+    const size_t nc = std::min(per, ncells - c0);
+    const size_t ou = c0 * n3 * es, og = c0 * q3 * es;
+    cudaError_t e = cudaMemcpyAsync(du2 + ou, hu + ou, nc * n3 * es, cudaMemcpyHostToDevice,
+                                    g_host.in);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dg2 + og, hg + og, nc * q3 * es, cudaMemcpyHostToDevice, g_host.in);
+    if (e == cudaSuccess)
+      e = cudaEventRecord(g_host.ev_in[nch], g_host.in);
+    if (e == cudaSuccess)
+      e = cudaStreamWaitEvent(g_host.stream, g_host.ev_in[nch], 0);
+    if (e != cudaSuccess)
+      return cuda_fail(e, "staging copy (host to device)");
+    rc = apply(op, dtype, sem, degree, nquad, tables, du2 + ou, dy2 + ou, dg2 + og, nc,
+               g_host.stream);
+    if (rc != FEMTC_OK)
+    {
+      cudaDeviceSynchronize();
+      return rc;
+    }
+    e = cudaEventRecord(g_host.ev_k[nch], g_host.stream);
+    if (e == cudaSuccess)
+      e = cudaStreamWaitEvent(g_host.out, g_host.ev_k[nch], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hy + ou, dy2 + ou, nc * n3 * es, cudaMemcpyDeviceToHost, g_host.out);
+    if (e != cudaSuccess)
+      return cuda_fail(e, "staging copy (device to host)");
+  }
+  cudaError_t e = cudaStreamSynchronize(g_host.out);
   if (e != cudaSuccess)
     return cuda_fail(e, "cudaStreamSynchronize");
   return FEMTC_OK;

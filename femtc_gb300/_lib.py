@@ -15,11 +15,12 @@ import numpy as np
 
 from . import buildlib as _build
 
-F64, F32, F16X2, BF16X3 = 0, 1, 2, 3
+F64, F32, F16X2, BF16X3, F64E = 0, 1, 2, 3, 4
 EXACT, REFERENCE = 0, 1
 MASS, STIFFNESS = 0, 1
 
-DTYPE_NAMES = {F64: "f64", F32: "f32", F16X2: "f16x2", BF16X3: "bf16x3"}
+DTYPE_NAMES = {F64: "f64", F32: "f32", F16X2: "f16x2", BF16X3: "bf16x3", F64E: "f64e"}
+FP64_STORAGE = (F64, F64E)
 
 _lock = threading.Lock()
 _lib = None
@@ -38,6 +39,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     dp = ctypes.POINTER(ctypes.c_double)
     sigs = {
         "femtc_version": ([], c_int),
+        "femtc_operator_launches": ([], ctypes.c_longlong),
         "femtc_last_error": ([], ctypes.c_char_p),
         "femtc_device_status": ([], c_int),
         "femtc_supported": ([c_int] * 5, c_int),
@@ -117,7 +119,7 @@ def ptr(x) -> int | None:
 
 
 def host_tables(tables, dtype: int) -> np.ndarray:
-    want = np.float64 if dtype == F64 else np.float32
+    want = np.float64 if dtype in FP64_STORAGE else np.float32
     return np.ascontiguousarray(np.asarray(tables), dtype=want)
 
 
@@ -161,6 +163,11 @@ def apply_host(op: int, dtype: int, semantics: int, degree: int, nquad: int,
     fn = lib.femtc_mass_apply_host if op == MASS else lib.femtc_stiffness_apply_host
     check(fn(dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
              ptr(geo), ncells))
+
+
+def operator_launches() -> int:
+    """Operator kernels launched by the library so far in this process."""
+    return int(load().femtc_operator_launches())
 
 
 def set_host_path(mode: int) -> None:

@@ -55,6 +55,20 @@ void add_all(std::vector<CellVariant>& v, int dtype)
   add_degree<T, OP, 8, L>(v, dtype);
 }
 
+// Exact semantics, N = 2..MAXN only (the double-float form: its register
+// footprint is twice FP32's, and degrees above 4 spill).
+template <typename T, int OP, int L, int N, int MAXN>
+void add_exact_upto(std::vector<CellVariant>& v, int dtype)
+{
+  if constexpr (N <= MAXN)
+  {
+    add_variant<T, N, N, OP, SEM_EXACT, L>(v, dtype);
+    add_variant<T, N, N + 1, OP, SEM_EXACT, L>(v, dtype);
+    add_variant<T, N, N + 2, OP, SEM_EXACT, L>(v, dtype);
+    add_exact_upto<T, OP, L, N + 1, MAXN>(v, dtype);
+  }
+}
+
 inline unsigned read_clear_fault_word()
 {
   unsigned w = 0, z = 0;
@@ -72,6 +86,16 @@ inline unsigned read_clear_fault_word()
   void NAME(std::vector<CellVariant>& v, std::vector<FaultReader>& f)          \
   {                                                                            \
     add_all<T, OP, L>(v, DTYPE);                                               \
+    f.push_back(&read_clear_fault_word);                                       \
+  }                                                                            \
+  }
+
+#define FEMTC_CELL_UNIT_EXACT_UPTO(NAME, T, DTYPE, OP, L, MAXN)                 \
+  namespace femtc                                                              \
+  {                                                                            \
+  void NAME(std::vector<CellVariant>& v, std::vector<FaultReader>& f)          \
+  {                                                                            \
+    add_exact_upto<T, OP, L, 2, MAXN>(v, DTYPE);                               \
     f.push_back(&read_clear_fault_word);                                       \
   }                                                                            \
   }

@@ -30,6 +30,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "df64.cuh"
 
 #include <type_traits>
 
@@ -51,12 +52,52 @@ constexpr int kMaxN = 9;
 constexpr int kMaxQ = 10;
 constexpr int kCellThreads = 256;
 
+// Storage type of a compute type: values live in HBM and in the staging
+// buffers as `type`; double-float arithmetic keeps FP64 storage.
+template <typename T>
+struct storage_of
+{
+  using type = T;
+};
+template <>
+struct storage_of<df64>
+{
+  using type = double;
+};
+template <typename T>
+using storage_t = typename storage_of<T>::type;
+
+template <typename T>
+__device__ __forceinline__ T from_storage(storage_t<T> v)
+{
+  if constexpr (std::is_same<T, df64>::value)
+    return to_df64(v);
+  else
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ storage_t<T> to_storage(T v)
+{
+  if constexpr (std::is_same<T, df64>::value)
+    return to_double(v);
+  else
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_xor(T v, int lane_mask)
+{
+  return __shfl_xor_sync(0xffffffffu, v, lane_mask);
+}
+
 template <typename T>
 struct CellParams
 {
-  const T* u;        // [ncells][N^3]
-  T* y;              // [ncells][N^3]
-  const T* geo;      // mass: [ncells][Q^3]; stiffness: [ncells][Q^3][6]
+  using ST = storage_t<T>;
+  const ST* u;       // [ncells][N^3]
+  ST* y;             // [ncells][N^3]
+  const ST* geo;     // mass: [ncells][Q^3]; stiffness: [ncells][Q^3][6]
   long long ncells;
   int cb;            // cells per tile, a multiple of 4
   int geo_staged;    // 1: geometry slab staged by TMA, 0: read in the fused pass
@@ -171,15 +212,17 @@ __device__ __forceinline__ void mv_acc(const T* __restrict__ A,
 template <typename T, typename Tile, int N, int Q, int NC>
 __host__ __device__ inline CellLayout tile_layout(const CellParams<T>& p)
 {
-  const unsigned bu = (unsigned)p.cb * N * Tile::US * sizeof(T);
+  using ST = storage_t<T>;
+  const unsigned bu = (unsigned)p.cb * N * Tile::US * sizeof(ST);
   const unsigned bg =
-      p.geo_staged ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(T) : 0u;
+      p.geo_staged ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(ST) : 0u;
   return CellLayout(bu, bg, Tile::work_bytes(p));
 }
 
 template <typename T, typename Tile, int N, int Q, int NC>
 __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
 {
+  using ST = storage_t<T>; // staged values; T is the arithmetic type
   constexpr int N2 = N * N, N3 = N * N * N, Q3NC = Q * Q * Q * NC;
   constexpr int US = Tile::US;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -189,13 +232,13 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   // stage s buffers (selected arithmetically: no local-memory arrays)
-  auto su = [&](int s) { return reinterpret_cast<T*>(smem + (s ? L.u1 : L.u0)); };
-  auto sg = [&](int s) { return reinterpret_cast<T*>(smem + (s ? L.g1 : L.g0)); };
-  T* sy = reinterpret_cast<T*>(smem + L.y);
+  auto su = [&](int s) { return reinterpret_cast<ST*>(smem + (s ? L.u1 : L.u0)); };
+  auto sg = [&](int s) { return reinterpret_cast<ST*>(smem + (s ? L.g1 : L.g0)); };
+  ST* sy = reinterpret_cast<ST*>(smem + L.y);
   T* sw = reinterpret_cast<T*>(smem + L.w);
-  const unsigned bslab = N2 * sizeof(T);
-  const unsigned bu = (unsigned)cb * N3 * sizeof(T);
-  const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(T) : 0u;
+  const unsigned bslab = N2 * sizeof(ST);
+  const unsigned bu = (unsigned)cb * N3 * sizeof(ST);
+  const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(ST) : 0u;
   const int lane = threadIdx.x & 31;
   const bool warp0 = threadIdx.x < 32;
   const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc};
@@ -255,7 +298,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
       // lengths are multiples of 16 bytes: cb % 4 == 0 and N*N % 4 == 0
       // whenever slabs are padded)
       using V = uint4;
-      constexpr int W = 16 / sizeof(T);
+      constexpr int W = 16 / sizeof(ST);
       const V* gu = reinterpret_cast<const V*>(p.u + tile * cb * N3);
       const int nv = cb * N3 / W;
 #pragma unroll 4
@@ -326,7 +369,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     {
       __syncthreads();
       using V = uint4;
-      constexpr int W = 16 / sizeof(T);
+      constexpr int W = 16 / sizeof(ST);
       V* gy = reinterpret_cast<V*>(p.y + tile * cb * N3);
       const int nv = cb * N3 / W;
 #pragma unroll 4
@@ -374,9 +417,10 @@ __host__ __device__ constexpr int slab_lanes()
 template <typename T, int N, int Q, int OP, int SEM, int LANES = slab_lanes<T>()>
 struct SlabTile
 {
+  using ST = storage_t<T>; // staged u, y and geometry; T is the arithmetic
   static constexpr int S = LANES;
   static constexpr bool kSlabCopies = (N % 2 == 0);
-  static constexpr int US = slab_stride<T>(N);
+  static constexpr int US = slab_stride<ST>(N);
   static constexpr int N2 = N * N, Q2 = Q * Q, Q3 = Q * Q * Q;
   static constexpr int NBUF =
       (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
@@ -395,46 +439,46 @@ struct SlabTile
     return (unsigned)NBUF * p.cb * p.sbc * sizeof(T);
   }
 
-  static __device__ __forceinline__ void load_slab(const T* __restrict__ src,
+  static __device__ __forceinline__ void load_slab(const ST* __restrict__ src,
                                                    T (&x)[N2])
   {
     if constexpr (kSlabCopies)
     {
-      using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-      constexpr int W = 16 / sizeof(T);
+      using V = typename std::conditional<sizeof(ST) == 4, float4, double2>::type;
+      constexpr int W = 16 / sizeof(ST);
 #pragma unroll
       for (int k = 0; k < N2 / W; ++k)
       {
         const V v = reinterpret_cast<const V*>(src)[k];
-        const T* e = reinterpret_cast<const T*>(&v);
+        const ST* e = reinterpret_cast<const ST*>(&v);
 #pragma unroll
         for (int j = 0; j < W; ++j)
-          x[k * W + j] = e[j];
+          x[k * W + j] = from_storage<T>(e[j]);
       }
     }
     else
     {
 #pragma unroll
       for (int k = 0; k < N2; ++k)
-        x[k] = src[k];
+        x[k] = from_storage<T>(src[k]);
     }
   }
 
-  static __device__ __forceinline__ void store_slab(T* __restrict__ dst,
+  static __device__ __forceinline__ void store_slab(ST* __restrict__ dst,
                                                     const T (&x)[N2])
   {
     if constexpr (kSlabCopies)
     {
-      using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-      constexpr int W = 16 / sizeof(T);
+      using V = typename std::conditional<sizeof(ST) == 4, float4, double2>::type;
+      constexpr int W = 16 / sizeof(ST);
 #pragma unroll
       for (int k = 0; k < N2 / W; ++k)
       {
         V v;
-        T* e = reinterpret_cast<T*>(&v);
+        ST* e = reinterpret_cast<ST*>(&v);
 #pragma unroll
         for (int j = 0; j < W; ++j)
-          e[j] = x[k * W + j];
+          e[j] = to_storage<T>(x[k * W + j]);
         reinterpret_cast<V*>(dst)[k] = v;
       }
     }
@@ -442,12 +486,12 @@ struct SlabTile
     {
 #pragma unroll
       for (int k = 0; k < N2; ++k)
-        dst[k] = x[k];
+        dst[k] = to_storage<T>(x[k]);
     }
   }
 
   static __device__ __forceinline__ void forward(const TabView<T>& p,
-                                                 const T* __restrict__ su,
+                                                 const ST* __restrict__ su,
                                                  T* __restrict__ sw, int ncb)
   {
     const T* __restrict__ P = p.P;
@@ -538,7 +582,7 @@ struct SlabTile
 
   static __device__ __forceinline__ void fused(const TabView<T>& p,
                                                T* __restrict__ sw, int ncb,
-                                               const T* __restrict__ geo,
+                                               const ST* __restrict__ geo,
                                                long long geo_cell0)
   {
     const T* __restrict__ P = p.P;
@@ -553,7 +597,7 @@ struct SlabTile
       const int sq = p.sq;
       if constexpr (OP == OP_MASS)
       {
-        const T* dw = geo + (geo_cell0 + c) * Q3 + r;
+        const ST* dw = geo + (geo_cell0 + c) * Q3 + r;
         T x[N], v[Q];
 #pragma unroll
         for (int k = 0; k < N; ++k)
@@ -561,7 +605,7 @@ struct SlabTile
         mv<Q, N, 1, Q>(P, x, v);
 #pragma unroll
         for (int q = 0; q < Q; ++q)
-          v[q] *= dw[q * Q2];
+          v[q] *= from_storage<T>(dw[q * Q2]);
         mv<N, Q, BSM, BSK>(P, v, x);
 #pragma unroll
         for (int k = 0; k < N; ++k)
@@ -569,7 +613,7 @@ struct SlabTile
       }
       else
       {
-        const T* G = geo + ((geo_cell0 + c) * Q3 + r) * 6;
+        const ST* G = geo + ((geo_cell0 + c) * Q3 + r) * 6;
         T xa[N], xg[N], fx[Q], fy[Q], fz[Q];
 #pragma unroll
         for (int k = 0; k < N; ++k)
@@ -593,14 +637,15 @@ struct SlabTile
         }
         // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx], read
         // as three 8/16-byte pairs
-        using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+        using V2 = typename std::conditional<sizeof(ST) == 4, float2, double2>::type;
 #pragma unroll
         for (int q = 0; q < Q; ++q)
         {
           const V2* g2 = reinterpret_cast<const V2*>(G + (long long)q * Q2 * 6);
           const V2 g01 = g2[0], g23 = g2[1], g45 = g2[2];
-          const T zz = g01.x, yz = g01.y, xz = g23.x, yy = g23.y, xy = g45.x,
-                  xx = g45.y;
+          const T zz = from_storage<T>(g01.x), yz = from_storage<T>(g01.y),
+                  xz = from_storage<T>(g23.x), yy = from_storage<T>(g23.y),
+                  xy = from_storage<T>(g45.x), xx = from_storage<T>(g45.y);
           const T w0 = fx[q], w1 = fy[q], w2 = fz[q];
           if constexpr (SEM == SEM_EXACT)
           {
@@ -638,7 +683,7 @@ struct SlabTile
 
   static __device__ __forceinline__ void backward(const TabView<T>& p,
                                                   const T* __restrict__ sw,
-                                                  T* __restrict__ sy, int ncb)
+                                                  ST* __restrict__ sy, int ncb)
   {
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
@@ -744,7 +789,7 @@ struct SlabTile
         {
 #pragma unroll
           for (int o = 1; o < S; o <<= 1)
-            y[k] += __shfl_xor_sync(0xffffffffu, y[k], o);
+            y[k] += shfl_xor(y[k], o);
         }
       }
       // the S lanes of a slab hold the same sums: the store is one write

@@ -7,6 +7,8 @@
 #include "registry.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -24,6 +26,7 @@ namespace
 {
 
 thread_local std::string t_last_error;
+std::atomic<long long> g_launches{0}; // kernels launched by this library
 
 int fail(int code, const char* fmt, ...)
 {
@@ -58,6 +61,8 @@ Registry& registry()
     register_cell_f32_mass_l2(r.cells, r.faults);
     register_cell_f32_stiffness_l1(r.cells, r.faults);
     register_cell_f32_stiffness_l2(r.cells, r.faults);
+    register_cell_f64e_mass(r.cells, r.faults);
+    register_cell_f64e_stiffness(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);
     register_mma_f16x2_stiffness(r.cells, r.faults);
     register_mma_bf16x3_mass(r.cells, r.faults);
@@ -391,7 +396,7 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
                  const void* geo, const CellVariant** out)
 {
   if (dtype != FEMTC_F64 && dtype != FEMTC_F32 && dtype != FEMTC_F16X2 &&
-      dtype != FEMTC_BF16X3)
+      dtype != FEMTC_BF16X3 && dtype != FEMTC_F64E)
     return fail(FEMTC_ERR_INVALID, "unknown dtype %d", dtype);
   if (sem != FEMTC_EXACT && sem != FEMTC_REFERENCE)
     return fail(FEMTC_ERR_INVALID, "unknown semantics %d", sem);
@@ -417,20 +422,32 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
   return FEMTC_OK;
 }
 
+// Launch-parameter form of a table entry (double-float splits FP64).
 template <typename T>
-int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
-                const void* u, void* y, const void* geo, size_t ncells,
-                cudaStream_t stream, int host_io = 0)
+T param_value(storage_t<T> x)
 {
+  if constexpr (std::is_same<T, df64>::value)
+    return host_df64(x);
+  else
+    return x;
+}
+
+template <typename T>
+int launch_cell(const CellVariant& v, const TileCfg& cfg,
+                const storage_t<T>* tables, const void* u, void* y,
+                const void* geo, size_t ncells, cudaStream_t stream,
+                int host_io = 0)
+{
+  using ST = storage_t<T>;
   if (!aligned16(u) || !aligned16(y) || !aligned16(geo))
     return fail(FEMTC_ERR_INVALID,
                 "u, y and the geometry must be 16-byte aligned device "
                 "pointers (TMA bulk copies)");
   CellParams<T> p;
   std::memset(&p, 0, sizeof(p));
-  p.u = static_cast<const T*>(u);
-  p.y = static_cast<T*>(y);
-  p.geo = static_cast<const T*>(geo);
+  p.u = static_cast<const ST*>(u);
+  p.y = static_cast<ST*>(y);
+  p.geo = static_cast<const ST*>(geo);
   p.ncells = (long long)ncells;
   p.cb = cfg.cb;
   p.geo_staged = cfg.staged;
@@ -440,7 +457,7 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
   const int ntab = (v.op == FEMTC_OP_STIFFNESS) ? 2 : 1;
   for (int t = 0; t < ntab; ++t)
     for (int i = 0; i < v.n * v.q; ++i)
-      p.tab[t][i] = tables[t * v.n * v.q + i];
+      p.tab[t][i] = param_value<T>(tables[t * v.n * v.q + i]);
   const unsigned smem = smem_of(v, cfg);
   int blocks = 0;
   int rc = prepare(v.fn, smem, cfg.nt, &blocks);
@@ -454,6 +471,7 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg, const T* tables,
                                    dim3((unsigned)cfg.nt), args, smem, stream);
   if (e != cudaSuccess)
     return cuda_fail(e, "cudaLaunchKernel");
+  g_launches.fetch_add(1, std::memory_order_relaxed);
   return FEMTC_OK;
 }
 
@@ -465,6 +483,9 @@ int launch_variant(const CellVariant& v, const TileCfg& cfg,
   if (v.dtype == FEMTC_F64)
     return launch_cell<double>(v, cfg, static_cast<const double*>(tables), u,
                                y, geo, ncells, st, host_io);
+  if (v.dtype == FEMTC_F64E)
+    return launch_cell<df64>(v, cfg, static_cast<const double*>(tables), u, y,
+                             geo, ncells, st, host_io);
   return launch_cell<float>(v, cfg, static_cast<const float*>(tables), u, y,
                             geo, ncells, st, host_io);
 }
@@ -484,7 +505,10 @@ int apply(int op, int dtype, int sem, int degree, int nquad,
                         static_cast<cudaStream_t>(stream));
 }
 
-size_t elem_size(int dtype) { return dtype == FEMTC_F64 ? 8 : 4; }
+size_t elem_size(int dtype)
+{
+  return (dtype == FEMTC_F64 || dtype == FEMTC_F64E) ? 8 : 4;
+}
 
 // ------------------------------------------------------- host-buffer path --
 // Host-buffer path state: the device it was set up on, a compute stream,
@@ -535,9 +559,35 @@ int host_buffer(int i, size_t bytes)
   return FEMTC_OK;
 }
 
+// Preferred transfer mode of the host path per variant, measured by
+// femtc_autotune_host: 0 zero-copy, 1 staging pipeline.
+std::map<Key, int> g_host_pref;
+
+int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
+                      const void* tables, const void* u, void* y,
+                      const void* geo, size_t ncells, int mode);
+
 int apply_host(int op, int dtype, int sem, int degree, int nquad,
                const void* tables, const void* u, void* y, const void* geo,
                size_t ncells)
+{
+  std::lock_guard<std::mutex> lk(g_host.m);
+  int mode = g_host_mode;
+  if (mode == 0)
+  {
+    std::lock_guard<std::mutex> lk2(g_cfg_mutex);
+    auto it = g_host_pref.find(Key(op, dtype, sem, degree + 1, nquad));
+    if (it != g_host_pref.end() && it->second == 1)
+      mode = 1;
+  }
+  return apply_host_locked(op, dtype, sem, degree, nquad, tables, u, y, geo, ncells, mode);
+}
+
+// The host path with g_host.m held; mode 0 zero-copy when the buffers are
+// pinned (else staging), 1 staging, 2 zero-copy or error.
+int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
+                      const void* tables, const void* u, void* y,
+                      const void* geo, size_t ncells, int mode)
 {
   const CellVariant* v = nullptr;
   int rc = check_common(op, dtype, sem, degree, nquad, tables, u, y, geo, &v);
@@ -545,7 +595,6 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return FEMTC_OK;
-  std::lock_guard<std::mutex> lk(g_host.m);
   int dev = 0;
   cudaGetDevice(&dev);
   // Pinned host buffers: the kernel reads u and the geometry and writes y
@@ -553,7 +602,7 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
   const void* du = nullptr;
   void* dy = nullptr;
   const void* dg = nullptr;
-  if (g_host_mode != 1 && device_view(u, &du) && device_view(y, (const void**)&dy) &&
+  if (mode != 1 && device_view(u, &du) && device_view(y, (const void**)&dy) &&
       device_view(geo, &dg))
   {
     if (!g_host.stream &&
@@ -568,7 +617,7 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
     cudaError_t e = cudaStreamSynchronize(g_host.stream);
     return e == cudaSuccess ? FEMTC_OK : cuda_fail(e, "cudaStreamSynchronize");
   }
-  if (g_host_mode == 2)
+  if (mode == 2)
     return fail(FEMTC_ERR_INVALID, "zero-copy host mode needs pinned host buffers");
   if (g_host.device != dev)
   {
@@ -764,6 +813,8 @@ extern "C" {
 
 int femtc_version(void) { return 100; }
 
+long long femtc_operator_launches(void) { return g_launches.load(); }
+
 const char* femtc_last_error(void) { return t_last_error.c_str(); }
 
 int femtc_device_status(void)
@@ -877,8 +928,32 @@ int femtc_autotune_host(int op, int dtype, int semantics, int degree,
   if (!g_host.stream &&
       cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(FEMTC_ERR_CUDA, "cudaStreamCreate failed");
-  return autotune_impl(op, dtype, semantics, degree, nquad, tables, du, dy, dg, ncells,
-                       g_host.stream, 1, cb, geo_staged, threads, best_ms);
+  int rc = autotune_impl(op, dtype, semantics, degree, nquad, tables, du, dy, dg, ncells,
+                         g_host.stream, 1, cb, geo_staged, threads, best_ms);
+  if (rc != FEMTC_OK)
+    return rc;
+  // then the transfer mode: whole calls (copies, kernels, synchronisation)
+  // of the zero-copy path and of the staging pipeline, wall clock
+  double best_call[2] = {0, 0};
+  for (int mode = 0; mode <= 1; ++mode)
+  {
+    rc = apply_host_locked(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells,
+                           mode == 0 ? 2 : 1); // warm
+    if (rc != FEMTC_OK)
+      return rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int r = 0; r < 3; ++r)
+      apply_host_locked(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells,
+                        mode == 0 ? 2 : 1);
+    best_call[mode] =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  {
+    std::lock_guard<std::mutex> lk2(g_cfg_mutex);
+    g_host_pref[Key(op, dtype, semantics, degree + 1, nquad)] =
+        best_call[1] < best_call[0] ? 1 : 0;
+  }
+  return FEMTC_OK;
 }
 
 } // extern "C"

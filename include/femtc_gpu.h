@@ -21,8 +21,8 @@
  *            (src/stiffness.hpp:44-48).  Mass reads only Phi.  Tables are
  *            HOST memory: they are copied into the launch's parameter block.
  *
- * Element types: FEMTC_F64 -> double everywhere; FEMTC_F32 and the mixed
- * forms -> float storage of u, y, dw/G and the tables.
+ * Element types: FEMTC_F64 and FEMTC_F64E -> double storage of u, y, dw/G
+ * and the tables; FEMTC_F32 and the mixed forms -> float storage.
  */
 #ifndef FEMTC_GPU_H
 #define FEMTC_GPU_H
@@ -47,7 +47,9 @@ typedef enum
   FEMTC_F64 = 0,   /* FP64 storage and arithmetic */
   FEMTC_F32 = 1,   /* FP32 storage and arithmetic (CUDA cores) */
   FEMTC_F16X2 = 2, /* FP32 storage; tensor-core FP16 hi/lo split, FP32 acc. */
-  FEMTC_BF16X3 = 3 /* FP32 storage; tensor-core BF16 3-term split, FP32 acc. */
+  FEMTC_BF16X3 = 3, /* FP32 storage; tensor-core BF16 3-term split, FP32 acc. */
+  FEMTC_F64E = 4    /* FP64 storage and tables; double-float (FP32-pair)
+                       arithmetic on the FP32 pipes, FP64-accurate */
 } femtc_dtype;
 
 typedef enum
@@ -64,6 +66,10 @@ typedef enum
 
 /* Library version (major*10000 + minor*100 + patch). */
 int femtc_version(void);
+
+/* Number of operator kernels (mass / stiffness, every form) this library
+ * has launched in this process (a monotonic counter). */
+long long femtc_operator_launches(void);
 
 /* Description of the last failure on the calling thread ("" if none). */
 const char* femtc_last_error(void);
@@ -112,8 +118,12 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
  * the geometry are all pinned host memory (cudaHostAlloc /
  * cudaHostRegister), the kernel reads u and the geometry and writes y
  * directly over the coherent Grace-Blackwell host link, with no staging
- * copies; otherwise they are copied through device staging buffers.
- * 1: always copy.  2: zero-copy only (pageable buffers are an error). */
+ * copies -- unless femtc_autotune_host found the staging pipeline faster
+ * for this variant; other buffers are copied through device staging
+ * buffers in a pipeline of whole-wave chunks (host-to-device copy, kernel
+ * and device-to-host copy of neighbouring chunks overlap).
+ * 1: always the staging pipeline.  2: zero-copy only (pageable buffers are
+ * an error). */
 int femtc_set_host_path(int mode);
 
 /* Tile shape of a variant: cells per tile cb (multiple of 4), whether the
@@ -138,10 +148,11 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
                    const void* geo, size_t ncells, void* stream, int* cb,
                    int* geo_staged, int* threads, float* best_ms);
 
-/* The same for the zero-copy host path: u, y and geo are pinned host
- * buffers; the kernels read and write them over the host link while tiles
- * are timed, and the winner becomes the tile shape the host-buffer entry
- * points use for pinned buffers. */
+/* The same for the host-buffer path: u, y and geo are pinned host buffers.
+ * Tile shapes are timed with the kernels reading and writing them over the
+ * host link (zero-copy); then whole calls of the zero-copy path and of the
+ * staging-copy pipeline are timed, and host-path mode 0 (auto) uses the
+ * faster of the two for this variant from then on. */
 int femtc_autotune_host(int op, int dtype, int semantics, int degree,
                         int nquad, const void* tables, const void* u, void* y,
                         const void* geo, size_t ncells, int* cb,

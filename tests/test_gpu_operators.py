@@ -23,9 +23,9 @@ def relerr(a, b):
 
 def run_gpu(femtc, dev, op, dtype, sem, P, Q, tables, u, geo, host=False):
     import torch
-    tdt = torch.float64 if dtype == femtc.F64 else torch.float32
+    tdt = torch.float64 if dtype in femtc.FP64_STORAGE else torch.float32
     if host:
-        uh = np.ascontiguousarray(u, dtype=np.float64 if dtype == femtc.F64 else np.float32)
+        uh = np.ascontiguousarray(u, dtype=np.float64 if dtype in femtc.FP64_STORAGE else np.float32)
         gh = np.ascontiguousarray(geo, dtype=uh.dtype)
         yh = np.empty_like(uh)
         femtc.apply_host(op, dtype, sem, P, Q, tables, uh, yh, gh, u.shape[0])
@@ -213,3 +213,17 @@ def test_autotune_host_then_parity(femtc, orc, dev):
     femtc.apply_host(femtc.STIFFNESS, femtc.F64, femtc.EXACT, P, Q, w.tables, uh, yh, gh, 2000)
     ref = orc.stiffness(orc.EXACT, P, Q, w.tables, w.u, w.geo)
     assert np.abs(yh.numpy() - ref).max() / np.abs(ref).max() <= 1e-12
+
+
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", [1, 2, 3, 4])
+@pytest.mark.parametrize("dq", [0, 1, 2])
+def test_double_float_form_vs_oracle(femtc, orc, dev, op, P, dq):
+    """FEMTC_F64E: FP64 storage, FP32-pair arithmetic, FP64 accuracy (1e-12)."""
+    from femtc_gb300 import workloads as W
+    Q = P + 1 + dq
+    for ncells in (37, 1001):
+        w = W.make_custom("t", op, P, Q, ncells, seed=3 * P + dq + 50 * op)
+        y = run_gpu(femtc, dev, op, femtc.F64E, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+        ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
+        assert relerr(y, ref) <= 1e-12, relerr(y, ref)

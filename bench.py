@@ -221,25 +221,58 @@ def run_batch(args, rank, world, dev, pg):
         spec = [(op, P, max(1, n * args.cells // 100000)) for op, P, n in spec]
     gen = torch.Generator(device=dev).manual_seed(1004)
     rng = np.random.default_rng(1004)
-    meshes = []
+    meshes, meshes64 = [], []
     for op, P, n in spec:
         Q = P + 2
         tables, _, wts, _ = F.tabulate(P, Q)
         J = torch.from_numpy(W.random_jacobians(rng, n).reshape(n, 9)).to(dev)
         u = torch.rand(n, (P + 1) ** 3, device=dev, generator=gen, dtype=torch.float32) * 2 - 1
         y = torch.empty_like(u)
-        if op == F.MASS:
-            geo = torch.empty(n, Q ** 3, device=dev, dtype=torch.float32)
-            F.geometry(F.F32, Q, wts, J, geo, None, n)
-        else:
-            geo = torch.empty(n, Q ** 3, 6, device=dev, dtype=torch.float32)
-            F.geometry(F.F32, Q, wts, J, None, geo, n)
+        shape = (n, Q ** 3) if op == F.MASS else (n, Q ** 3, 6)
+        geo = torch.empty(shape, device=dev, dtype=torch.float32)
+        geo64 = torch.empty(shape, device=dev, dtype=torch.float64)
+        for dt, g in ((F.F32, geo), (F.F64, geo64)):
+            if op == F.MASS:
+                F.geometry(dt, Q, wts, J, g, None, n)
+            else:
+                F.geometry(dt, Q, wts, J, None, g, n)
         meshes.append((op, P, Q, tables.astype(np.float32), u, y, geo, n))
+        u64 = u.double()
+        meshes64.append((op, P, Q, tables, u64, torch.empty_like(u64), geo64, n))
     torch.cuda.synchronize()
     ndofs = sum(n * (P + 1) ** 3 for _, P, n in spec)
     nbytes = sum(4 * (2 * (P + 1) ** 3 + (1 if op == 0 else 6) * (P + 2) ** 3) * n for op, P, n in spec)
     stream = torch.cuda.current_stream()
     out = {}
+
+    def timed(step):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    # the plain FP64 path on the same meshes, one launch per mesh: the
+    # denominator of the mixed-precision speed-up and the accuracy reference
+    def step64():
+        for op, P, Q, tables, u64, y64, geo64, n in meshes64:
+            F.apply(op, F.F64, F.EXACT, P, Q, tables, u64, y64, geo64, n, stream)
+    ms64 = timed(step64)
+    out["f64"] = {"separate": {"ms": ms64, "gdofs": ndofs / ms64 / 1e6,
+                               "hbm_gbs": 2 * nbytes / ms64 / 1e6}}
+
+    def max_rel_err():
+        worst = 0.0
+        for m32, m64 in zip(meshes, meshes64):
+            y, y64 = m32[5], m64[5]
+            worst = max(worst, ((y.double() - y64).abs().max() / y64.abs().max()).item())
+        return worst
+
     for dtype in (F.F32, F.BF16X3, F.F16X2):
         b = F.Batch(dtype, meshes, tune=True)
         res = {}
@@ -252,17 +285,11 @@ def run_batch(args, rank, world, dev, pg):
                 else:
                     for op, P, Q, tab, u, y, geo, n in meshes:
                         F.apply(op, dtype, F.EXACT, P, Q, tab, u, y, geo, n, stream)
-            for _ in range(args.warmup):
-                step()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(args.steps):
-                step()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / args.steps
+            ms = timed(step)
             res[mode] = {"ms": ms, "gdofs": ndofs / ms / 1e6, "hbm_gbs": nbytes / ms / 1e6}
+            if mode == "graph":
+                res["max_rel_err_vs_f64"] = max_rel_err()
+        res["speedup_vs_f64_plain"] = res["graph"]["gdofs"] / out["f64"]["separate"]["gdofs"]
         res["info"] = b.info()
         b.close()
         out[F.DTYPE_NAMES[dtype]] = res

@@ -66,6 +66,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_batch_info": ([vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(c_int),
                               ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong)], c_int),
         "femtc_batch_layout": ([vp, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
+        "femtc_batch_threads": ([vp], c_int),
         "femtc_batch_destroy": ([vp], None),
         "femtc_batch_apply_static": ([c_int, vp, c_int, vp], c_int),
         "femtc_solve_bytes": ([c_int, c_int, c_size], c_size),
@@ -312,7 +313,10 @@ class Batch:
         nt, ctas, smem, nd = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
         check(load().femtc_batch_info(self.handle, ctypes.byref(nt), ctypes.byref(ctas),
                                       ctypes.byref(smem), ctypes.byref(nd)))
-        return {"tiles": nt.value, "ctas": ctas.value, "smem": smem.value, "dofs": nd.value}
+        threads = load().femtc_batch_threads(self.handle)
+        check(min(threads, 0))
+        return {"tiles": nt.value, "ctas": ctas.value, "threads": threads, "smem": smem.value,
+                "dofs": nd.value}
 
     def layout(self, op: int, degree: int):
         cb, st = ctypes.c_int(), ctypes.c_int()

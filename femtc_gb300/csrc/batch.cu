@@ -16,7 +16,7 @@
 namespace femtc
 {
 int aux_fail(int code, const char* msg); // femtc_abi.cu
-std::pair<int, int> slab_layout_for(int n, int q, int esize); // femtc_abi.cu
+std::pair<int, int> slab_layout_for(int n, int q, int esize, int lanes); // femtc_abi.cu
 
 namespace
 {
@@ -24,12 +24,16 @@ constexpr unsigned kBatchSmemCap = 220u * 1024u;
 // Per-variant caps on a tile's stage sizes: the batch's shared memory is the
 // sum of the maxima over its variants (3 x DOF/output stage, 2 x geometry
 // stage, work), so capping each part keeps every mix of variants within
-// 3*8 + 2*16 + 48 KB = 104 KB: two CTAs per SM whatever the mix.
+// 3*8 + 2*16 + 48 KB = 104 KB at 256 threads per CTA: two CTAs per SM
+// whatever the mix.  Smaller CTAs take proportionally smaller caps (tiles of
+// fewer cells), so that shared memory never limits the CTAs per SM below
+// what 256-thread CTAs get.
 constexpr unsigned kCapU = 8u * 1024u, kCapG = 16u * 1024u, kCapW = 48u * 1024u;
 
-bool within_caps(unsigned bu, unsigned bg, unsigned bw)
+bool within_caps(unsigned bu, unsigned bg, unsigned bw, int threads)
 {
-  return bu <= kCapU && bg <= kCapG && bw <= kCapW;
+  const unsigned t = (unsigned)threads, f = (unsigned)kCellThreads;
+  return bu * f <= kCapU * t && bg * f <= kCapG * t && bw * f <= kCapW * t;
 }
 
 const BatchKernelInfo* family_for(int dtype)
@@ -73,15 +77,19 @@ const BatchKernelInfo* batch_family_for(int dtype) { return family_for(dtype); }
 
 namespace
 {
-// Default layout of a variant for the batch kernel (256 threads per CTA):
-// the best lane efficiency for tiles whose stages stay within the cap.
-BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v)
+// Default layout of a variant for the batch kernel with `threads` threads
+// per CTA: the best lane efficiency for tiles whose stages stay within the
+// caps.
+BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads)
 {
   const int op = v / kBatchDegrees, n = 2 + v % kBatchDegrees, q = n + 1;
+  const int lanes = fam.family == kFamilySlab
+                        ? batch_slab_lanes(op == 0 ? OP_MASS : OP_STIFFNESS, n)
+                        : 1;
   BatchLayout best{4, 0, 0, 0};
   if (fam.family == kFamilySlab)
   {
-    auto l = slab_layout_for(n, q, 4);
+    auto l = slab_layout_for(n, q, 4, lanes);
     best.sq = l.first;
     best.sbc = l.second;
   }
@@ -93,14 +101,13 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v)
     l.staged = 0;
     unsigned bu, bg, bw;
     fam.bytes(v, l, &bu, &bg, &bw);
-    if (!within_caps(bu, bg, bw))
+    if (!within_caps(bu, bg, bw, threads))
       break;
-    // lanes: slab passes (2 lanes per slab) and pencil passes
-    const double lanes[2] = {double(cb * n * (fam.family == kFamilySlab ? 2 : 1)),
-                             double(cb * q * q)};
+    // busy lanes of the slab passes and of the pencil pass
+    const double busy[2] = {double(cb * n * lanes), double(cb * q * q)};
     double eff = 0.0;
-    for (double x : lanes)
-      eff += x / (std::ceil(x / kCellThreads) * kCellThreads);
+    for (double x : busy)
+      eff += x / (std::ceil(x / threads) * threads);
     const double score = eff + 1e-4 * cb;
     if (score > best_score)
     {
@@ -108,8 +115,17 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v)
       best = l;
     }
   }
-  (void)op;
   return best;
+}
+
+// Threads per CTA without tuning.  The CUDA-core family needs about 255
+// registers per thread (the whole slab of a degree-7 cell), so a 256-thread
+// CTA is alone on its SM and every barrier of a tile idles the SM; two
+// 128-thread CTAs per SM overlap one another's barriers and TMA waits.  The
+// tensor-core families fit in 128 registers and run two 256-thread CTAs.
+int default_threads(const BatchKernelInfo& fam)
+{
+  return fam.family == kFamilySlab ? 128 : kCellThreads;
 }
 
 } // namespace
@@ -149,7 +165,7 @@ int batch_plan(femtc_batch* b, const std::vector<BatchLayout>& lay,
   if (e != cudaSuccess)
     return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
   int per_sm = 0, dev = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fam.fn, kCellThreads, b->smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fam.fn, b->threads, b->smem);
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (per_sm < 1)
@@ -217,10 +233,12 @@ namespace
 {
 } // namespace
 
-BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v)
+BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v, int threads)
 {
-  return default_batch_layout(fam, v);
+  return default_batch_layout(fam, v, threads);
 }
+
+int batch_default_threads(const BatchKernelInfo& fam) { return default_threads(fam); }
 
 namespace
 {
@@ -255,8 +273,8 @@ int build(femtc_batch* b, const std::vector<BatchLayout>& lay)
 int launch_eager(femtc_batch* b, cudaStream_t st)
 {
   void* args[] = {&b->params};
-  cudaError_t e = cudaLaunchKernel(b->fam->fn, dim3((unsigned)b->grid), dim3(kCellThreads), args,
-                                   b->smem, st);
+  cudaError_t e = cudaLaunchKernel(b->fam->fn, dim3((unsigned)b->grid), dim3((unsigned)b->threads),
+                                   args, b->smem, st);
   return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
 }
 
@@ -305,11 +323,9 @@ float time_launches(femtc_batch* b, cudaStream_t st, int reps)
 // Autotuner of the batch: for every variant present, time candidate tile
 // shapes on that variant's meshes alone (the batch kernel, same stage
 // budget) and keep the fastest.
-void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
+void tune_layouts(femtc_batch* b, std::vector<BatchLayout>& lay, cudaStream_t st)
 {
   const std::vector<femtc_batch_item> all = b->items;
-  cudaStream_t st;
-  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   for (int v = 0; v < kBatchVariants; ++v)
   {
     std::vector<femtc_batch_item> mine;
@@ -321,6 +337,7 @@ void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
     femtc_batch sub;
     sub.dtype = b->dtype;
     sub.fam = b->fam;
+    sub.threads = b->threads;
     sub.items = mine;
     std::memcpy(sub.params.tabs, b->params.tabs, sizeof(b->params.tabs));
     const BatchLayout base = lay[v];
@@ -334,7 +351,7 @@ void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
         l.staged = staged;
         unsigned bu, bg, bw;
         b->fam->bytes(v, l, &bu, &bg, &bw);
-        if (!within_caps(bu, bg, bw))
+        if (!within_caps(bu, bg, bw, b->threads))
           continue;
         std::vector<BatchLayout> trial = lay;
         trial[v] = l;
@@ -349,6 +366,36 @@ void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
       }
     lay[v] = best_l;
   }
+}
+
+// Threads per CTA and tile layouts: for each candidate CTA size, tune the
+// layouts variant by variant, then time the whole batch; keep the fastest.
+void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
+{
+  cudaStream_t st;
+  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  float best = 1e30f;
+  int best_threads = b->threads;
+  std::vector<BatchLayout> best_lay = lay;
+  for (int threads : {128, 256})
+  {
+    b->threads = threads;
+    std::vector<BatchLayout> trial(kBatchVariants);
+    for (int v = 0; v < kBatchVariants; ++v)
+      trial[v] = default_batch_layout(*b->fam, v, threads);
+    tune_layouts(b, trial, st);
+    if (build(b, trial) != FEMTC_OK)
+      continue;
+    const float ms = time_launches(b, st, 3);
+    if (ms < best)
+    {
+      best = ms;
+      best_threads = threads;
+      best_lay = trial;
+    }
+  }
+  b->threads = best_threads;
+  lay = best_lay;
   cudaStreamSynchronize(st);
   cudaStreamDestroy(st);
 }
@@ -408,9 +455,10 @@ int femtc_batch_create(int dtype, const femtc_batch_item* items, int nitems,
     b->items.push_back(it);
     b->ndofs += (long long)it.ncells * n * n * n;
   }
+  b->threads = default_threads(*fam);
   std::vector<BatchLayout> lay(kBatchVariants);
   for (int v = 0; v < kBatchVariants; ++v)
-    lay[v] = default_batch_layout(*fam, v);
+    lay[v] = default_batch_layout(*fam, v, b->threads);
   if (flags & FEMTC_BATCH_TUNE)
     tune(b.get(), lay);
   int rc = build(b.get(), lay);
@@ -465,6 +513,13 @@ int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
   if (geo_staged)
     *geo_staged = l.staged;
   return FEMTC_OK;
+}
+
+int femtc_batch_threads(const femtc_batch* b)
+{
+  if (!b)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
+  return b->threads;
 }
 
 void femtc_batch_destroy(femtc_batch* b) { delete b; }

@@ -18,6 +18,7 @@ struct femtc_batch
   femtc::BatchItem<float>* d_items = nullptr;
   long long ntiles = 0;
   int grid = 0;
+  int threads = femtc::kCellThreads; // per CTA (the tile code is blockDim-generic)
   unsigned smem = 0;
   long long ndofs = 0;
   cudaStream_t cap_stream = nullptr;
@@ -43,8 +44,11 @@ namespace femtc
 {
 // Kernel family of a batch dtype (FEMTC_F32, FEMTC_F16X2, FEMTC_BF16X3).
 const BatchKernelInfo* batch_family_for(int dtype);
-// Built-in tile layout of variant v for the batch kernel.
-BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v);
+// Built-in tile layout of variant v for the batch kernel with `threads`
+// threads per CTA.
+BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v, int threads);
+// Built-in threads per CTA of a family's batch kernel.
+int batch_default_threads(const BatchKernelInfo& fam);
 // Host plan of a batch: stage sizes, shared memory, grid and tile order.
 int batch_plan(femtc_batch* b, const std::vector<BatchLayout>& lay,
                std::vector<BatchTile>& order);

@@ -73,11 +73,20 @@ constexpr int kFamilySlab = 0;
 constexpr int kFamilyF16X2 = 1;
 constexpr int kFamilyBF16X3 = 2;
 
+// Lanes per slab of the CUDA-core tiles, per variant: two for the stiffness
+// operator up to N = 5 (three outputs per slab), one elsewhere -- the same
+// choice as the single-mesh launches.  Two lanes at N >= 6 would need more
+// than 255 registers for the stiffness slabs.
+__host__ __device__ constexpr int batch_slab_lanes(int op, int n)
+{
+  return (op == OP_STIFFNESS && n <= 5) ? 2 : 1;
+}
+
 template <typename T>
 struct BatchFamily<T, kFamilySlab>
 {
   template <int N, int OP>
-  using Tile = SlabTile<T, N, N + 1, OP, SEM_EXACT>;
+  using Tile = SlabTile<T, N, N + 1, OP, SEM_EXACT, batch_slab_lanes(OP, N)>;
 };
 template <>
 struct BatchFamily<float, kFamilyF16X2>

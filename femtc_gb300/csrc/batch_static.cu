@@ -132,9 +132,10 @@ extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items
     }
     b.items.push_back(it);
   }
+  b.threads = batch_default_threads(*fam);
   std::vector<BatchLayout> lay(kBatchVariants);
   for (int v = 0; v < kBatchVariants; ++v)
-    lay[v] = batch_default_layout(*fam, v);
+    lay[v] = batch_default_layout(*fam, v, b.threads);
   std::vector<BatchTile> order;
   int rc = batch_plan(&b, lay, order);
   if (rc != FEMTC_OK)
@@ -168,7 +169,8 @@ extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items
   b.params.items = reinterpret_cast<const BatchItem<float>*>(p);
   b.params.tiles = reinterpret_cast<const BatchTile*>(p + items_bytes);
   void* args[] = {&b.params};
-  e = cudaLaunchKernel(fam->fn, dim3((unsigned)b.grid), dim3(kCellThreads), args, b.smem, st);
+  e = cudaLaunchKernel(fam->fn, dim3((unsigned)b.grid), dim3((unsigned)b.threads), args, b.smem,
+                       st);
   if (e != cudaSuccess)
     return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
   return FEMTC_OK;

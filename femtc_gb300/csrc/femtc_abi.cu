@@ -795,10 +795,9 @@ void gll_nodes(int p, double* x)
 
 int aux_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 
-std::pair<int, int> slab_layout_for(int n, int q, int esize)
+std::pair<int, int> slab_layout_for(int n, int q, int esize, int lanes)
 {
-  // the batch kernels run the slab tiles with their default lanes
-  return slab_layout(n, q, esize, esize == 4 ? 2 : 1);
+  return slab_layout(n, q, esize, lanes);
 }
 } // namespace femtc
 

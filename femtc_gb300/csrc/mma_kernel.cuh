@@ -353,6 +353,43 @@ __device__ __forceinline__ void contract_pass(
   }
 }
 
+// Two contractions of the same input with two tables (one gather and one
+// split of A for both): out_a = T_a in, out_b = T_b in.
+template <int SPLIT, int K, int M, bool FWD, int Q, typename InIdx, typename OutIdx>
+__device__ __forceinline__ void contract_pass_shared(
+    const float* __restrict__ in, const Table<SPLIT, K, M, FWD, Q>& ta,
+    const Table<SPLIT, K, M, FWD, Q>& tb, InIdx iidx, int istride,
+    float* __restrict__ out_a, float* __restrict__ out_b, OutIdx oidx, int ostride, int np)
+{
+  constexpr int NT = (M + 7) / 8;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int base = warp * 16; base < np; base += nwarps * 16)
+  {
+    float v[8];
+    gather<K>(in, iidx, istride, base, np, v);
+    AFrag<SPLIT> a;
+    a.build(v);
+    {
+      Acc<SPLIT, NT> acc;
+      acc.zero();
+      acc.mma(a, ta);
+      float o[NT][4];
+      zero(o);
+      acc.unscale_into(a, o);
+      scatter<M, NT>(out_a, oidx, ostride, base, np, o);
+    }
+    {
+      Acc<SPLIT, NT> acc;
+      acc.zero();
+      acc.mma(a, tb);
+      float o[NT][4];
+      zero(o);
+      acc.unscale_into(a, o);
+      scatter<M, NT>(out_b, oidx, ostride, base, np, o);
+    }
+  }
+}
+
 template <int SPLIT, int N, int Q, int OP>
 struct MmaTile
 {
@@ -404,12 +441,15 @@ struct MmaTile
     auto oidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
     Table<SPLIT, N, Q, true, Q> phi;
     phi.build(p.P);
-    contract_pass<SPLIT, N, Q, true, Q>(su, phi, su, phi, iidx, 1, A0, oidx, 1, np);
     if constexpr (OP == OP_STIFFNESS)
     {
       Table<SPLIT, N, Q, true, Q> gam;
       gam.build(p.D);
-      contract_pass<SPLIT, N, Q, true, Q>(su, gam, su, gam, iidx, 1, A1, oidx, 1, np);
+      contract_pass_shared<SPLIT, N, Q, true, Q>(su, phi, gam, iidx, 1, A0, A1, oidx, 1, np);
+    }
+    else
+    {
+      contract_pass<SPLIT, N, Q, true, Q>(su, phi, su, phi, iidx, 1, A0, oidx, 1, np);
     }
   }
 
@@ -433,13 +473,17 @@ struct MmaTile
     };
     Table<SPLIT, N, Q, true, Q> phi;
     phi.build(p.P);
-    contract_pass<SPLIT, N, Q, true, Q>(A0, phi, A0, phi, iidx, S::QP, B0, oidx, Q, np);
     if constexpr (OP == OP_STIFFNESS)
     {
-      contract_pass<SPLIT, N, Q, true, Q>(A1, phi, A1, phi, iidx, S::QP, B2, oidx, Q, np);
       Table<SPLIT, N, Q, true, Q> gam;
       gam.build(p.D);
-      contract_pass<SPLIT, N, Q, true, Q>(A0, gam, A0, gam, iidx, S::QP, B1, oidx, Q, np);
+      // A0 feeds both Phi (-> B0) and Gamma (-> B1): one gather and split
+      contract_pass_shared<SPLIT, N, Q, true, Q>(A0, phi, gam, iidx, S::QP, B0, B1, oidx, Q, np);
+      contract_pass<SPLIT, N, Q, true, Q>(A1, phi, A1, phi, iidx, S::QP, B2, oidx, Q, np);
+    }
+    else
+    {
+      contract_pass<SPLIT, N, Q, true, Q>(A0, phi, A0, phi, iidx, S::QP, B0, oidx, Q, np);
     }
   }
 

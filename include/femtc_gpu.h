@@ -233,6 +233,8 @@ int femtc_batch_info(const femtc_batch* b, long long* ntiles, int* ctas,
                      int* smem_bytes, long long* ndofs);
 int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
                        int* geo_staged);
+/* Threads per CTA of the batch's launch (built-in or chosen by the tuner). */
+int femtc_batch_threads(const femtc_batch* b);
 void femtc_batch_destroy(femtc_batch* b);
 
 /* The batched launch for callers that cannot allocate device memory (code

@@ -142,6 +142,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def host_link_gbs(dev, nbytes=1 << 30, reps=3):
+    """Pinned host<->device copy bandwidth (GB/s, each direction alone),
+    timed with CUDA events: the ceiling of every host-buffer call."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    s = torch.cuda.current_stream()
+    out = []
+    for dst, src in ((d, h), (h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record(s)
+        torch.cuda.synchronize()
+        out.append(reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del h, d
+    return out[0], out[1]
+
+
 def peaks():
     try:
         with open(PEAKS_FILE) as f:
@@ -324,6 +346,7 @@ def run_serve(args, rank, world, dev, pg):
     from femtc_gb300 import workloads as W
     rng = np.random.default_rng(1005 + rank)
     nreq = args.requests
+    inner = {"f32": F.F32, "f16x2": F.F16X2, "bf16x3": F.BF16X3}[args.inner_dtype]
     probs = []
     for _ in range(nreq):
         P = int(rng.integers(2, 8))
@@ -334,14 +357,14 @@ def run_serve(args, rank, world, dev, pg):
         J = W.random_jacobians(rng, n).reshape(-1, 9)
         b = rng.standard_normal((n, (P + 1) ** 3))
         probs.append(F.Problem(P, P + 2, J, b, alpha=1.0, beta=sigma, rtol=1e-8,
-                               inner_dtype=F.F16X2))
+                               inner_dtype=inner))
     arrivals = np.cumsum(rng.exponential(1.0 / 2000.0, size=nreq))
     free = torch_free_bytes(dev)
     budget = int(min(free * 0.6, 120e9))
     # warm the kernels used by the solves (setup, outside the timed region)
     for P in range(2, 8):
         wp = F.Problem(P, P + 2, np.tile(np.eye(3).reshape(1, 9), (8, 1)), np.ones((8, (P + 1) ** 3)),
-                       inner_dtype=F.F16X2)
+                       inner_dtype=inner)
         F.solve(wp)
     srv = F.Server(budget, max_active=8)
     tickets = [None] * nreq
@@ -370,7 +393,8 @@ def run_serve(args, rank, world, dev, pg):
             "metric": "p50/p99 solve latency ms (serving, Poisson 2000 req/s)",
             "value": float(np.percentile(lat, 50)), "unit": "ms", "n_gpus": world,
             "steps": nreq, "warmup": 6, "ms_per_step": wall * 1e3 / nreq,
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f16x2+f64",
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": f"{args.inner_dtype}+f64",
             "data": "synthetic",
             "config": {"workload": "serve", "requests": nreq, "arrival_rate_per_s": 2000,
                        "degrees": "2..7", "cells": "log-uniform [1e3, 2e5]", "rtol": 1e-8,
@@ -402,6 +426,8 @@ def main():
     ap.add_argument("--workload", default="stiffness_p4",
                     choices=["stiffness_p4", "mass_p3", "stiffness_p6", "batch64", "serve"])
     ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
+    ap.add_argument("--inner-dtype", default="f32", choices=["f32", "f16x2", "bf16x3"],
+                    help="serve: operator form of the inner CG (FP64 refinement outside)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
@@ -590,12 +616,15 @@ def main():
         }
         if (head, 0) in e2e:
             a, z, c = e2e[(head, 0)], e2e[(head, 2)], e2e[(head, 1)]
+            h2d_gbs, d2h_gbs = host_link_gbs(dev)
+            link_s = max(a["h2d"] / (h2d_gbs * 1e9), a["d2h"] / (d2h_gbs * 1e9))
             line["e2e"] = {"value": a["gdofs"], "unit": "GDoF/s",
                            "h2d_bytes_per_step": a["h2d"], "d2h_bytes_per_step": a["d2h"],
                            "path": "femtc_*_apply_host, pinned host buffers, host-path mode "
                                    "auto (tuned: zero-copy or staging pipeline)",
                            "zero_copy_gdofs": z["gdofs"], "staging_pipeline_gdofs": c["gdofs"],
-                           "host_link_ceiling_gdofs": w.ndofs / (a["h2d"] / 211e9) / 1e9}
+                           "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
+                           "host_link_ceiling_gdofs": w.ndofs / link_s / 1e9}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(w)
         print(json.dumps(line), flush=True)

@@ -17,7 +17,7 @@ from . import buildlib as _build
 
 F64, F32, F16X2, BF16X3, F64E = 0, 1, 2, 3, 4
 EXACT, REFERENCE = 0, 1
-MASS, STIFFNESS = 0, 1
+MASS, STIFFNESS, HELMHOLTZ = 0, 1, 2
 
 DTYPE_NAMES = {F64: "f64", F32: "f32", F16X2: "f16x2", BF16X3: "bf16x3", F64E: "f64e"}
 FP64_STORAGE = (F64, F64E)
@@ -45,6 +45,9 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_supported": ([c_int] * 5, c_int),
         "femtc_mass_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
         "femtc_stiffness_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
+        "femtc_helmholtz_apply": ([c_int] * 3 + [vp] * 4 + [c_size, vp], c_int),
+        "femtc_helmholtz_geometry": ([c_int, ctypes.c_double, vp, ctypes.c_double, vp, vp, c_size, vp],
+                                     c_int),
         "femtc_mass_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_stiffness_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_set_tile_config": ([c_int] * 9, c_int),
@@ -154,6 +157,22 @@ def apply(op: int, dtype: int, semantics: int, degree: int, nquad: int,
     fn = lib.femtc_mass_apply if op == MASS else lib.femtc_stiffness_apply
     check(fn(dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
              ptr(geo), ncells, stream_ptr(stream)))
+
+
+def helmholtz_apply(dtype: int, degree: int, nquad: int, tables, u, y, geo8, ncells: int,
+                    stream=None) -> None:
+    """y = alpha M u + beta K u in one pass (femtc_helmholtz_apply); geo8 is
+    the interleaved [ncells][Q^3][8] geometry of helmholtz_geometry."""
+    tab = host_tables(tables, dtype)
+    check(load().femtc_helmholtz_apply(dtype, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
+                                       ptr(geo8), ncells, stream_ptr(stream)))
+
+
+def helmholtz_geometry(nquad: int, alpha: float, dw, beta: float, G, geo8, ncells: int,
+                       stream=None) -> None:
+    """geo8 = [beta G, alpha dw, 0] per quadrature point (FP32 device buffers)."""
+    check(load().femtc_helmholtz_geometry(nquad, alpha, ptr(dw), beta, ptr(G), ptr(geo8), ncells,
+                                          stream_ptr(stream)))
 
 
 def apply_host(op: int, dtype: int, semantics: int, degree: int, nquad: int,

@@ -267,6 +267,22 @@ int contractions_t(int na, int nb, int tr, const void* i0, const void* i1,
 
 using namespace femtc;
 
+// geo8[p] = (beta G[p][0..5], alpha dw[p], 0) per quadrature point p: the
+// interleaved geometry of the Helmholtz operator (two 16-byte stores).
+__global__ void __launch_bounds__(256)
+    helmholtz_geometry_kernel(const float* __restrict__ dw, const float* __restrict__ G,
+                              float alpha, float beta, float4* __restrict__ geo8,
+                              long long npts)
+{
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts;
+       p += (long long)gridDim.x * blockDim.x)
+  {
+    const float* g = G + p * 6;
+    geo8[2 * p] = make_float4(beta * g[0], beta * g[1], beta * g[2], beta * g[3]);
+    geo8[2 * p + 1] = make_float4(beta * g[4], beta * g[5], alpha * dw[p], 0.0f);
+  }
+}
+
 extern "C" {
 
 int femtc_gemm_blocked(int dtype, int k, int m, int n, const void* a,
@@ -331,6 +347,25 @@ int femtc_geometry(int out_dtype, int nquad, const double* weights,
         p.w[(a * nquad + b) * nquad + c] = weights[a] * weights[b] * weights[c];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   geometry_kernel<<<grid_for(p.ncells * p.q3, 256), 256, 0, st>>>(p);
+  return launch_error(cudaGetLastError());
+}
+
+int femtc_helmholtz_geometry(int nquad, double alpha, const void* dw, double beta,
+                             const void* G, void* geo8, size_t ncells, void* stream)
+{
+  if (nquad < 1 || nquad > 10)
+    return aux_fail(FEMTC_ERR_INVALID, "helmholtz_geometry: nquad in [1,10]");
+  if (!dw || !G || !geo8)
+    return aux_fail(FEMTC_ERR_INVALID, "helmholtz_geometry: null pointer");
+  if ((reinterpret_cast<uintptr_t>(geo8) & 15u) != 0)
+    return aux_fail(FEMTC_ERR_INVALID, "helmholtz_geometry: geo8 must be 16-byte aligned");
+  if (ncells == 0)
+    return FEMTC_OK;
+  const long long npts = (long long)ncells * nquad * nquad * nquad;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  helmholtz_geometry_kernel<<<grid_for(npts, 256), 256, 0, st>>>(
+      static_cast<const float*>(dw), static_cast<const float*>(G), (float)alpha, (float)beta,
+      static_cast<float4*>(geo8), npts);
   return launch_error(cudaGetLastError());
 }
 

@@ -21,19 +21,58 @@ std::pair<int, int> slab_layout_for(int n, int q, int esize, int lanes); // femt
 namespace
 {
 constexpr unsigned kBatchSmemCap = 220u * 1024u;
-// Per-variant caps on a tile's stage sizes: the batch's shared memory is the
-// sum of the maxima over its variants (3 x DOF/output stage, 2 x geometry
-// stage, work), so capping each part keeps every mix of variants within
-// 3*8 + 2*16 + 48 KB = 104 KB at 256 threads per CTA: two CTAs per SM
-// whatever the mix.  Smaller CTAs take proportionally smaller caps (tiles of
-// fewer cells), so that shared memory never limits the CTAs per SM below
-// what 256-thread CTAs get.
-constexpr unsigned kCapU = 8u * 1024u, kCapG = 16u * 1024u, kCapW = 48u * 1024u;
 
-bool within_caps(unsigned bu, unsigned bg, unsigned bw, int threads)
+// Shared memory one CTA of the batch kernel may take without lowering the
+// number of CTAs per SM that its registers allow (the kernel's register
+// count is its largest variant's, so registers set the occupancy and shared
+// memory is sized to it).
+unsigned smem_budget(const BatchKernelInfo& fam, int threads)
 {
-  const unsigned t = (unsigned)threads, f = (unsigned)kCellThreads;
-  return bu * f <= kCapU * t && bg * f <= kCapG * t && bw * f <= kCapW * t;
+  cudaFuncAttributes a{};
+  int dev = 0, regs_sm = 65536, smem_sm = 228 * 1024;
+  if (cudaFuncGetAttributes(&a, fam.fn) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess)
+    return 104u * 1024u;
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  const int warps = (threads + 31) / 32;
+  const int regs_warp = (a.numRegs * 32 + 255) / 256 * 256; // allocation unit: 256
+  const int ctas = std::max(1, std::min(8, regs_sm / std::max(1, regs_warp * warps)));
+  const long long b = (long long)smem_sm / ctas - 1024 - (long long)a.sharedSizeBytes;
+  return (unsigned)std::max<long long>(16 * 1024, std::min<long long>(b, kBatchSmemCap));
+}
+
+// Variants present in a list of meshes.
+std::vector<char> variants_present(const std::vector<femtc_batch_item>& items)
+{
+  std::vector<char> present(kBatchVariants, 0);
+  for (const femtc_batch_item& it : items)
+    present[batch_variant(it.op, it.degree + 1)] = 1;
+  return present;
+}
+
+// Shared memory of a batch CTA: the stages hold the largest tile of the
+// variants present (3 x DOF/output stage, 2 x geometry stage, work).
+unsigned smem_of_mix(const BatchKernelInfo& fam, const std::vector<char>& present,
+                     const std::vector<BatchLayout>& lay, unsigned* su_out = nullptr,
+                     unsigned* sg_out = nullptr, unsigned* sw_out = nullptr)
+{
+  unsigned su = 0, sg = 0, sw = 0;
+  for (int v = 0; v < kBatchVariants; ++v)
+    if (present[v])
+    {
+      unsigned bu, bg, bw;
+      fam.bytes(v, lay[v], &bu, &bg, &bw);
+      su = std::max(su, (bu + 15u) & ~15u);
+      sg = std::max(sg, (bg + 15u) & ~15u);
+      sw = std::max(sw, (bw + 15u) & ~15u);
+    }
+  if (su_out)
+    *su_out = su;
+  if (sg_out)
+    *sg_out = sg;
+  if (sw_out)
+    *sw_out = sw;
+  return 128 + 2 * (su + sg) + su + sw;
 }
 
 const BatchKernelInfo* family_for(int dtype)
@@ -78,9 +117,8 @@ const BatchKernelInfo* batch_family_for(int dtype) { return family_for(dtype); }
 namespace
 {
 // Default layout of a variant for the batch kernel with `threads` threads
-// per CTA: the best lane efficiency for tiles whose stages stay within the
-// caps.
-BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads)
+// per CTA: the best lane efficiency for tiles whose own stages fit `budget`.
+BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads, unsigned budget)
 {
   const int op = v / kBatchDegrees, n = 2 + v % kBatchDegrees, q = n + 1;
   const int lanes = fam.family == kFamilySlab
@@ -101,7 +139,7 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads)
     l.staged = 0;
     unsigned bu, bg, bw;
     fam.bytes(v, l, &bu, &bg, &bw);
-    if (!within_caps(bu, bg, bw, threads))
+    if (128 + 3 * bu + 2 * bg + bw > budget)
       break;
     // busy lanes of the slab passes and of the pencil pass
     const double busy[2] = {double(cb * n * lanes), double(cb * q * q)};
@@ -116,6 +154,42 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads)
     }
   }
   return best;
+}
+
+// Default layouts of a mix: every variant's own best, then the tiles that
+// set the stage maxima shrink (4 cells at a time) until the mix fits the
+// budget.
+std::vector<BatchLayout> default_batch_layouts(const BatchKernelInfo& fam, int threads,
+                                               const std::vector<char>& present)
+{
+  const unsigned budget = smem_budget(fam, threads);
+  std::vector<BatchLayout> lay(kBatchVariants);
+  for (int v = 0; v < kBatchVariants; ++v)
+    lay[v] = default_batch_layout(fam, v, threads, budget);
+  unsigned total = smem_of_mix(fam, present, lay);
+  while (total > budget)
+  {
+    int best_v = -1;
+    unsigned best_total = total;
+    for (int v = 0; v < kBatchVariants; ++v)
+    {
+      if (!present[v] || lay[v].cb <= 4)
+        continue;
+      std::vector<BatchLayout> trial = lay;
+      trial[v].cb -= 4;
+      const unsigned t = smem_of_mix(fam, present, trial);
+      if (t < best_total)
+      {
+        best_total = t;
+        best_v = v;
+      }
+    }
+    if (best_v < 0)
+      break; // every tile at its minimum: the plan runs with fewer CTAs per SM
+    lay[best_v].cb -= 4;
+    total = best_total;
+  }
+  return lay;
 }
 
 // Threads per CTA without tuning.  The CUDA-core family needs about 255
@@ -140,20 +214,13 @@ int batch_plan(femtc_batch* b, const std::vector<BatchLayout>& lay,
   BatchParams<float>& p = b->params;
   for (int v = 0; v < kBatchVariants; ++v)
     p.lay[v] = lay[v];
-  // stage sizes: max over the variants present
+  // stage sizes: max over the variants present (work buffers at least as
+  // large as the batch's min_smem asks, so that a sub-batch timed by the
+  // tuner runs at the full batch's occupancy)
   unsigned su = 0, sg = 0, sw = 0;
-  std::vector<char> present(kBatchVariants, 0);
-  for (const femtc_batch_item& it : b->items)
-    present[batch_variant(it.op, it.degree + 1)] = 1;
-  for (int v = 0; v < kBatchVariants; ++v)
-    if (present[v])
-    {
-      unsigned bu, bg, bw;
-      fam.bytes(v, lay[v], &bu, &bg, &bw);
-      su = std::max(su, (bu + 15u) & ~15u);
-      sg = std::max(sg, (bg + 15u) & ~15u);
-      sw = std::max(sw, (bw + 15u) & ~15u);
-    }
+  const unsigned mix = smem_of_mix(fam, variants_present(b->items), lay, &su, &sg, &sw);
+  if (b->min_smem > mix)
+    sw += (b->min_smem - mix + 15u) & ~15u;
   p.stage_u = su;
   p.stage_g = sg;
   p.stage_y = su;
@@ -233,9 +300,10 @@ namespace
 {
 } // namespace
 
-BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v, int threads)
+std::vector<BatchLayout> batch_default_layouts(const BatchKernelInfo& fam, int threads,
+                                               const std::vector<femtc_batch_item>& items)
 {
-  return default_batch_layout(fam, v, threads);
+  return default_batch_layouts(fam, threads, variants_present(items));
 }
 
 int batch_default_threads(const BatchKernelInfo& fam) { return default_threads(fam); }
@@ -326,6 +394,8 @@ float time_launches(femtc_batch* b, cudaStream_t st, int reps)
 void tune_layouts(femtc_batch* b, std::vector<BatchLayout>& lay, cudaStream_t st)
 {
   const std::vector<femtc_batch_item> all = b->items;
+  const std::vector<char> present = variants_present(all);
+  const unsigned budget = smem_budget(*b->fam, b->threads);
   for (int v = 0; v < kBatchVariants; ++v)
   {
     std::vector<femtc_batch_item> mine;
@@ -349,12 +419,14 @@ void tune_layouts(femtc_batch* b, std::vector<BatchLayout>& lay, cudaStream_t st
         BatchLayout l = base;
         l.cb = std::max(4, (base.cb * mult / 4 + 3) / 4 * 4);
         l.staged = staged;
-        unsigned bu, bg, bw;
-        b->fam->bytes(v, l, &bu, &bg, &bw);
-        if (!within_caps(bu, bg, bw, b->threads))
-          continue;
         std::vector<BatchLayout> trial = lay;
         trial[v] = l;
+        // the whole mix must stay within the budget; the sub-batch is timed
+        // with the mix's shared memory (same CTAs per SM)
+        const unsigned mix = smem_of_mix(*b->fam, present, trial);
+        if (mix > budget && !(mult == 1 && staged == 0))
+          continue;
+        sub.min_smem = mix;
         if (build(&sub, trial) != FEMTC_OK)
           continue;
         const float ms = time_launches(&sub, st, 3);
@@ -380,9 +452,8 @@ void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
   for (int threads : {128, 256})
   {
     b->threads = threads;
-    std::vector<BatchLayout> trial(kBatchVariants);
-    for (int v = 0; v < kBatchVariants; ++v)
-      trial[v] = default_batch_layout(*b->fam, v, threads);
+    std::vector<BatchLayout> trial =
+        default_batch_layouts(*b->fam, threads, variants_present(b->items));
     tune_layouts(b, trial, st);
     if (build(b, trial) != FEMTC_OK)
       continue;
@@ -456,9 +527,7 @@ int femtc_batch_create(int dtype, const femtc_batch_item* items, int nitems,
     b->ndofs += (long long)it.ncells * n * n * n;
   }
   b->threads = default_threads(*fam);
-  std::vector<BatchLayout> lay(kBatchVariants);
-  for (int v = 0; v < kBatchVariants; ++v)
-    lay[v] = default_batch_layout(*fam, v, b->threads);
+  std::vector<BatchLayout> lay = batch_default_layouts(*fam, b->threads, b->items);
   if (flags & FEMTC_BATCH_TUNE)
     tune(b.get(), lay);
   int rc = build(b.get(), lay);

@@ -19,6 +19,7 @@ struct femtc_batch
   long long ntiles = 0;
   int grid = 0;
   int threads = femtc::kCellThreads; // per CTA (the tile code is blockDim-generic)
+  unsigned min_smem = 0;             // shared memory at least (tuner sub-batches)
   unsigned smem = 0;
   long long ndofs = 0;
   cudaStream_t cap_stream = nullptr;
@@ -44,9 +45,11 @@ namespace femtc
 {
 // Kernel family of a batch dtype (FEMTC_F32, FEMTC_F16X2, FEMTC_BF16X3).
 const BatchKernelInfo* batch_family_for(int dtype);
-// Built-in tile layout of variant v for the batch kernel with `threads`
-// threads per CTA.
-BatchLayout batch_default_layout(const BatchKernelInfo& fam, int v, int threads);
+// Built-in tile layouts (one per variant) of the batch kernel with `threads`
+// threads per CTA for a mix of meshes: within the shared memory that keeps
+// the CTAs per SM its registers allow.
+std::vector<BatchLayout> batch_default_layouts(const BatchKernelInfo& fam, int threads,
+                                               const std::vector<femtc_batch_item>& items);
 // Built-in threads per CTA of a family's batch kernel.
 int batch_default_threads(const BatchKernelInfo& fam);
 // Host plan of a batch: stage sizes, shared memory, grid and tile order.

@@ -14,8 +14,7 @@
 // ragged tiles are loaded without TMA.
 //
 // Tables ride in the parameter block, one slot per degree: the slot index is
-// a compile-time constant of each dispatched variant, so table operands stay
-// constant-bank operands.
+// a compile-time constant of each dispatched variant.
 #pragma once
 
 #include "cell_kernel.cuh"
@@ -108,7 +107,7 @@ __host__ __device__ inline void batch_tile_bytes(const BatchLayout& l,
                                                  unsigned* bw)
 {
   using Tl = typename BatchFamily<T, FAMILY>::template Tile<N, OP>;
-  constexpr int Q = N + 1, NC = OP == OP_MASS ? 1 : 6;
+  constexpr int Q = N + 1, NC = geo_nc(OP);
   CellParams<T> p{};
   p.cb = l.cb;
   p.geo_staged = l.staged;
@@ -139,7 +138,7 @@ __device__ __noinline__ void batch_issue(const BatchParams<T>& bp,
                                             const BatchSmem& sm, int s)
 {
   using Tl = typename BatchFamily<T, FAMILY>::template Tile<N, OP>;
-  constexpr int Q = N + 1, NC = OP == OP_MASS ? 1 : 6;
+  constexpr int Q = N + 1, NC = geo_nc(OP);
   constexpr int N2 = N * N, N3 = N * N * N, Q3NC = Q * Q * Q * NC;
   const BatchLayout& l = bp.lay[batch_variant(OP, N)];
   const BatchItem<T>& it = bp.items[t.item];
@@ -173,7 +172,7 @@ __device__ __noinline__ void batch_run(const BatchParams<T>& bp,
                                           const BatchSmem& sm, int s)
 {
   using Tl = typename BatchFamily<T, FAMILY>::template Tile<N, OP>;
-  constexpr int Q = N + 1, NC = OP == OP_MASS ? 1 : 6;
+  constexpr int Q = N + 1, NC = geo_nc(OP);
   constexpr int N2 = N * N, N3 = N * N * N, Q3NC = Q * Q * Q * NC;
   constexpr int US = Tl::US;
   const BatchLayout& l = bp.lay[batch_variant(OP, N)];

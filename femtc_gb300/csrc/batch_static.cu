@@ -133,9 +133,7 @@ extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items
     b.items.push_back(it);
   }
   b.threads = batch_default_threads(*fam);
-  std::vector<BatchLayout> lay(kBatchVariants);
-  for (int v = 0; v < kBatchVariants; ++v)
-    lay[v] = batch_default_layout(*fam, v, b.threads);
+  const std::vector<BatchLayout> lay = batch_default_layouts(*fam, b.threads, b.items);
   std::vector<BatchTile> order;
   int rc = batch_plan(&b, lay, order);
   if (rc != FEMTC_OK)

@@ -17,8 +17,7 @@ unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
   p.geo_staged = staged;
   p.sq = sq;
   p.sbc = sbc;
-  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L>, N, Q,
-                     (OP == OP_MASS) ? 1 : 6>(p)
+  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L>, N, Q, geo_nc(OP)>(p)
       .total;
 }
 
@@ -66,6 +65,21 @@ void add_exact_upto(std::vector<CellVariant>& v, int dtype)
     add_variant<T, N, N + 1, OP, SEM_EXACT, L>(v, dtype);
     add_variant<T, N, N + 2, OP, SEM_EXACT, L>(v, dtype);
     add_exact_upto<T, OP, L, N + 1, MAXN>(v, dtype);
+  }
+}
+
+// Helmholtz (exact semantics only), N = N0..8, Q = N..N+2; lanes per slab
+// as the stiffness operator's default (two up to N = 5).
+template <typename T, int N>
+void add_helmholtz(std::vector<CellVariant>& v, int dtype)
+{
+  if constexpr (N <= 8)
+  {
+    constexpr int L = N <= 5 ? 2 : 1;
+    add_variant<T, N, N, OP_HELMHOLTZ, SEM_EXACT, L>(v, dtype);
+    add_variant<T, N, N + 1, OP_HELMHOLTZ, SEM_EXACT, L>(v, dtype);
+    add_variant<T, N, N + 2, OP_HELMHOLTZ, SEM_EXACT, L>(v, dtype);
+    add_helmholtz<T, N + 1>(v, dtype);
   }
 }
 

@@ -40,8 +40,17 @@ namespace femtc
 enum Op : int
 {
   OP_MASS = 0,
-  OP_STIFFNESS = 1
+  OP_STIFFNESS = 1,
+  OP_HELMHOLTZ = 2 // alpha M + beta K in one pass (exact semantics)
 };
+
+// Geometry values per quadrature point: mass detJ*w; stiffness the six
+// components of G; Helmholtz [zz,yz,xz,yy,xy,xx] of beta*G, then alpha*detJ*w
+// and one zero (eight values: four 8-byte pairs per point).
+__host__ __device__ constexpr int geo_nc(int op)
+{
+  return op == OP_MASS ? 1 : (op == OP_STIFFNESS ? 6 : 8);
+}
 enum Sem : int
 {
   SEM_EXACT = 0,
@@ -97,7 +106,7 @@ struct CellParams
   using ST = storage_t<T>;
   const ST* u;       // [ncells][N^3]
   ST* y;             // [ncells][N^3]
-  const ST* geo;     // mass: [ncells][Q^3]; stiffness: [ncells][Q^3][6]
+  const ST* geo;     // [ncells][Q^3][geo_nc(op)] (mass: [ncells][Q^3])
   long long ncells;
   int cb;            // cells per tile, a multiple of 4
   int geo_staged;    // 1: geometry slab staged by TMA, 0: read in the fused pass
@@ -124,7 +133,7 @@ struct Shape
 {
   static constexpr int N3 = N * N * N;
   static constexpr int Q3 = Q * Q * Q;
-  static constexpr int NC = (OP == OP_MASS) ? 1 : 6;
+  static constexpr int NC = geo_nc(OP);
   static constexpr int QP = Q | 1; // odd row length: conflict-free pencils
   static constexpr int SA = N * N * QP; // [i0][i1][q2] buffers
   static constexpr int SB = N * Q * Q;  // [i0][q1][q2] buffers
@@ -422,6 +431,9 @@ struct SlabTile
   static constexpr bool kSlabCopies = (N % 2 == 0);
   static constexpr int US = slab_stride<ST>(N);
   static constexpr int N2 = N * N, Q2 = Q * Q, Q3 = Q * Q * Q;
+  // the gradient passes: stiffness and Helmholtz (the latter exact only)
+  static constexpr bool kGrad = (OP != OP_MASS);
+  static_assert(OP != OP_HELMHOLTZ || SEM == SEM_EXACT, "Helmholtz: exact semantics only");
   static constexpr int NBUF =
       (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
@@ -542,7 +554,7 @@ struct SlabTile
           for (int i2 = 1; i2 < N; ++i2)
             acc = fma(pq(i2), x[i1 * N + i2], acc);
           a[i1] = acc;
-          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          if constexpr (kGrad && SEM == SEM_EXACT)
           {
             T gcc = dq(0) * x[i1 * N];
 #pragma unroll
@@ -559,7 +571,7 @@ struct SlabTile
           for (int i1 = 1; i1 < N; ++i1)
             o0 = fma(P[q1 + i1 * Q], a[i1], o0);
           b0[q1 * Q + q2] = o0; // AA = Phi_1 Phi_2 u
-          if constexpr (OP == OP_STIFFNESS)
+          if constexpr (kGrad)
           {
             T o1 = D[q1] * a[0];
 #pragma unroll
@@ -613,8 +625,10 @@ struct SlabTile
       }
       else
       {
-        const ST* G = geo + ((geo_cell0 + c) * Q3 + r) * 6;
+        constexpr int NCG = geo_nc(OP);
+        const ST* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG;
         T xa[N], xg[N], fx[Q], fy[Q], fz[Q];
+        T fm[OP == OP_HELMHOLTZ ? Q : 1];
 #pragma unroll
         for (int k = 0; k < N; ++k)
         {
@@ -623,6 +637,8 @@ struct SlabTile
         }
         mv<Q, N, 1, Q>(D, xa, fx); // d/dx: Gamma on axis 0
         mv<Q, N, 1, Q>(P, xg, fy); // d/dy: Gamma was applied on axis 1
+        if constexpr (OP == OP_HELMHOLTZ)
+          mv<Q, N, 1, Q>(P, xa, fm); // the value u at the points (mass term)
         if constexpr (SEM == SEM_EXACT)
         {
           T xb[N];
@@ -636,13 +652,16 @@ struct SlabTile
           mv<Q, N, 1, Q>(P, xa, fz); // reference: W_z carries no derivative
         }
         // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx], read
-        // as three 8/16-byte pairs
+        // as three 8/16-byte pairs (Helmholtz: a fourth pair holds the mass
+        // factor)
         using V2 = typename std::conditional<sizeof(ST) == 4, float2, double2>::type;
 #pragma unroll
         for (int q = 0; q < Q; ++q)
         {
-          const V2* g2 = reinterpret_cast<const V2*>(G + (long long)q * Q2 * 6);
+          const V2* g2 = reinterpret_cast<const V2*>(G + (long long)q * Q2 * NCG);
           const V2 g01 = g2[0], g23 = g2[1], g45 = g2[2];
+          if constexpr (OP == OP_HELMHOLTZ)
+            fm[q] *= from_storage<T>(g2[3].x);
           const T zz = from_storage<T>(g01.x), yz = from_storage<T>(g01.y),
                   xz = from_storage<T>(g23.x), yy = from_storage<T>(g23.y),
                   xy = from_storage<T>(g45.x), xx = from_storage<T>(g45.y);
@@ -658,6 +677,8 @@ struct SlabTile
         if constexpr (SEM == SEM_EXACT)
         {
           mv<N, Q, BSM, BSK>(D, fx, o);
+          if constexpr (OP == OP_HELMHOLTZ)
+            mv_acc<N, Q, BSM, BSK>(P, fm, o); // Phi_0^T (m u): same chain as x
 #pragma unroll
           for (int k = 0; k < N; ++k)
             b0[k * sq] = o[k];
@@ -730,7 +751,7 @@ struct SlabTile
         for (int q1 = 0; q1 < Q; ++q1)
         {
           X[q1] = b0[q1 * Q + q2];
-          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          if constexpr (kGrad && SEM == SEM_EXACT)
           {
             Y[q1] = b1[q1 * Q + q2];
             Z[q1] = b2[q1 * Q + q2];
@@ -744,7 +765,7 @@ struct SlabTile
 #pragma unroll
           for (int q1 = 1; q1 < Q; ++q1)
             acc = fma(P[i1 * BSM + q1 * BSK], X[q1], acc);
-          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          if constexpr (kGrad && SEM == SEM_EXACT)
           {
 #pragma unroll
             for (int q1 = 0; q1 < Q; ++q1)
@@ -769,7 +790,7 @@ struct SlabTile
 #pragma unroll
           for (int i1 = 0; i1 < N; ++i1)
             y[i1 * N + i2] = fma(t1, U1[i1], y[i1 * N + i2]);
-          if constexpr (OP == OP_STIFFNESS && SEM == SEM_EXACT)
+          if constexpr (kGrad && SEM == SEM_EXACT)
           {
             T t2;
             if constexpr (PRE)
@@ -803,7 +824,7 @@ template <typename T, int N, int Q, int OP, int SEM, int LANES>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  stream_tiles<T, SlabTile<T, N, Q, OP, SEM, LANES>, N, Q, (OP == OP_MASS) ? 1 : 6>(p);
+  stream_tiles<T, SlabTile<T, N, Q, OP, SEM, LANES>, N, Q, geo_nc(OP)>(p);
 }
 
 } // namespace femtc

@@ -61,6 +61,7 @@ Registry& registry()
     register_cell_f32_mass_l2(r.cells, r.faults);
     register_cell_f32_stiffness_l1(r.cells, r.faults);
     register_cell_f32_stiffness_l2(r.cells, r.faults);
+    register_cell_f32_helmholtz(r.cells, r.faults);
     register_cell_f64e_mass(r.cells, r.faults);
     register_cell_f64e_stiffness(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);
@@ -90,7 +91,7 @@ int default_lanes(int op, int dtype, int n)
 {
   if (dtype != FEMTC_F32)
     return 1;
-  return (op == FEMTC_OP_STIFFNESS && n <= 5) ? 2 : 1;
+  return (op != FEMTC_OP_MASS && n <= 5) ? 2 : 1;
 }
 
 // ---------------------------------------------------------------- tiles --
@@ -416,7 +417,8 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
   if (!v)
     return fail(FEMTC_ERR_UNSUPPORTED,
                 "no %s kernel for dtype %d, semantics %d, degree %d, nquad %d",
-                op == FEMTC_OP_MASS ? "mass" : "stiffness", dtype, sem, degree,
+                op == FEMTC_OP_MASS ? "mass" : (op == FEMTC_OP_STIFFNESS ? "stiffness" : "Helmholtz"),
+                dtype, sem, degree,
                 nquad);
   *out = v;
   return FEMTC_OK;
@@ -454,7 +456,7 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
   p.sq = cfg.sq;
   p.sbc = cfg.sbc;
   p.host_io = host_io;
-  const int ntab = (v.op == FEMTC_OP_STIFFNESS) ? 2 : 1;
+  const int ntab = (v.op != FEMTC_OP_MASS) ? 2 : 1;
   for (int t = 0; t < ntab; ++t)
     for (int i = 0; i < v.n * v.q; ++i)
       p.tab[t][i] = param_value<T>(tables[t * v.n * v.q + i]);
@@ -642,7 +644,7 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
   }
   const size_t es = elem_size(dtype);
   const size_t n3 = (size_t)v->n * v->n * v->n;
-  const size_t q3 = (size_t)v->q * v->q * v->q * (op == FEMTC_OP_MASS ? 1 : 6);
+  const size_t q3 = (size_t)v->q * v->q * v->q * geo_nc(op);
   const size_t bu = ncells * n3 * es, bg = ncells * q3 * es;
   if ((rc = host_buffer(0, bu)) != FEMTC_OK ||
       (rc = host_buffer(1, bu)) != FEMTC_OK ||
@@ -846,6 +848,16 @@ int femtc_stiffness_apply(int dtype, int semantics, int degree, int nquad,
 {
   return apply(FEMTC_OP_STIFFNESS, dtype, semantics, degree, nquad, tables, u,
                y, G, ncells, stream);
+}
+
+int femtc_helmholtz_apply(int dtype, int degree, int nquad, const void* tables,
+                          const void* u, void* y, const void* geo8,
+                          size_t ncells, void* stream)
+{
+  if (dtype != FEMTC_F32)
+    return fail(FEMTC_ERR_UNSUPPORTED, "Helmholtz: FEMTC_F32 only (got dtype %d)", dtype);
+  return apply(FEMTC_OP_HELMHOLTZ, dtype, FEMTC_EXACT, degree, nquad, tables, u, y, geo8,
+               ncells, stream);
 }
 
 int femtc_mass_apply_host(int dtype, int semantics, int degree, int nquad,

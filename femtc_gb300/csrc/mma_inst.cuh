@@ -14,7 +14,7 @@ unsigned mma_smem_bytes(int cb, int staged, int, int)
   p.cb = cb;
   p.geo_staged = staged;
   return tile_layout<float, MmaTile<SPLIT, N, Q, OP>, N, Q,
-                     (OP == OP_MASS) ? 1 : 6>(p)
+                     geo_nc(OP)>(p)
       .total;
 }
 

@@ -720,7 +720,7 @@ template <int SPLIT, int N, int Q, int OP>
 __global__ void __launch_bounds__(kCellThreads)
     mma_kernel(const __grid_constant__ CellParams<float> p)
 {
-  stream_tiles<float, MmaTile<SPLIT, N, Q, OP>, N, Q, (OP == OP_MASS) ? 1 : 6>(p);
+  stream_tiles<float, MmaTile<SPLIT, N, Q, OP>, N, Q, geo_nc(OP)>(p);
 }
 
 } // namespace femtc

@@ -31,6 +31,7 @@ void register_cell_f32_mass_l1(std::vector<CellVariant>&, std::vector<FaultReade
 void register_cell_f32_mass_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32_stiffness_l1(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32_stiffness_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32_helmholtz(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_f16x2_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);

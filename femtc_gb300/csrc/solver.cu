@@ -9,7 +9,9 @@
 //   inner (mixed): CG on A d = r/||r|| with the FP32 / tensor-core operator,
 //                  FP32 vectors, FP64 dot products, to a loose tolerance;
 //                  x += ||r|| d.
-// The operator is the sum of the library's mass and stiffness actions.  The
+// The FP32 inner operator is one fused Helmholtz launch (alpha M + beta K,
+// femtc_helmholtz_apply); the tensor-core forms sum the library's mass and
+// stiffness actions.  The
 // Jacobi diagonal comes from sum factorization (squared and product 1D tables
 // applied to the per-point factors).  Inner iterations run as CUDA graphs of
 // kItersPerGraph iterations; the host reads one residual scalar per graph.
@@ -41,8 +43,9 @@ constexpr int kDiagTab = 10 * 9; // Q*N entries of a 1D table (Q <= 10, N <= 9)
 // ---------------------------------------------------------------- diag --
 struct DiagParams
 {
-  const float* dw;   // [ncells][Q^3]
-  const float* G;    // [ncells][Q^3][6] ([zz,yz,xz,yy,xy,xx])
+  const float* dw;   // [ncells][Q^3] (point stride gs: 1, or 8 in geo8)
+  const float* G;    // [ncells][Q^3][gs] ([zz,yz,xz,yy,xy,xx]; gs = 6, or 8)
+  int ds, gs;        // point strides of dw and G
   float* invdiag;    // [ncells][N^3]: 1 / diag(alpha M + beta K)
   long long ncells;
   int n, q;
@@ -88,7 +91,7 @@ __global__ void __launch_bounds__(256) diag_kernel(const __grid_constant__ DiagP
         continue;
       const float c = coef[t];
       for (int i = threadIdx.x; i < q3; i += blockDim.x)
-        F[i] = c * (comp[t] < 0 ? p.dw[cell * q3 + i] : p.G[(cell * q3 + i) * 6 + comp[t]]);
+        F[i] = c * (comp[t] < 0 ? p.dw[(cell * q3 + i) * p.ds] : p.G[(cell * q3 + i) * p.gs + comp[t]]);
       __syncthreads();
       const float* A0 = tb + t0[t] * qn;
       const float* A1 = tb + t1[t] * qn;
@@ -305,11 +308,40 @@ __global__ void __launch_bounds__(kRedThreads)
     b[i] = (float)a[i];
 }
 
+// geo8[p] = (beta G[p][0..5], alpha dw[p], 0) in FP32 from the FP64 factors:
+// the interleaved geometry of the Helmholtz kernel
+__global__ void __launch_bounds__(kRedThreads)
+    pack_geo8_kernel(const double* dw, const double* G, double a, double c, float4* geo8,
+                     long long npts)
+{
+  for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < npts;
+       i += (long long)gridDim.x * kRedThreads)
+  {
+    const double* g = G + i * 6;
+    geo8[2 * i] = make_float4((float)(c * g[0]), (float)(c * g[1]), (float)(c * g[2]),
+                              (float)(c * g[3]));
+    geo8[2 * i + 1] = make_float4((float)(c * g[4]), (float)(c * g[5]), (float)(a * dw[i]), 0.f);
+  }
+}
+
+// s = <p, Ap> partial sums (the fused operator already wrote Ap)
+__global__ void __launch_bounds__(kRedThreads)
+    dot_kernel(const float* pv, const float* Ap, long long n, double* part)
+{
+  double s = 0.0;
+  for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n;
+       i += (long long)gridDim.x * kRedThreads)
+    s += (double)pv[i] * (double)Ap[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0)
+    part[blockIdx.x] = s;
+}
+
 // --------------------------------------------------------------- buffers --
 struct Bufs
 {
   double *J, *dw64, *G64, *b, *x, *r, *t1d, *t2d, *part;
-  float *dw32, *G32, *r32, *z, *p, *Ap, *t1, *t2, *d, *invdiag;
+  float *dw32, *G32, *geo8, *r32, *z, *p, *Ap, *t1, *t2, *d, *invdiag;
   Scalars* sc;
 };
 
@@ -334,8 +366,15 @@ size_t carve(void* base, int n, int q, size_t nc, Bufs* B)
   b.t1d = (double*)take(n3 * 8);
   b.t2d = (double*)take(n3 * 8);
   b.part = (double*)take(2 * kRedBlocks * 8);
-  b.dw32 = (float*)take(q3 * 4);
-  b.G32 = (float*)take(6 * q3 * 4);
+  // FP32 geometry: separate dw and G (mass and stiffness launches), or the
+  // interleaved geo8 of the fused Helmholtz launch, in one region sized for
+  // the larger (8 values per point)
+  {
+    char* g = take(8 * q3 * 4);
+    b.dw32 = (float*)g;
+    b.G32 = g ? (float*)(g + align256(q3 * 4)) : nullptr;
+    b.geo8 = (float*)g;
+  }
   b.r32 = (float*)take(n3 * 4);
   b.z = (float*)take(n3 * 4);
   b.p = (float*)take(n3 * 4);
@@ -361,21 +400,40 @@ int grid_of(long long n)
   return (int)(g < kRedBlocks ? (g < 1 ? 1 : g) : kRedBlocks);
 }
 
-// One inner CG iteration (7 launches) on stream st.
+// The FP32 inner operator with a stiffness term runs as one Helmholtz
+// launch (alpha and beta folded into its geometry).
+bool fused_operator(const femtc_solve_request& rq)
+{
+  return rq.inner_dtype == FEMTC_F32 && rq.beta != 0.0;
+}
+
+// One inner CG iteration (6 or 7 launches) on stream st.
 int inner_iteration(const femtc_solve_request& rq, const Bufs& B, const float* tab32,
                     size_t nd, cudaStream_t st)
 {
-  int rc = femtc_mass_apply(rq.inner_dtype, FEMTC_EXACT, rq.degree, rq.nquad, tab32, B.p,
-                            B.t1, B.dw32, rq.ncells, st);
-  if (rc == FEMTC_OK && rq.beta != 0.0)
-    rc = femtc_stiffness_apply(rq.inner_dtype, FEMTC_EXACT, rq.degree, rq.nquad, tab32, B.p,
-                               B.t2, B.G32, rq.ncells, st);
-  if (rc != FEMTC_OK)
-    return rc;
   const int g = grid_of((long long)nd);
-  ap_dot_kernel<<<g, kRedThreads, 0, st>>>(B.t1, rq.beta != 0.0 ? B.t2 : B.t1, (float)rq.alpha,
-                                           rq.beta != 0.0 ? (float)rq.beta : 0.f, B.p, B.Ap,
-                                           (long long)nd, B.part);
+  if (fused_operator(rq))
+  {
+    int rc = femtc_helmholtz_apply(FEMTC_F32, rq.degree, rq.nquad, tab32, B.p, B.Ap, B.geo8,
+                                   rq.ncells, st);
+    if (rc != FEMTC_OK)
+      return rc;
+    dot_kernel<<<g, kRedThreads, 0, st>>>(B.p, B.Ap, (long long)nd, B.part);
+  }
+  else
+  {
+    int rc = femtc_mass_apply(rq.inner_dtype, FEMTC_EXACT, rq.degree, rq.nquad, tab32, B.p,
+                              B.t1, B.dw32, rq.ncells, st);
+    if (rc == FEMTC_OK && rq.beta != 0.0)
+      rc = femtc_stiffness_apply(rq.inner_dtype, FEMTC_EXACT, rq.degree, rq.nquad, tab32, B.p,
+                                 B.t2, B.G32, rq.ncells, st);
+    if (rc != FEMTC_OK)
+      return rc;
+    ap_dot_kernel<<<g, kRedThreads, 0, st>>>(B.t1, rq.beta != 0.0 ? B.t2 : B.t1,
+                                             (float)rq.alpha,
+                                             rq.beta != 0.0 ? (float)rq.beta : 0.f, B.p, B.Ap,
+                                             (long long)nd, B.part);
+  }
   reduce_alpha_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc);
   update_kernel<<<g, kRedThreads, 0, st>>>(B.sc, B.p, B.Ap, B.d, B.r32, B.z, B.invdiag,
                                            (long long)nd, B.part);
@@ -447,20 +505,31 @@ int solve_on_stream(const femtc_solve_request* rq, femtc_solve_result* res, cuda
   rc = femtc_geometry(FEMTC_F64, q, wts.data(), B.J, 0, B.dw64, B.G64, nc, st);
   if (rc != FEMTC_OK)
     return finish(rc);
-  to_f32_kernel<<<grid_of((long long)q3), kRedThreads, 0, st>>>(B.dw64, B.dw32, (long long)q3);
-  to_f32_kernel<<<grid_of((long long)(6 * q3)), kRedThreads, 0, st>>>(B.G64, B.G32,
-                                                                      (long long)(6 * q3));
+  const bool fused = fused_operator(*rq);
+  if (fused)
+    pack_geo8_kernel<<<grid_of((long long)q3), kRedThreads, 0, st>>>(
+        B.dw64, B.G64, rq->alpha, rq->beta, reinterpret_cast<float4*>(B.geo8), (long long)q3);
+  else
+  {
+    to_f32_kernel<<<grid_of((long long)q3), kRedThreads, 0, st>>>(B.dw64, B.dw32,
+                                                                  (long long)q3);
+    to_f32_kernel<<<grid_of((long long)(6 * q3)), kRedThreads, 0, st>>>(B.G64, B.G32,
+                                                                        (long long)(6 * q3));
+  }
   {
     DiagParams dp;
     std::memset(&dp, 0, sizeof(dp));
-    dp.dw = B.dw32;
-    dp.G = B.G32;
+    // the fused geometry already carries alpha and beta
+    dp.dw = fused ? B.geo8 + 6 : B.dw32;
+    dp.G = fused ? B.geo8 : B.G32;
+    dp.ds = fused ? 8 : 1;
+    dp.gs = fused ? 8 : 6;
     dp.invdiag = B.invdiag;
     dp.ncells = (long long)nc;
     dp.n = n;
     dp.q = q;
-    dp.alpha = (float)rq->alpha;
-    dp.beta = (float)rq->beta;
+    dp.alpha = fused ? 1.0f : (float)rq->alpha;
+    dp.beta = fused ? 1.0f : (float)rq->beta;
     for (int i = 0; i < q * n; ++i)
     {
       dp.phi[i] = (float)tab64[i];

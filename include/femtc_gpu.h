@@ -61,7 +61,8 @@ typedef enum
 typedef enum
 {
   FEMTC_OP_MASS = 0,
-  FEMTC_OP_STIFFNESS = 1
+  FEMTC_OP_STIFFNESS = 1,
+  FEMTC_OP_HELMHOLTZ = 2 /* alpha M + beta K in one pass (femtc_helmholtz_apply) */
 } femtc_op;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -103,7 +104,28 @@ int femtc_stiffness_apply(int dtype, int semantics, int degree, int nquad,
                           const void* tables, const void* u, void* y,
                           const void* G, size_t ncells, void* stream);
 
-/* Host-buffer forms of the two calls above: every pointer is host memory
+/* Helmholtz action y = alpha M u + beta K u in one pass over the cells,
+ * device-resident buffers, exact semantics, FEMTC_F32 only.  No reference
+ * counterpart: the reference applies mass and stiffness separately; this
+ * is the operator of the matrix-free solver (femtc_solve) exposed as an
+ * entry point.  One read of u and one write of y instead of two each; the
+ * stiffness passes already hold the values the mass term needs.
+ * geo8: [ncells][Q^3][8] per quadrature point: beta*G as
+ * [zz,yz,xz,yy,xy,xx], then alpha*detJ*w, then 0 (the caller folds alpha and
+ * beta in; femtc_helmholtz_geometry builds it from dw and G).
+ * tables: Phi then Gamma, as for femtc_stiffness_apply. */
+int femtc_helmholtz_apply(int dtype, int degree, int nquad, const void* tables,
+                          const void* u, void* y, const void* geo8,
+                          size_t ncells, void* stream);
+
+/* geo8 = [beta*G, alpha*dw, 0] per quadrature point from dw [ncells][Q^3]
+ * and G [ncells][Q^3][6], all FP32 device buffers (16-byte aligned geo8),
+ * asynchronous on `stream`. */
+int femtc_helmholtz_geometry(int nquad, double alpha, const void* dw,
+                             double beta, const void* G, void* geo8,
+                             size_t ncells, void* stream);
+
+/* Host-buffer forms of mass and stiffness: every pointer is host memory
  * (pinned memory copies fastest).  Copies u and dw/G to the device, applies
  * the operator, copies y back and returns when y is written -- the drop-in
  * path behind the templated C++ header femtc_gpu/operators.hpp. */

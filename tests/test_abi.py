@@ -93,3 +93,18 @@ def test_fp32_lanes_choice_roundtrip(femtc):
         assert femtc.get_tile_config(*key) == (12, 0, 128, lanes)
     femtc.set_tile_config(*key, 0, 0)
     assert femtc.get_tile_config(*key)[3] in (1, 2)
+
+
+def test_helmholtz_supported_and_rejected(femtc):
+    """The fused Helmholtz action: FP32 exact Q in N..N+2 built, other forms
+    rejected before any device work."""
+    lib = femtc.load()
+    for P in range(1, 8):
+        for Q in (P + 1, P + 2, P + 3):
+            assert femtc.supported(femtc.HELMHOLTZ, femtc.F32, femtc.EXACT, P, Q)
+        assert not femtc.supported(femtc.HELMHOLTZ, femtc.F64, femtc.EXACT, P, P + 1)
+    t = np.zeros(128, dtype=np.float32)
+    assert lib.femtc_helmholtz_apply(femtc.F64, 3, 4, t.ctypes.data, 16, 16, 16, 1, None) == -2
+    assert lib.femtc_helmholtz_apply(femtc.F32, 3, 4, t.ctypes.data, None, 16, 16, 1, None) == -1
+    assert lib.femtc_helmholtz_geometry(0, 1.0, 16, 1.0, 16, 16, 1, None) == -1
+    assert lib.femtc_helmholtz_geometry(4, 1.0, 16, 1.0, 16, 24, 1, None) == -1  # misaligned

@@ -50,6 +50,71 @@ def flops_per_cell(op: int, n: int, q: int) -> float:
     return 4.0 * q * n * (2 * n * n + 3 * q * n + 3 * q * q) + 15.0 * q ** 3
 
 
+def _eo_mv_flops(m: int, k: int, sig: int) -> int:
+    """FP64 operations (FMA = 2) of one even-odd contraction, M outputs from
+    K inputs, as the kernels' mv_eo executes it."""
+    m2, mm, k2, km = m // 2, m % 2, k // 2, k % 2
+    mid = (2 * (k2 + km) - 1) if sig > 0 else (2 * k2 - 1)
+    return 2 * k2 + m2 * (4 * k2 + 2 * km) + mm * mid
+
+
+def flops_per_cell_even_odd(op: int, n: int, q: int) -> float:
+    """Operations the even-odd kernels execute per cell (forward_eo, fused
+    pass, backward_eo in cell_kernel.cuh); the achieved rate of the FP64 pipe
+    is this count over the kernel time."""
+    grad = op != 0
+    n2, nm, q2, qm = n // 2, n % 2, q // 2, q % 2
+    mv_f = lambda s: _eo_mv_flops(q, n, s)   # N -> Q
+    mv_b = lambda s: _eo_mv_flops(n, q, s)   # Q -> N
+    # forward, per slab
+    emit = mv_f(1) + (mv_f(-1) + mv_f(1) if grad else 0)
+    pair_row = (4 * n2 + 2 * nm) * (2 if grad else 1)
+    mid_row = (2 * (n2 + nm) - 1) + ((2 * n2 - 1) if grad else 0)
+    fwd = n * 2 * n2 + q2 * (n * pair_row + 2 * emit) + qm * (n * mid_row + emit)
+    # fused, per pencil
+    if grad:
+        fused = 3 * mv_f(1) + 15 * q + 3 * mv_b(1)
+    else:
+        fused = mv_f(1) + q + mv_b(1)
+    # backward, per slab
+    col = mv_b(1) + ((mv_b(-1) + n + mv_b(1)) if grad else 0)
+    pair_acc = n * ((2 + 4 * n2 + 2 * nm) * (2 if grad else 1))
+    mid_col = n * (2 * n2 * (2 if grad else 1) + 2 * nm)
+    bwd = q2 * (2 * col + pair_acc) + qm * (col + mid_col) + n * 2 * n2
+    return float(n * fwd + q * q * fused + n * bwd)
+
+
+def _eo_mv_instr(m: int, k: int, sig: int) -> int:
+    """Arithmetic instructions (FMA, MUL, ADD: one each) of mv_eo."""
+    m2, mm, k2, km = m // 2, m % 2, k // 2, k % 2
+    mid = (k2 + km) if sig > 0 else k2
+    return 2 * k2 + m2 * (2 * k2 + km + 2) + mm * mid
+
+
+def pipe_instr_per_cell(op: int, n: int, q: int, even_odd: bool) -> float:
+    """FP64-pipe instructions per cell: every FMA, MUL and ADD takes one
+    issue slot of the pipe, so this (not the flop count) is what the pipe's
+    busy fraction measures.  Plain kernels: one FMA per multiply-add plus
+    the point-wise work; even-odd kernels: as their code runs."""
+    grad = op != 0
+    if not even_odd:
+        macs = flops_per_cell(op, n, q) - (15 if grad else 1) * q ** 3
+        return macs / 2 + (9 if grad else 1) * q ** 3
+    n2, nm, q2, qm = n // 2, n % 2, q // 2, q % 2
+    mv_f = lambda s: _eo_mv_instr(q, n, s)
+    mv_b = lambda s: _eo_mv_instr(n, q, s)
+    emit = mv_f(1) + (mv_f(-1) + mv_f(1) if grad else 0)
+    pair_row = (2 * n2 + nm + 2) * (2 if grad else 1)
+    mid_row = (n2 + nm) + (n2 if grad else 0)
+    fwd = n * 2 * n2 + q2 * (n * pair_row + 2 * emit) + qm * (n * mid_row + emit)
+    fused = (3 * mv_f(1) + 9 * q + 3 * mv_b(1)) if grad else (mv_f(1) + q + mv_b(1))
+    col = mv_b(1) + ((mv_b(-1) + n + mv_b(1)) if grad else 0)
+    pair_acc = n * ((2 + 2 * n2 + nm) * (2 if grad else 1))
+    mid_col = n * (n2 * (2 if grad else 1) + nm)
+    bwd = q2 * (2 * col + pair_acc) + qm * (col + mid_col) + n * 2 * n2
+    return float(n * fwd + q * q * fused + n * bwd)
+
+
 def bytes_per_cell(op: int, n: int, q: int, es: int) -> float:
     return es * (2 * n ** 3 + (1 if op == 0 else 6) * q ** 3)
 
@@ -63,14 +128,15 @@ def traffic_for(workload, ncells, dtype):
     return MEASURED_TRAFFIC.get((workload, ncells, dtype))
 
 
-def roofline(head, ach_tf, ach_gbs, hbm, hbm_src, traffic=None):
+def roofline(head, ach_tf, ach_gbs, hbm, hbm_src, traffic=None, flop_count=None, pipe_frac=None):
     """The binding roof of the headline kernel: the FP64 pipe for FP64 (its
     arithmetic intensity puts it far above the FP64 ridge), HBM otherwise."""
     hbm_part = {"achieved": ach_gbs, "peak": hbm, "unit": "GB/s", "frac": ach_gbs / hbm,
                 "peak_source": hbm_src}
     if head == 0:
         return {"bound": "fp64", "achieved": ach_tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                "frac": ach_tf / FP64_PEAK_TFLOPS, "traffic": traffic,
+                "frac": ach_tf / FP64_PEAK_TFLOPS, "flop_count": flop_count,
+                "fp64_pipe_instruction_frac": pipe_frac, "traffic": traffic,
                 "traffic_unit": "bytes per launch (ncu, profiles/stiffness_p4_32k_cells_slab_kernels.md)",
                 "peak_source": "measured FP64 FMA pipe (profiles/gb300_pipe_peaks.md)",
                 "hbm": hbm_part}
@@ -431,7 +497,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
-    ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3,f64e",
+    ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3,f64e,f64plain",
                     help="comma list of forms to time; the first is the headline")
     ap.add_argument("--tile-db", default=None,
                     help="tile configuration file: loaded if it exists (no tuning), "
@@ -466,6 +532,12 @@ def main():
     n, q, op = w.n, w.nquad, w.op
     stream = torch.cuda.current_stream()
     names = {v: k for k, v in F.DTYPE_NAMES.items()}
+    # "f64plain": FP64 with the even-odd contractions switched off (the plain
+    # sum-factorized kernels), for comparison with the default FP64 form
+    F64PLAIN = -1
+    names["f64plain"] = F64PLAIN
+    dname = dict(F.DTYPE_NAMES)
+    dname[F64PLAIN] = "f64plain"
     dtypes = [names[d] for d in args.dtypes.split(",")]
     head = dtypes[0]
 
@@ -493,9 +565,11 @@ def main():
         tuned = True
     launches_timed = [0]
     results = {}
-    for dtype in dtypes:
+    for key in dtypes:
+        dtype = F.F64 if key == F64PLAIN else key
         if not F.supported(op, dtype, F.EXACT, w.degree, q):
             continue
+        F.set_even_odd(key != F64PLAIN)
         tdt = torch.float64 if dtype in F.FP64_STORAGE else torch.float32
         u = torch.from_numpy(w.u).to(dev, tdt)
         g = torch.from_numpy(w.geo).to(dev, tdt)
@@ -504,7 +578,7 @@ def main():
         def step():
             F.apply(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
 
-        if not tuned:  # the project's autotuner, outside the timed region
+        if not tuned and key != F64PLAIN:  # the project's autotuner, outside the timed region
             F.autotune(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
         tile = F.get_tile_config(op, dtype, F.EXACT, w.degree, q)
 
@@ -513,7 +587,7 @@ def main():
         barrier()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
-        sampler = ClockSampler(local) if dtype == head else None
+        sampler = ClockSampler(local) if key == head else None
         if sampler:
             sampler.__enter__()
         barrier()
@@ -536,8 +610,9 @@ def main():
         if y_oracle is not None:
             yo = y[:err_cells].double().cpu().numpy()
             err = float(np.abs(yo - y_oracle).max() / np.abs(y_oracle).max())
-        results[dtype] = dict(total_ms=total_ms, kern_ms=kern_ms, err=err, tile=tile,
-                              clocks=sampler.summary() if sampler else None)
+        results[key] = dict(total_ms=total_ms, kern_ms=kern_ms, err=err, tile=tile,
+                            clocks=sampler.summary() if sampler else None)
+        F.set_even_odd(True)
         if F.device_status() != 0:
             raise RuntimeError("device fault word set during the benchmark")
         del u, g, y
@@ -582,18 +657,27 @@ def main():
     r = results[head]
     value = world * args.steps * w.ndofs / (r["total_ms"] * 1e-3) / 1e9
     fpc = flops_per_cell(op, n, q)
+    # the FP64 pipe's roof counts the operations the kernel runs: the even-odd
+    # kernels execute fewer than the reference's flop convention
+    head_eo = head == F.F64 and F.even_odd_used(op, F.F64, F.EXACT, w.degree, q, w.tables)
+    fpc_head = flops_per_cell_even_odd(op, n, q) if head_eo else fpc
     bpc = bytes_per_cell(op, n, q, 8 if head == F.F64 else 4)
-    ach_tf = fpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e12
+    ach_tf = fpc_head * w.ncells / (r["kern_ms"] * 1e-3) / 1e12
+    # FP64 pipe: instructions issued per second against its peak (half the
+    # FMA flop rate: one FMA = two flops = one instruction)
+    pipe_frac = (pipe_instr_per_cell(op, n, q, head_eo) * w.ncells / (r["kern_ms"] * 1e-3)
+                 / (FP64_PEAK_TFLOPS * 1e12 / 2)) if head == F.F64 else None
     ach_gbs = bpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e9
     hbm, hbm_src = peaks()
     variants = {}
-    for dtype, res in results.items():
+    for key, res in results.items():
+        dtype = F.F64 if key == F64PLAIN else key
         es = 8 if dtype in F.FP64_STORAGE else 4
-        variants[F.DTYPE_NAMES[dtype]] = {
+        variants[dname[key]] = {
             "gdofs": world * args.steps * w.ndofs / (res["total_ms"] * 1e-3) / 1e9,
             "kernel_ms": res["kern_ms"],
             "hbm_gbs": bytes_per_cell(op, n, q, es) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
-            "tflops": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
+            "tflops_reference_convention": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
             "max_rel_err_vs_fp64_oracle": res["err"],
             "tile": {"cells": res["tile"][0], "geo_staged": res["tile"][1], "threads": res["tile"][2],
                      "lanes_per_slab": res["tile"][3]},
@@ -609,7 +693,10 @@ def main():
                        "dofs": w.ndofs, "parallelism": f"replicas{world}",
                        "l2": f"inputs {bpc * w.ncells / 1e6:.0f} MB > 129 MB L2, no flush"},
             "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src,
-                                 traffic_for(args.workload, w.ncells, head)),
+                                 traffic_for(args.workload, w.ncells, head),
+                                 flop_count=("even-odd kernel operations per cell "
+                                             f"{fpc_head:.0f} (reference convention {fpc:.0f})")
+                                 if head == F.F64 else None, pipe_frac=pipe_frac),
             "gpu_launches": launches_timed[0],
             "clocks": r["clocks"],
             "variants": variants,

@@ -46,6 +46,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_mass_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
         "femtc_stiffness_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
         "femtc_helmholtz_apply": ([c_int] * 3 + [vp] * 4 + [c_size, vp], c_int),
+        "femtc_set_even_odd": ([c_int], c_int),
+        "femtc_even_odd_used": ([c_int] * 5 + [vp], c_int),
         "femtc_helmholtz_geometry": ([c_int, ctypes.c_double, vp, ctypes.c_double, vp, vp, c_size, vp],
                                      c_int),
         "femtc_mass_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
@@ -183,6 +185,19 @@ def apply_host(op: int, dtype: int, semantics: int, degree: int, nquad: int,
     fn = lib.femtc_mass_apply_host if op == MASS else lib.femtc_stiffness_apply_host
     check(fn(dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
              ptr(geo), ncells))
+
+
+def set_even_odd(enable: bool) -> None:
+    """Even-odd contractions for symmetric tables (FP64, exact); on by default."""
+    check(load().femtc_set_even_odd(1 if enable else 0))
+
+
+def even_odd_used(op: int, dtype: int, semantics: int, degree: int, nquad: int, tables) -> bool:
+    """Whether a launch with these tables runs the even-odd kernels."""
+    tab = host_tables(tables, dtype)
+    rc = load().femtc_even_odd_used(op, dtype, semantics, degree, nquad, tab.ctypes.data)
+    check(min(rc, 0))
+    return rc == 1
 
 
 def operator_launches() -> int:

@@ -8,6 +8,7 @@
 #include "registry.hpp"
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <queue>
@@ -114,6 +115,94 @@ namespace
 
 const BatchKernelInfo* batch_family_for(int dtype) { return family_for(dtype); }
 
+bool even_odd_tables_f32(const float* tab, int n, int q, int ntab); // femtc_abi.cu
+
+int batch_setup(femtc_batch* b, int dtype, const femtc_batch_item* items, int nitems,
+                const char* who)
+{
+  char msg[160];
+  auto bad = [&](int code, const char* what) -> int {
+    std::snprintf(msg, sizeof(msg), "%s: %s", who, what);
+    return aux_fail(code, msg);
+  };
+  const BatchKernelInfo* fam = family_for(dtype);
+  if (!fam)
+    return bad(FEMTC_ERR_UNSUPPORTED, "dtype must be FEMTC_F32, FEMTC_F16X2 or FEMTC_BF16X3");
+  if (!items || nitems < 1)
+    return bad(FEMTC_ERR_INVALID, "no items");
+  b->dtype = dtype;
+  b->fam = fam;
+  std::memset(&b->params, 0, sizeof(b->params));
+  char slot_set[kBatchDegrees] = {};
+  for (int i = 0; i < nitems; ++i)
+  {
+    const femtc_batch_item& it = items[i];
+    if (it.op != FEMTC_OP_MASS && it.op != FEMTC_OP_STIFFNESS)
+      return bad(FEMTC_ERR_INVALID, "bad op");
+    if (it.degree < 1 || it.degree > kBatchDegrees)
+      return bad(FEMTC_ERR_UNSUPPORTED, "degree must be in 1..7");
+    if (it.nquad != it.degree + 2)
+      return bad(FEMTC_ERR_UNSUPPORTED, "nquad must be degree+2");
+    if (!it.tables || !it.u || !it.y || !it.geo)
+      return bad(FEMTC_ERR_INVALID, "null pointer in an item");
+    if (!aligned16(it.u) || !aligned16(it.y) || !aligned16(it.geo))
+      return bad(FEMTC_ERR_INVALID, "device pointers must be 16-byte aligned");
+    const int n = it.degree + 1, q = it.nquad, slot = n - 2;
+    const int ntab = it.op == FEMTC_OP_STIFFNESS ? 2 : 1;
+    const float* t = static_cast<const float*>(it.tables);
+    for (int w = 0; w < ntab; ++w)
+    {
+      float* dst = b->params.tabs[slot][w];
+      if (slot_set[slot] & (1 << w))
+      {
+        if (std::memcmp(dst, t + w * q * n, sizeof(float) * q * n) != 0)
+          return bad(FEMTC_ERR_INVALID, "meshes of the same degree must share their tables");
+      }
+      else
+      {
+        std::memcpy(dst, t + w * q * n, sizeof(float) * q * n);
+        slot_set[slot] |= (char)(1 << w);
+      }
+    }
+    b->items.push_back(it);
+    b->ndofs += (long long)it.ncells * n * n * n;
+  }
+  // FP32 with symmetric tables everywhere: the even-odd family, whose
+  // per-degree tables are the even-odd forms of Phi, Gamma, Phi^T, Gamma^T
+  if (dtype == FEMTC_F32)
+  {
+    bool eo = true;
+    for (int slot = 0; slot < kBatchDegrees && eo; ++slot)
+      if (slot_set[slot])
+      {
+        const int n = slot + 2, q = n + 1;
+        float both[2 * kMaxQ * kMaxN];
+        std::memcpy(both, b->params.tabs[slot][0], sizeof(float) * q * n);
+        std::memcpy(both + q * n, b->params.tabs[slot][1], sizeof(float) * q * n);
+        eo = even_odd_tables_f32(both, n, q, (slot_set[slot] & 2) ? 2 : 1);
+      }
+    if (eo)
+    {
+      static const BatchKernelInfo f32eo = batch_kernel_f32eo();
+      b->fam = &f32eo;
+      for (int slot = 0; slot < kBatchDegrees; ++slot)
+        if (slot_set[slot])
+        {
+          const int n = slot + 2, q = n + 1;
+          float plain[2][kMaxQ * kMaxN];
+          std::memcpy(plain, b->params.tabs[slot], sizeof(plain));
+          for (int w = 0; w < 2; ++w)
+          {
+            const int sig = w == 0 ? 1 : -1;
+            host_eo_table<float>(plain[w], q, n, 1, q, sig, b->params.tabs[slot][w]);
+            host_eo_table<float>(plain[w], n, q, q, 1, sig, b->params.tabs[slot][2 + w]);
+          }
+        }
+    }
+  }
+  return FEMTC_OK;
+}
+
 namespace
 {
 // Default layout of a variant for the batch kernel with `threads` threads
@@ -123,9 +212,9 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads,
   const int op = v / kBatchDegrees, n = 2 + v % kBatchDegrees, q = n + 1;
   const int lanes = fam.family == kFamilySlab
                         ? batch_slab_lanes(op == 0 ? OP_MASS : OP_STIFFNESS, n)
-                        : 1;
+                        : 1; // even-odd and tensor-core tiles: one lane
   BatchLayout best{4, 0, 0, 0};
-  if (fam.family == kFamilySlab)
+  if (slab_family(fam.family))
   {
     auto l = slab_layout_for(n, q, 4, lanes);
     best.sq = l.first;
@@ -192,11 +281,12 @@ std::vector<BatchLayout> default_batch_layouts(const BatchKernelInfo& fam, int t
   return lay;
 }
 
-// Threads per CTA without tuning.  The CUDA-core family needs about 255
-// registers per thread (the whole slab of a degree-7 cell), so a 256-thread
-// CTA is alone on its SM and every barrier of a tile idles the SM; two
-// 128-thread CTAs per SM overlap one another's barriers and TMA waits.  The
-// tensor-core families fit in 128 registers and run two 256-thread CTAs.
+// Threads per CTA without tuning.  The plain CUDA-core family needs about
+// 255 registers per thread (the whole slab of a degree-7 cell), so a
+// 256-thread CTA is alone on its SM and every barrier of a tile idles the
+// SM; two 128-thread CTAs per SM overlap one another's barriers and TMA
+// waits.  The even-odd and tensor-core families fit in 128 registers and
+// run two 256-thread CTAs per SM.
 int default_threads(const BatchKernelInfo& fam)
 {
   return fam.family == kFamilySlab ? 128 : kCellThreads;
@@ -481,56 +571,16 @@ int femtc_batch_create(int dtype, const femtc_batch_item* items, int nitems,
   if (!out)
     return aux_fail(FEMTC_ERR_INVALID, "batch: null output");
   *out = nullptr;
-  const BatchKernelInfo* fam = family_for(dtype);
-  if (!fam)
-    return aux_fail(FEMTC_ERR_UNSUPPORTED,
-                    "batch: dtype must be FEMTC_F32, FEMTC_F16X2 or FEMTC_BF16X3");
-  if (!items || nitems < 1)
-    return aux_fail(FEMTC_ERR_INVALID, "batch: no items");
   auto b = std::make_unique<femtc_batch>();
-  b->dtype = dtype;
-  b->fam = fam;
-  std::memset(&b->params, 0, sizeof(b->params));
-  std::vector<char> slot_set(kBatchDegrees, 0);
-  for (int i = 0; i < nitems; ++i)
-  {
-    const femtc_batch_item& it = items[i];
-    if (it.op != FEMTC_OP_MASS && it.op != FEMTC_OP_STIFFNESS)
-      return aux_fail(FEMTC_ERR_INVALID, "batch: bad op");
-    if (it.degree < 1 || it.degree > kBatchDegrees)
-      return aux_fail(FEMTC_ERR_UNSUPPORTED, "batch: degree must be in 1..7");
-    if (it.nquad != it.degree + 2)
-      return aux_fail(FEMTC_ERR_UNSUPPORTED, "batch: nquad must be degree+2");
-    if (!it.tables || !it.u || !it.y || !it.geo)
-      return aux_fail(FEMTC_ERR_INVALID, "batch: null pointer in an item");
-    if (!aligned16(it.u) || !aligned16(it.y) || !aligned16(it.geo))
-      return aux_fail(FEMTC_ERR_INVALID, "batch: device pointers must be 16-byte aligned");
-    const int n = it.degree + 1, q = it.nquad, slot = n - 2;
-    const int ntab = it.op == FEMTC_OP_STIFFNESS ? 2 : 1;
-    const float* t = static_cast<const float*>(it.tables);
-    for (int w = 0; w < ntab; ++w)
-    {
-      float* dst = b->params.tabs[slot][w];
-      if (slot_set[slot] & (1 << w))
-      {
-        if (std::memcmp(dst, t + w * q * n, sizeof(float) * q * n) != 0)
-          return aux_fail(FEMTC_ERR_INVALID,
-                          "batch: meshes of the same degree must share their tables");
-      }
-      else
-      {
-        std::memcpy(dst, t + w * q * n, sizeof(float) * q * n);
-        slot_set[slot] |= (char)(1 << w);
-      }
-    }
-    b->items.push_back(it);
-    b->ndofs += (long long)it.ncells * n * n * n;
-  }
+  int rc = batch_setup(b.get(), dtype, items, nitems, "batch");
+  if (rc != FEMTC_OK)
+    return rc;
+  const BatchKernelInfo* fam = b->fam;
   b->threads = default_threads(*fam);
   std::vector<BatchLayout> lay = batch_default_layouts(*fam, b->threads, b->items);
   if (flags & FEMTC_BATCH_TUNE)
     tune(b.get(), lay);
-  int rc = build(b.get(), lay);
+  rc = build(b.get(), lay);
   if (rc != FEMTC_OK)
     return rc;
   rc = capture(b.get());

@@ -45,6 +45,11 @@ namespace femtc
 {
 // Kernel family of a batch dtype (FEMTC_F32, FEMTC_F16X2, FEMTC_BF16X3).
 const BatchKernelInfo* batch_family_for(int dtype);
+// Validate the meshes of a batch and fill b's items and per-degree tables;
+// FP32 batches whose tables are all symmetric take the even-odd family.
+// `who` prefixes the error messages.
+int batch_setup(femtc_batch* b, int dtype, const femtc_batch_item* items, int nitems,
+                const char* who);
 // Built-in tile layouts (one per variant) of the batch kernel with `threads`
 // threads per CTA for a mix of meshes: within the shared memory that keeps
 // the CTAs per SM its registers allow.

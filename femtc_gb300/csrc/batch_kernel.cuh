@@ -61,7 +61,9 @@ struct BatchParams
   long long ntiles;
   unsigned stage_u, stage_g, stage_y; // bytes of the stage regions (max)
   BatchLayout lay[kBatchVariants];
-  T tabs[kBatchDegrees][2][kMaxQ * kMaxN];
+  // per degree: Phi, Gamma; the even-odd family: the even-odd tables of Phi,
+  // Gamma (forward) and Phi^T, Gamma^T (backward)
+  T tabs[kBatchDegrees][4][kMaxQ * kMaxN];
 };
 
 // Family of tile code: the CUDA-core slab tiles or the tensor-core tiles.
@@ -71,6 +73,12 @@ struct BatchFamily;
 constexpr int kFamilySlab = 0;
 constexpr int kFamilyF16X2 = 1;
 constexpr int kFamilyBF16X3 = 2;
+constexpr int kFamilySlabEO = 3; // CUDA-core tiles, even-odd contractions
+
+__host__ __device__ constexpr bool slab_family(int family)
+{
+  return family == kFamilySlab || family == kFamilySlabEO;
+}
 
 // Lanes per slab of the CUDA-core tiles, per variant: two for the stiffness
 // operator up to N = 5 (three outputs per slab), one elsewhere -- the same
@@ -86,6 +94,13 @@ struct BatchFamily<T, kFamilySlab>
 {
   template <int N, int OP>
   using Tile = SlabTile<T, N, N + 1, OP, SEM_EXACT, batch_slab_lanes(OP, N)>;
+};
+// Every even-odd tile fits in 128 registers (one lane per slab).
+template <typename T>
+struct BatchFamily<T, kFamilySlabEO>
+{
+  template <int N, int OP>
+  using Tile = SlabTile<T, N, N + 1, OP, SEM_EXACT, 1, true>;
 };
 template <>
 struct BatchFamily<float, kFamilyF16X2>
@@ -133,7 +148,7 @@ struct BatchSmem
 
 // TMA loads of one full tile of variant (N, OP) into stage s (warp 0).
 template <typename T, int FAMILY, int N, int OP>
-__device__ __noinline__ void batch_issue(const BatchParams<T>& bp,
+__device__ __forceinline__ void batch_issue_body(const BatchParams<T>& bp,
                                             const BatchTile& t,
                                             const BatchSmem& sm, int s)
 {
@@ -167,7 +182,7 @@ __device__ __noinline__ void batch_issue(const BatchParams<T>& bp,
 
 // Compute one tile of variant (N, OP) whose inputs sit in stage s.
 template <typename T, int FAMILY, int N, int OP>
-__device__ __noinline__ void batch_run(const BatchParams<T>& bp,
+__device__ __forceinline__ void batch_run_body(const BatchParams<T>& bp,
                                           const BatchTile& t,
                                           const BatchSmem& sm, int s)
 {
@@ -177,7 +192,8 @@ __device__ __noinline__ void batch_run(const BatchParams<T>& bp,
   constexpr int US = Tl::US;
   const BatchLayout& l = bp.lay[batch_variant(OP, N)];
   const BatchItem<T>& it = bp.items[t.item];
-  const TabView<T> tv{bp.tabs[N - 2][0], bp.tabs[N - 2][1], l.sq, l.sbc};
+  const TabView<T> tv{bp.tabs[N - 2][0], bp.tabs[N - 2][1], l.sq, l.sbc, bp.tabs[N - 2][2],
+                      bp.tabs[N - 2][3]};
   const int ncb = t.ncb;
   T* su = reinterpret_cast<T*>(sm.u(s));
   T* sg = reinterpret_cast<T*>(sm.g(s));
@@ -237,6 +253,51 @@ __device__ __noinline__ void batch_run(const BatchParams<T>& bp,
   __syncthreads();
 }
 
+// Per-variant code is a separate function (one register allocation per
+// variant, the kernel's count the largest) for the plain CUDA-core family,
+// whose tiles need up to 255 registers: one function holding every variant
+// measured slower.  The even-odd family is inlined into the kernel: it then
+// fits 128 registers, where separate functions would spill kilobytes.
+template <int FAMILY>
+__host__ __device__ constexpr bool batch_inline()
+{
+  return FAMILY == kFamilySlabEO;
+}
+
+template <typename T, int FAMILY, int N, int OP>
+__device__ __noinline__ void batch_issue_call(const BatchParams<T>& bp, const BatchTile& t,
+                                              const BatchSmem& sm, int s)
+{
+  batch_issue_body<T, FAMILY, N, OP>(bp, t, sm, s);
+}
+
+template <typename T, int FAMILY, int N, int OP>
+__device__ __noinline__ void batch_run_call(const BatchParams<T>& bp, const BatchTile& t,
+                                            const BatchSmem& sm, int s)
+{
+  batch_run_body<T, FAMILY, N, OP>(bp, t, sm, s);
+}
+
+template <typename T, int FAMILY, int N, int OP>
+__device__ __forceinline__ void batch_issue(const BatchParams<T>& bp, const BatchTile& t,
+                                            const BatchSmem& sm, int s)
+{
+  if constexpr (batch_inline<FAMILY>())
+    batch_issue_body<T, FAMILY, N, OP>(bp, t, sm, s);
+  else
+    batch_issue_call<T, FAMILY, N, OP>(bp, t, sm, s);
+}
+
+template <typename T, int FAMILY, int N, int OP>
+__device__ __forceinline__ void batch_run(const BatchParams<T>& bp, const BatchTile& t,
+                                          const BatchSmem& sm, int s)
+{
+  if constexpr (batch_inline<FAMILY>())
+    batch_run_body<T, FAMILY, N, OP>(bp, t, sm, s);
+  else
+    batch_run_call<T, FAMILY, N, OP>(bp, t, sm, s);
+}
+
 #define FEMTC_BATCH_CASES(X)                                                   \
   X(2, OP_MASS) X(3, OP_MASS) X(4, OP_MASS) X(5, OP_MASS) X(6, OP_MASS)        \
   X(7, OP_MASS) X(8, OP_MASS) X(2, OP_STIFFNESS) X(3, OP_STIFFNESS)            \
@@ -244,13 +305,15 @@ __device__ __noinline__ void batch_run(const BatchParams<T>& bp,
   X(7, OP_STIFFNESS) X(8, OP_STIFFNESS)
 
 // The kernel's register budget is its largest variant's.  Tensor-core
-// families fit in 128 registers: two CTAs per SM.  The CUDA-core slab
-// tiles of degree >= 5 hold a whole slab per thread and spill under that
-// cap, so that family keeps one CTA per SM and its full register file.
+// families and the (inlined) even-odd family fit in 128 registers: two
+// 256-thread CTAs per SM.  The plain CUDA-core slab tiles of degree >= 5
+// hold a whole slab per thread and spill under that cap, so that family
+// keeps the full register file (one 256-thread CTA, or two of 128 threads,
+// per SM).
 template <int FAMILY>
 __host__ __device__ constexpr int batch_min_blocks()
 {
-  return FAMILY == 0 ? 1 : 2;
+  return FAMILY == kFamilySlab ? 1 : 2;
 }
 
 template <typename T, int FAMILY>
@@ -370,6 +433,7 @@ void batch_bytes(int v, const BatchLayout& l, unsigned* bu, unsigned* bg,
 }
 
 BatchKernelInfo batch_kernel_f32();
+BatchKernelInfo batch_kernel_f32eo();
 BatchKernelInfo batch_kernel_f16x2();
 BatchKernelInfo batch_kernel_bf16x3();
 } // namespace femtc

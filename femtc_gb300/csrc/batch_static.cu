@@ -78,12 +78,6 @@ using namespace femtc;
 extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items,
                                         int nitems, void* stream)
 {
-  const BatchKernelInfo* fam = batch_family_for(dtype);
-  if (!fam)
-    return aux_fail(FEMTC_ERR_UNSUPPORTED,
-                    "batch_apply_static: dtype must be FEMTC_F32, FEMTC_F16X2 or FEMTC_BF16X3");
-  if (!items || nitems < 1)
-    return aux_fail(FEMTC_ERR_INVALID, "batch_apply_static: no items");
   if (nitems > kStaticMaxItems)
   {
     char msg[160];
@@ -94,48 +88,14 @@ extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items
   }
   // the batch's host description; it owns no device memory
   femtc_batch b;
-  b.dtype = dtype;
-  b.fam = fam;
-  std::memset(&b.params, 0, sizeof(b.params));
-  char slot_set[kBatchDegrees] = {};
-  for (int i = 0; i < nitems; ++i)
-  {
-    const femtc_batch_item& it = items[i];
-    if (it.op != FEMTC_OP_MASS && it.op != FEMTC_OP_STIFFNESS)
-      return aux_fail(FEMTC_ERR_INVALID, "batch_apply_static: bad op");
-    if (it.degree < 1 || it.degree > kBatchDegrees || it.nquad != it.degree + 2)
-      return aux_fail(FEMTC_ERR_UNSUPPORTED,
-                      "batch_apply_static: degree in 1..7 and nquad = degree+2");
-    if (!it.tables || !it.u || !it.y || !it.geo)
-      return aux_fail(FEMTC_ERR_INVALID, "batch_apply_static: null pointer in an item");
-    if (((reinterpret_cast<uintptr_t>(it.u) | reinterpret_cast<uintptr_t>(it.y) |
-          reinterpret_cast<uintptr_t>(it.geo)) & 15u) != 0)
-      return aux_fail(FEMTC_ERR_INVALID,
-                      "batch_apply_static: device pointers must be 16-byte aligned");
-    const int n = it.degree + 1, q = it.nquad, slot = n - 2;
-    const int ntab = it.op == FEMTC_OP_STIFFNESS ? 2 : 1;
-    const float* t = static_cast<const float*>(it.tables);
-    for (int w = 0; w < ntab; ++w)
-    {
-      float* dst = b.params.tabs[slot][w];
-      if (slot_set[slot] & (1 << w))
-      {
-        if (std::memcmp(dst, t + w * q * n, sizeof(float) * q * n) != 0)
-          return aux_fail(FEMTC_ERR_INVALID,
-                          "batch_apply_static: meshes of one degree must share their tables");
-      }
-      else
-      {
-        std::memcpy(dst, t + w * q * n, sizeof(float) * q * n);
-        slot_set[slot] |= (char)(1 << w);
-      }
-    }
-    b.items.push_back(it);
-  }
+  int rc = batch_setup(&b, dtype, items, nitems, "batch_apply_static");
+  if (rc != FEMTC_OK)
+    return rc;
+  const BatchKernelInfo* fam = b.fam;
   b.threads = batch_default_threads(*fam);
   const std::vector<BatchLayout> lay = batch_default_layouts(*fam, b.threads, b.items);
   std::vector<BatchTile> order;
-  int rc = batch_plan(&b, lay, order);
+  rc = batch_plan(&b, lay, order);
   if (rc != FEMTC_OK)
     return rc;
   std::vector<BatchItem<float>> table;

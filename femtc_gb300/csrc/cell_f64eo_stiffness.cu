@@ -1,0 +1,12 @@
+// CUDA-core stiffness cell kernels, double arithmetic and storage, even-odd
+// contractions (tables with the GLL-to-Gauss symmetry), exact semantics.
+#include "cell_inst.cuh"
+
+namespace femtc
+{
+void register_cell_f64eo_stiffness(std::vector<CellVariant>& v, std::vector<FaultReader>& f)
+{
+  add_even_odd<double, OP_STIFFNESS, 2, 7>(v, 0); // FEMTC_F64 (N = 8 spills: plain form)
+  f.push_back(&read_clear_fault_word);
+}
+} // namespace femtc

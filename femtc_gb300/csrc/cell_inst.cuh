@@ -9,7 +9,7 @@
 
 namespace femtc
 {
-template <typename T, int N, int Q, int OP, int SEM, int L>
+template <typename T, int N, int Q, int OP, int SEM, int L, bool EVOD = false>
 unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
 {
   CellParams<T> p{};
@@ -17,18 +17,31 @@ unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
   p.geo_staged = staged;
   p.sq = sq;
   p.sbc = sbc;
-  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L>, N, Q, geo_nc(OP)>(p)
+  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L, EVOD>, N, Q, geo_nc(OP)>(p)
       .total;
 }
 
-template <typename T, int N, int Q, int OP, int SEM, int L>
+template <typename T, int N, int Q, int OP, int SEM, int L, bool EVOD = false>
 void add_variant(std::vector<CellVariant>& v, int dtype)
 {
   v.push_back(CellVariant{dtype, OP, SEM, N, Q,
                           reinterpret_cast<const void*>(
-                              &cell_kernel<T, N, Q, OP, SEM, L>),
-                          &cell_smem_bytes<T, N, Q, OP, SEM, L>, 1, (int)sizeof(T),
-                          L});
+                              &cell_kernel<T, N, Q, OP, SEM, L, EVOD>),
+                          &cell_smem_bytes<T, N, Q, OP, SEM, L, EVOD>, 1, (int)sizeof(T),
+                          L, EVOD ? 1 : 0});
+}
+
+// Even-odd variants (exact semantics, one lane), N = N0..MAXN, Q = N..N+2.
+template <typename T, int OP, int N, int MAXN>
+void add_even_odd(std::vector<CellVariant>& v, int dtype)
+{
+  if constexpr (N <= MAXN)
+  {
+    add_variant<T, N, N, OP, SEM_EXACT, 1, true>(v, dtype);
+    add_variant<T, N, N + 1, OP, SEM_EXACT, 1, true>(v, dtype);
+    add_variant<T, N, N + 2, OP, SEM_EXACT, 1, true>(v, dtype);
+    add_even_odd<T, OP, N + 1, MAXN>(v, dtype);
+  }
 }
 
 template <typename T, int OP, int N, int L>

@@ -114,7 +114,10 @@ struct CellParams
   int sbc;           // slab kernels: stride of one cell in the work buffers
   int host_io;       // 1: u, geo, y are host memory read/written over the
                      // coherent host link with plain vector accesses (no TMA)
-  T tab[2][kMaxQ * kMaxN]; // Phi(q,i) = tab[0][q + i*Q], Gamma = tab[1]
+  // Phi(q,i) = tab[0][q + i*Q], Gamma = tab[1]; even-odd kernels: the
+  // even-odd tables of Phi, Gamma (forward) and Phi^T, Gamma^T (backward)
+  // in tab[0..3] (see mv_eo)
+  T tab[4][kMaxQ * kMaxN];
 };
 
 // What the tile passes read besides the data: the two 1D tables (pointers
@@ -123,9 +126,11 @@ struct CellParams
 template <typename T>
 struct TabView
 {
-  const T* __restrict__ P; // Phi(q,i) = P[q + i*Q]
-  const T* __restrict__ D; // Gamma(q,i) = D[q + i*Q]
+  const T* __restrict__ P; // Phi(q,i) = P[q + i*Q] (even-odd: forward table)
+  const T* __restrict__ D; // Gamma(q,i) = D[q + i*Q] (even-odd: forward table)
   int sq, sbc;
+  const T* __restrict__ PB = nullptr; // even-odd kernels: Phi^T table
+  const T* __restrict__ DB = nullptr; // even-odd kernels: Gamma^T table
 };
 
 template <int N, int Q, int OP, int SEM>
@@ -210,6 +215,108 @@ __device__ __forceinline__ void mv_acc(const T* __restrict__ A,
   }
 }
 
+// Even-odd form of y = A x for an M x K matrix with A(M-1-m, K-1-k) =
+// SIG * A(m, k): the GLL-to-Gauss tables are such matrices (Phi symmetric,
+// Gamma antisymmetric, both nodes and points symmetric about the centre).
+// This is the even-odd decomposition of Solomonoff (1992) as described by
+// Kopriva, "Implementing Spectral Methods for PDEs" (2009), sec. 3.5: with
+// xe_k = x_k + x_{K-1-k} and xo_k = x_k - x_{K-1-k} (k < K/2), each pair of
+// outputs m, M-1-m costs K/2 + K/2 products instead of 2K:
+//   s = sum_k E(m,k) xe_k (+ C(m) x_mid for odd K),  d = sum_k O(m,k) xo_k,
+//   y_m = s + d,  y_{M-1-m} = SIG (s - d),
+// with E, O = (A(m,k) +- A(m,K-1-k)) / 2, C(m) = A(m, K/2).  The middle row
+// of odd M takes xe (SIG > 0) or xo (SIG < 0) alone.  t is the host-built
+// table: rows m <= M/2 of K entries [E (K/2) | C (odd K) | O (K/2)]; the
+// middle row keeps A(M/2, k) in the E (and C) slots for SIG > 0, in the O
+// slots for SIG < 0.
+template <int M, int K>
+struct EO
+{
+  static constexpr int M2 = M / 2, MM = M % 2, K2 = K / 2, KM = K % 2;
+  static constexpr int E = 0, C = K2, O = K2 + KM; // column offsets in a row
+};
+
+template <int M, int K, int SIG, typename T>
+__device__ __forceinline__ void mv_eo(const T* __restrict__ t, const T (&x)[K], T (&y)[M])
+{
+  using S = EO<M, K>;
+  T xe[S::K2], xo[S::K2];
+#pragma unroll
+  for (int k = 0; k < S::K2; ++k)
+  {
+    xe[k] = x[k] + x[K - 1 - k];
+    xo[k] = x[k] - x[K - 1 - k];
+  }
+#pragma unroll
+  for (int m = 0; m < S::M2; ++m)
+  {
+    T s = t[m * K + S::E] * xe[0];
+#pragma unroll
+    for (int k = 1; k < S::K2; ++k)
+      s = fma(t[m * K + S::E + k], xe[k], s);
+    if constexpr (S::KM)
+      s = fma(t[m * K + S::C], x[S::K2], s);
+    T d = t[m * K + S::O] * xo[0];
+#pragma unroll
+    for (int k = 1; k < S::K2; ++k)
+      d = fma(t[m * K + S::O + k], xo[k], d);
+    y[m] = s + d;
+    y[M - 1 - m] = SIG > 0 ? s - d : d - s;
+  }
+  if constexpr (S::MM)
+  {
+    constexpr int m = S::M2;
+    if constexpr (SIG > 0)
+    {
+      T s = t[m * K + S::E] * xe[0];
+#pragma unroll
+      for (int k = 1; k < S::K2; ++k)
+        s = fma(t[m * K + S::E + k], xe[k], s);
+      if constexpr (S::KM)
+        s = fma(t[m * K + S::C], x[S::K2], s);
+      y[m] = s;
+    }
+    else
+    {
+      T d = t[m * K + S::O] * xo[0];
+#pragma unroll
+      for (int k = 1; k < S::K2; ++k)
+        d = fma(t[m * K + S::O + k], xo[k], d);
+      y[m] = d;
+    }
+  }
+}
+
+// Host: the even-odd table of an M x K matrix A(m,k) = a[m*sm + k*sk] (see
+// mv_eo), in the arithmetic of S; entries past the used rows are left as
+// they are.
+template <typename T, typename S>
+inline void host_eo_table(const S* a, int M, int K, int sm, int sk, int sig, T* t)
+{
+  const int M2 = M / 2, MM = M % 2, K2 = K / 2, KM = K % 2;
+  auto A = [&](int m, int k) { return a[m * sm + k * sk]; };
+  for (int m = 0; m < M2 + MM; ++m)
+    for (int k = 0; k < K; ++k)
+      t[m * K + k] = T(0);
+  for (int m = 0; m < M2; ++m)
+  {
+    for (int k = 0; k < K2; ++k)
+    {
+      t[m * K + k] = T((A(m, k) + A(m, K - 1 - k)) / 2);
+      t[m * K + K2 + KM + k] = T((A(m, k) - A(m, K - 1 - k)) / 2);
+    }
+    if (KM)
+      t[m * K + K2] = T(A(m, K2));
+  }
+  if (MM)
+  {
+    for (int k = 0; k < K2; ++k)
+      t[M2 * K + (sig > 0 ? k : K2 + KM + k)] = T(A(M2, k));
+    if (KM && sig > 0)
+      t[M2 * K + K2] = T(A(M2, K2));
+  }
+}
+
 // ---------------------------------------------------------------------------
 // The streaming main loop shared by every kernel family.  `Tile` provides:
 //   kSlabCopies, US      staging of the DOF/output slabs (see slab_stride)
@@ -250,7 +357,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(ST) : 0u;
   const int lane = threadIdx.x & 31;
   const bool warp0 = threadIdx.x < 32;
-  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc};
+  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3]};
 
   if (threadIdx.x == 0)
   {
@@ -423,7 +530,10 @@ __host__ __device__ constexpr int slab_lanes()
   return sizeof(T) == 4 ? 2 : 1; // FP32: more busy lanes; FP64: pipe-bound
 }
 
-template <typename T, int N, int Q, int OP, int SEM, int LANES = slab_lanes<T>()>
+// EVOD: even-odd contractions (mv_eo) for tables with the GLL-to-Gauss
+// symmetry; one lane per slab, exact semantics.
+template <typename T, int N, int Q, int OP, int SEM, int LANES = slab_lanes<T>(),
+          bool EVOD = false>
 struct SlabTile
 {
   using ST = storage_t<T>; // staged u, y and geometry; T is the arithmetic
@@ -434,6 +544,7 @@ struct SlabTile
   // the gradient passes: stiffness and Helmholtz (the latter exact only)
   static constexpr bool kGrad = (OP != OP_MASS);
   static_assert(OP != OP_HELMHOLTZ || SEM == SEM_EXACT, "Helmholtz: exact semantics only");
+  static_assert(!EVOD || (SEM == SEM_EXACT && LANES == 1), "even-odd: exact, one lane per slab");
   static constexpr int NBUF =
       (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
@@ -502,10 +613,142 @@ struct SlabTile
     }
   }
 
+  // One pencil contraction along axis 0: forward (N -> Q) and backward
+  // (Q -> N); SIG is the table's symmetry (+1 Phi, -1 Gamma) for even-odd.
+  template <int SIG>
+  static __device__ __forceinline__ void fwd(const T* __restrict__ t, const T (&x)[N], T (&y)[Q])
+  {
+    if constexpr (EVOD)
+      mv_eo<Q, N, SIG>(t, x, y);
+    else
+      mv<Q, N, 1, Q>(t, x, y);
+  }
+  template <int SIG>
+  static __device__ __forceinline__ void bwd(const T* __restrict__ t, const T (&x)[Q], T (&y)[N])
+  {
+    if constexpr (EVOD)
+      mv_eo<N, Q, SIG>(t, x, y);
+    else
+      mv<N, Q, BSM, BSK>(t, x, y);
+  }
+
+  // Even-odd forward: the columns q2 and Q-1-q2 of a pair come from the
+  // even and odd parts of the slab's rows.
+  static __device__ __forceinline__ void forward_eo(const TabView<T>& p,
+                                                    const ST* __restrict__ su,
+                                                    T* __restrict__ sw, int ncb)
+  {
+    using E = EO<Q, N>; // forward tables: Q x N
+    const T* __restrict__ PF = p.P;
+    const T* __restrict__ DF = p.D;
+    const int ns = ncb * N, bstride = ncb * p.sbc;
+    for (int sl = threadIdx.x; sl < ns; sl += blockDim.x)
+    {
+      const int c = sl / N, i0 = sl - c * N;
+      T x[N2];
+      load_slab(su + sl * US, x);
+      T xe[N][E::K2], xo[N][E::K2];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+#pragma unroll
+        for (int k = 0; k < E::K2; ++k)
+        {
+          xe[i1][k] = x[i1 * N + k] + x[i1 * N + N - 1 - k];
+          xo[i1][k] = x[i1 * N + k] - x[i1 * N + N - 1 - k];
+        }
+      T* b0 = sw + c * p.sbc + i0 * p.sq;
+      T* b1 = b0 + bstride;
+      T* b2 = b1 + bstride;
+      // axis 1 of one column: AA, AG, BA
+      auto emit = [&](int q2, const T(&a)[N], const T(&g)[N]) {
+        T o[Q];
+        mv_eo<Q, N, 1>(PF, a, o);
+#pragma unroll
+        for (int q1 = 0; q1 < Q; ++q1)
+          b0[q1 * Q + q2] = o[q1];
+        if constexpr (kGrad)
+        {
+          mv_eo<Q, N, -1>(DF, a, o);
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+            b1[q1 * Q + q2] = o[q1];
+          mv_eo<Q, N, 1>(PF, g, o);
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+            b2[q1 * Q + q2] = o[q1];
+        }
+      };
+      // even and odd sums of row i1 against row j of an even-odd table
+      auto sums = [&](const T* __restrict__ t, int j, int i1, T& s, T& d) {
+        s = t[j * N + E::E] * xe[i1][0];
+#pragma unroll
+        for (int k = 1; k < E::K2; ++k)
+          s = fma(t[j * N + E::E + k], xe[i1][k], s);
+        if constexpr (E::KM)
+          s = fma(t[j * N + E::C], x[i1 * N + E::K2], s);
+        d = t[j * N + E::O] * xo[i1][0];
+#pragma unroll
+        for (int k = 1; k < E::K2; ++k)
+          d = fma(t[j * N + E::O + k], xo[i1][k], d);
+      };
+#pragma unroll
+      for (int j = 0; j < E::M2; ++j) // column pair (j, Q-1-j)
+      {
+        T a0[N], a1[N], g0[N], g1[N];
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          T s, d;
+          sums(PF, j, i1, s, d);
+          a0[i1] = s + d;
+          a1[i1] = s - d;
+          if constexpr (kGrad)
+          {
+            sums(DF, j, i1, s, d);
+            g0[i1] = s + d;
+            g1[i1] = d - s;
+          }
+        }
+        emit(j, a0, g0);
+        emit(Q - 1 - j, a1, g1);
+      }
+      if constexpr (E::MM) // middle column of odd Q
+      {
+        constexpr int j = E::M2;
+        T a[N], g[N];
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          T s = PF[j * N + E::E] * xe[i1][0];
+#pragma unroll
+          for (int k = 1; k < E::K2; ++k)
+            s = fma(PF[j * N + E::E + k], xe[i1][k], s);
+          if constexpr (E::KM)
+            s = fma(PF[j * N + E::C], x[i1 * N + E::K2], s);
+          a[i1] = s;
+          if constexpr (kGrad)
+          {
+            T d = DF[j * N + E::O] * xo[i1][0];
+#pragma unroll
+            for (int k = 1; k < E::K2; ++k)
+              d = fma(DF[j * N + E::O + k], xo[i1][k], d);
+            g[i1] = d;
+          }
+        }
+        emit(j, a, g);
+      }
+    }
+  }
+
   static __device__ __forceinline__ void forward(const TabView<T>& p,
                                                  const ST* __restrict__ su,
                                                  T* __restrict__ sw, int ncb)
   {
+    if constexpr (EVOD)
+    {
+      forward_eo(p, su, sw, ncb);
+      return;
+    }
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
     const int ns = ncb * N * S, bstride = ncb * p.sbc;
@@ -599,6 +842,9 @@ struct SlabTile
   {
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
+    // backward tables: the even-odd ones, else the forward ones transposed
+    const T* __restrict__ PB = EVOD ? p.PB : p.P;
+    const T* __restrict__ DB = EVOD ? p.DB : p.D;
     const int np = ncb * Q2, bstride = ncb * p.sbc;
     for (int t = threadIdx.x; t < np; t += blockDim.x)
     {
@@ -614,11 +860,11 @@ struct SlabTile
 #pragma unroll
         for (int k = 0; k < N; ++k)
           x[k] = b0[k * sq];
-        mv<Q, N, 1, Q>(P, x, v);
+        fwd<1>(P, x, v);
 #pragma unroll
         for (int q = 0; q < Q; ++q)
           v[q] *= from_storage<T>(dw[q * Q2]);
-        mv<N, Q, BSM, BSK>(P, v, x);
+        bwd<1>(PB, v, x);
 #pragma unroll
         for (int k = 0; k < N; ++k)
           b0[k * sq] = x[k];
@@ -635,21 +881,21 @@ struct SlabTile
           xa[k] = b0[k * sq];
           xg[k] = b1[k * sq];
         }
-        mv<Q, N, 1, Q>(D, xa, fx); // d/dx: Gamma on axis 0
-        mv<Q, N, 1, Q>(P, xg, fy); // d/dy: Gamma was applied on axis 1
+        fwd<-1>(D, xa, fx); // d/dx: Gamma on axis 0
+        fwd<1>(P, xg, fy);  // d/dy: Gamma was applied on axis 1
         if constexpr (OP == OP_HELMHOLTZ)
-          mv<Q, N, 1, Q>(P, xa, fm); // the value u at the points (mass term)
+          fwd<1>(P, xa, fm); // the value u at the points (mass term)
         if constexpr (SEM == SEM_EXACT)
         {
           T xb[N];
 #pragma unroll
           for (int k = 0; k < N; ++k)
             xb[k] = b2[k * sq];
-          mv<Q, N, 1, Q>(P, xb, fz); // d/dz: Gamma was applied on axis 2
+          fwd<1>(P, xb, fz); // d/dz: Gamma was applied on axis 2
         }
         else
         {
-          mv<Q, N, 1, Q>(P, xa, fz); // reference: W_z carries no derivative
+          fwd<1>(P, xa, fz); // reference: W_z carries no derivative
         }
         // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx], read
         // as three 8/16-byte pairs (Helmholtz: a fourth pair holds the mass
@@ -676,24 +922,32 @@ struct SlabTile
         T o[N];
         if constexpr (SEM == SEM_EXACT)
         {
-          mv<N, Q, BSM, BSK>(D, fx, o);
-          if constexpr (OP == OP_HELMHOLTZ)
+          bwd<-1>(DB, fx, o);
+          if constexpr (OP == OP_HELMHOLTZ && EVOD)
+          {
+            T om[N];
+            bwd<1>(PB, fm, om); // Phi_0^T (m u): same chain as x
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+              o[k] += om[k];
+          }
+          else if constexpr (OP == OP_HELMHOLTZ)
             mv_acc<N, Q, BSM, BSK>(P, fm, o); // Phi_0^T (m u): same chain as x
 #pragma unroll
           for (int k = 0; k < N; ++k)
             b0[k * sq] = o[k];
-          mv<N, Q, BSM, BSK>(P, fy, o);
+          bwd<1>(PB, fy, o);
 #pragma unroll
           for (int k = 0; k < N; ++k)
             b1[k * sq] = o[k];
-          mv<N, Q, BSM, BSK>(P, fz, o);
+          bwd<1>(PB, fz, o);
 #pragma unroll
           for (int k = 0; k < N; ++k)
             b2[k * sq] = o[k];
         }
         else
         {
-          mv<N, Q, BSM, BSK>(P, fz, o); // (Phi, Phi, Gamma): axis 0 is Phi
+          bwd<1>(PB, fz, o); // (Phi, Phi, Gamma): axis 0 is Phi
 #pragma unroll
           for (int k = 0; k < N; ++k)
             b0[k * sq] = o[k];
@@ -702,10 +956,132 @@ struct SlabTile
     }
   }
 
+  // Even-odd backward: axis 1 back per column with mv_eo; axis 2 back over
+  // the column pairs (j, Q-1-j) into accumulators of the output pairs
+  // (i2, N-1-i2): A = s_Phi + d_Gamma, B = d_Phi + s_Gamma, then
+  // y(i2) = A + B and y(N-1-i2) = A - B (see mv_eo for s and d).
+  static __device__ __forceinline__ void backward_eo(const TabView<T>& p,
+                                                     const T* __restrict__ sw,
+                                                     ST* __restrict__ sy, int ncb)
+  {
+    using E = EO<N, Q>; // backward tables: N x Q
+    const T* __restrict__ PB = p.PB;
+    const T* __restrict__ DB = p.DB;
+    const int ns = ncb * N, bstride = ncb * p.sbc;
+    for (int sl = threadIdx.x; sl < ns; sl += blockDim.x)
+    {
+      const int c = sl / N, i0 = sl - c * N;
+      const T* b0 = sw + c * p.sbc + i0 * p.sq;
+      const T* b1 = b0 + bstride;
+      const T* b2 = b1 + bstride;
+      T A[N][E::M2 > 0 ? E::M2 : 1], B[N][E::M2 > 0 ? E::M2 : 1], Mid[N];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+      {
+#pragma unroll
+        for (int i2 = 0; i2 < E::M2; ++i2)
+          A[i1][i2] = B[i1][i2] = T(0);
+        Mid[i1] = T(0);
+      }
+      // axis 1 back of column q2: u1 = Phi^T X (+ Gamma^T Y), u2 = Phi^T Z
+      auto column = [&](int q2, T(&u1)[N], T(&u2)[N]) {
+        T X[Q];
+#pragma unroll
+        for (int q1 = 0; q1 < Q; ++q1)
+          X[q1] = b0[q1 * Q + q2];
+        mv_eo<N, Q, 1>(PB, X, u1);
+        if constexpr (kGrad)
+        {
+          T Y[Q], Z[Q], t[N];
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+          {
+            Y[q1] = b1[q1 * Q + q2];
+            Z[q1] = b2[q1 * Q + q2];
+          }
+          mv_eo<N, Q, -1>(DB, Y, t);
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            u1[i] += t[i];
+          mv_eo<N, Q, 1>(PB, Z, u2);
+        }
+      };
+#pragma unroll
+      for (int j = 0; j < E::K2; ++j) // column pair (j, Q-1-j)
+      {
+        T u1a[N], u2a[N], u1b[N], u2b[N];
+        column(j, u1a, u2a);
+        column(Q - 1 - j, u1b, u2b);
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          const T e1 = u1a[i1] + u1b[i1], o1 = u1a[i1] - u1b[i1];
+#pragma unroll
+          for (int i2 = 0; i2 < E::M2; ++i2)
+          {
+            A[i1][i2] = fma(PB[i2 * Q + E::E + j], e1, A[i1][i2]);
+            B[i1][i2] = fma(PB[i2 * Q + E::O + j], o1, B[i1][i2]);
+          }
+          if constexpr (E::MM)
+            Mid[i1] = fma(PB[E::M2 * Q + E::E + j], e1, Mid[i1]);
+          if constexpr (kGrad)
+          {
+            const T e2 = u2a[i1] + u2b[i1], o2 = u2a[i1] - u2b[i1];
+#pragma unroll
+            for (int i2 = 0; i2 < E::M2; ++i2)
+            {
+              A[i1][i2] = fma(DB[i2 * Q + E::O + j], o2, A[i1][i2]); // d_Gamma
+              B[i1][i2] = fma(DB[i2 * Q + E::E + j], e2, B[i1][i2]); // s_Gamma
+            }
+            if constexpr (E::MM)
+              Mid[i1] = fma(DB[E::M2 * Q + E::O + j], o2, Mid[i1]);
+          }
+        }
+      }
+      if constexpr (E::KM) // middle column of odd Q: the C entries
+      {
+        T u1[N], u2[N];
+        column(E::K2, u1, u2);
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+#pragma unroll
+          for (int i2 = 0; i2 < E::M2; ++i2)
+          {
+            A[i1][i2] = fma(PB[i2 * Q + E::C], u1[i1], A[i1][i2]); // s_Phi
+            if constexpr (kGrad)
+              B[i1][i2] = fma(DB[i2 * Q + E::C], u2[i1], B[i1][i2]); // s_Gamma
+          }
+          if constexpr (E::MM) // Gamma^T vanishes at the centre
+            Mid[i1] = fma(PB[E::M2 * Q + E::C], u1[i1], Mid[i1]);
+        }
+      }
+      T y[N2];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+      {
+#pragma unroll
+        for (int i2 = 0; i2 < E::M2; ++i2)
+        {
+          y[i1 * N + i2] = A[i1][i2] + B[i1][i2];
+          y[i1 * N + N - 1 - i2] = A[i1][i2] - B[i1][i2];
+        }
+        if constexpr (E::MM)
+          y[i1 * N + E::M2] = Mid[i1];
+      }
+      store_slab(sy + sl * US, y);
+    }
+  }
+
   static __device__ __forceinline__ void backward(const TabView<T>& p,
                                                   const T* __restrict__ sw,
                                                   ST* __restrict__ sy, int ncb)
   {
+    if constexpr (EVOD)
+    {
+      backward_eo(p, sw, sy, ncb);
+      return;
+    }
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
     // every lane of a warp takes part in the shuffle reduction, so the loop
@@ -820,11 +1196,11 @@ struct SlabTile
   }
 };
 
-template <typename T, int N, int Q, int OP, int SEM, int LANES>
+template <typename T, int N, int Q, int OP, int SEM, int LANES, bool EVOD = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  stream_tiles<T, SlabTile<T, N, Q, OP, SEM, LANES>, N, Q, geo_nc(OP)>(p);
+  stream_tiles<T, SlabTile<T, N, Q, OP, SEM, LANES, EVOD>, N, Q, geo_nc(OP)>(p);
 }
 
 } // namespace femtc

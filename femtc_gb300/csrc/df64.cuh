@@ -78,6 +78,10 @@ __device__ __forceinline__ df64 operator+(df64 a, df64 b)
   return df64(hi, lo);
 }
 
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.h, -a.l); }
+
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b)
 {
   a = a + b;

@@ -62,6 +62,12 @@ Registry& registry()
     register_cell_f32_stiffness_l1(r.cells, r.faults);
     register_cell_f32_stiffness_l2(r.cells, r.faults);
     register_cell_f32_helmholtz(r.cells, r.faults);
+    register_cell_f64eo_mass(r.cells, r.faults);
+    register_cell_f64eo_stiffness(r.cells, r.faults);
+    register_cell_f32eo_mass(r.cells, r.faults);
+    register_cell_f32eo_stiffness(r.cells, r.faults);
+    register_cell_f64eeo_mass(r.cells, r.faults);
+    register_cell_f64eeo_stiffness(r.cells, r.faults);
     register_cell_f64e_mass(r.cells, r.faults);
     register_cell_f64e_stiffness(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);
@@ -73,15 +79,63 @@ Registry& registry()
 }
 
 // The compiled variant of (op, dtype, semantics, n, q) with `lanes` lanes
-// per slab (lanes <= 0: any).
+// per slab (lanes <= 0: any); eo selects the even-odd twin.
 const CellVariant* find_cell(int op, int dtype, int sem, int n, int q,
-                             int lanes = 0)
+                             int lanes = 0, int eo = 0)
 {
   for (const CellVariant& v : registry().cells)
     if (v.op == op && v.dtype == dtype && v.sem == sem && v.n == n &&
-        v.q == q && (lanes <= 0 || v.lanes == lanes))
+        v.q == q && (lanes <= 0 || v.lanes == lanes) && v.eo == eo)
       return &v;
   return nullptr;
+}
+
+// Even-odd contractions where a twin is compiled and the tables have the
+// GLL-to-Gauss symmetry (femtc_set_even_odd switches this off).
+std::atomic<int> g_even_odd{1};
+
+// Phi(Q-1-q, N-1-i) = Phi(q,i) and Gamma(Q-1-q, N-1-i) = -Gamma(q,i) to
+// 1e-12 of the largest entry for FP64 tables (the tabulated ones hold to
+// ~4e-14), a few units in the last place for FP32 tables (the tabulated ones
+// rounded to FP32 are exactly symmetric).
+template <typename S>
+bool centro_symmetric(const S* tab, int n, int q, int ntab)
+{
+  const double tol = sizeof(S) == 8 ? 1e-12 : 5e-7;
+  for (int t = 0; t < ntab; ++t)
+  {
+    const S* a = tab + t * n * q;
+    const double sig = t == 0 ? 1.0 : -1.0;
+    double amax = 0.0, dev = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < q; ++k)
+      {
+        const double x = (double)a[k + i * q];
+        const double y = (double)a[(q - 1 - k) + (n - 1 - i) * q];
+        amax = std::max(amax, std::fabs(x));
+        dev = std::max(dev, std::fabs(y - sig * x));
+      }
+    if (!(dev <= tol * amax))
+      return false;
+  }
+  return true;
+}
+
+// The variant that runs a launch of v with these tables: v's even-odd twin
+// when there is one and the tables allow it.
+const CellVariant& launch_form(const CellVariant& v, const void* tables)
+{
+  if (v.eo || !g_even_odd.load(std::memory_order_relaxed) || v.dtype == FEMTC_F16X2 ||
+      v.dtype == FEMTC_BF16X3 || v.sem != FEMTC_EXACT || v.lanes != 1)
+    return v;
+  const CellVariant* t = find_cell(v.op, v.dtype, v.sem, v.n, v.q, 1, 1);
+  if (!t)
+    return v;
+  const int ntab = v.op == FEMTC_OP_MASS ? 1 : 2;
+  const bool sym = v.dtype == FEMTC_F32
+                       ? centro_symmetric(static_cast<const float*>(tables), v.n, v.q, ntab)
+                       : centro_symmetric(static_cast<const double*>(tables), v.n, v.q, ntab);
+  return sym ? *t : v;
 }
 
 // Built-in choice of lanes per slab where both are compiled (FP32): two
@@ -457,9 +511,28 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
   p.sbc = cfg.sbc;
   p.host_io = host_io;
   const int ntab = (v.op != FEMTC_OP_MASS) ? 2 : 1;
-  for (int t = 0; t < ntab; ++t)
-    for (int i = 0; i < v.n * v.q; ++i)
-      p.tab[t][i] = param_value<T>(tables[t * v.n * v.q + i]);
+  if (v.eo)
+  {
+    // even-odd tables: Phi, Gamma forward (Q x N), Phi^T, Gamma^T (N x Q),
+    // formed in the storage precision, then in the launch's form
+    for (int t = 0; t < ntab; ++t)
+    {
+      const ST* a = tables + t * v.n * v.q;
+      const int sig = t == 0 ? 1 : -1;
+      ST f[kMaxQ * kMaxN], b[kMaxQ * kMaxN];
+      host_eo_table<ST>(a, v.q, v.n, 1, v.q, sig, f);
+      host_eo_table<ST>(a, v.n, v.q, v.q, 1, sig, b);
+      for (int i = 0; i < v.n * v.q; ++i)
+      {
+        p.tab[t][i] = param_value<T>(f[i]);
+        p.tab[2 + t][i] = param_value<T>(b[i]);
+      }
+    }
+  }
+  else
+    for (int t = 0; t < ntab; ++t)
+      for (int i = 0; i < v.n * v.q; ++i)
+        p.tab[t][i] = param_value<T>(tables[t * v.n * v.q + i]);
   const unsigned smem = smem_of(v, cfg);
   int blocks = 0;
   int rc = prepare(v.fn, smem, cfg.nt, &blocks);
@@ -477,11 +550,13 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
   return FEMTC_OK;
 }
 
-int launch_variant(const CellVariant& v, const TileCfg& cfg,
+int launch_variant(const CellVariant& v0, const TileCfg& cfg,
                    const void* tables, const void* u, void* y,
                    const void* geo, size_t ncells, cudaStream_t st,
                    int host_io = 0)
 {
+  // the even-odd twin shares the tile shape (same buffers and layout)
+  const CellVariant& v = launch_form(v0, tables);
   if (v.dtype == FEMTC_F64)
     return launch_cell<double>(v, cfg, static_cast<const double*>(tables), u,
                                y, geo, ncells, st, host_io);
@@ -561,9 +636,23 @@ int host_buffer(int i, size_t bytes)
   return FEMTC_OK;
 }
 
-// Preferred transfer mode of the host path per variant, measured by
-// femtc_autotune_host: 0 zero-copy, 1 staging pipeline.
-std::map<Key, int> g_host_pref;
+// Preferred transfer mode of the host path per variant and size class
+// (cells, by powers of four), measured by femtc_autotune_host: 0 zero-copy,
+// 1 staging pipeline.  Small calls favour zero-copy (no pipeline start-up),
+// large ones the staging pipeline (copies in both directions overlap).
+using HostKey = std::pair<Key, int>;
+std::map<HostKey, int> g_host_pref;
+
+int size_class(size_t ncells)
+{
+  int c = 0;
+  while (ncells >= 4)
+  {
+    ncells /= 4;
+    ++c;
+  }
+  return c;
+}
 
 int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
                       const void* tables, const void* u, void* y,
@@ -578,7 +667,7 @@ int apply_host(int op, int dtype, int sem, int degree, int nquad,
   if (mode == 0)
   {
     std::lock_guard<std::mutex> lk2(g_cfg_mutex);
-    auto it = g_host_pref.find(Key(op, dtype, sem, degree + 1, nquad));
+    auto it = g_host_pref.find(HostKey(Key(op, dtype, sem, degree + 1, nquad), size_class(ncells)));
     if (it != g_host_pref.end() && it->second == 1)
       mode = 1;
   }
@@ -797,6 +886,13 @@ void gll_nodes(int p, double* x)
 
 int aux_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 
+// FP32 tables with the GLL-to-Gauss symmetry, and even-odd kernels enabled
+// (the batch's choice of its even-odd family).
+bool even_odd_tables_f32(const float* tab, int n, int q, int ntab)
+{
+  return g_even_odd.load(std::memory_order_relaxed) && centro_symmetric(tab, n, q, ntab);
+}
+
 std::pair<int, int> slab_layout_for(int n, int q, int esize, int lanes)
 {
   return slab_layout(n, q, esize, lanes);
@@ -876,6 +972,23 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
                     tables, u, y, G, ncells);
 }
 
+int femtc_set_even_odd(int enable)
+{
+  g_even_odd.store(enable ? 1 : 0);
+  return FEMTC_OK;
+}
+
+int femtc_even_odd_used(int op, int dtype, int semantics, int degree, int nquad,
+                        const void* tables)
+{
+  if (!tables)
+    return fail(FEMTC_ERR_INVALID, "null tables");
+  const auto sel = select_variant(op, dtype, semantics, degree + 1, nquad);
+  if (!sel.first)
+    return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
+  return launch_form(*sel.first, tables).eo;
+}
+
 int femtc_set_host_path(int mode)
 {
   if (mode < 0 || mode > 2)
@@ -944,24 +1057,31 @@ int femtc_autotune_host(int op, int dtype, int semantics, int degree,
   if (rc != FEMTC_OK)
     return rc;
   // then the transfer mode: whole calls (copies, kernels, synchronisation)
-  // of the zero-copy path and of the staging pipeline, wall clock
-  double best_call[2] = {0, 0};
-  for (int mode = 0; mode <= 1; ++mode)
+  // of the zero-copy path and of the staging pipeline, wall clock, the two
+  // modes alternating; the best call of each counts
+  double best_call[2] = {1e30, 1e30};
+  for (int mode = 0; mode <= 1; ++mode) // warm both
   {
     rc = apply_host_locked(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells,
-                           mode == 0 ? 2 : 1); // warm
+                           mode == 0 ? 2 : 1);
     if (rc != FEMTC_OK)
       return rc;
-    const auto t0 = std::chrono::steady_clock::now();
-    for (int r = 0; r < 3; ++r)
-      apply_host_locked(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells,
-                        mode == 0 ? 2 : 1);
-    best_call[mode] =
-        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
+  for (int r = 0; r < 4; ++r)
+    for (int mode = 0; mode <= 1; ++mode)
+    {
+      const auto t0 = std::chrono::steady_clock::now();
+      rc = apply_host_locked(op, dtype, semantics, degree, nquad, tables, u, y, geo, ncells,
+                             mode == 0 ? 2 : 1);
+      if (rc != FEMTC_OK)
+        return rc;
+      best_call[mode] = std::min(
+          best_call[mode],
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    }
   {
     std::lock_guard<std::mutex> lk2(g_cfg_mutex);
-    g_host_pref[Key(op, dtype, semantics, degree + 1, nquad)] =
+    g_host_pref[HostKey(Key(op, dtype, semantics, degree + 1, nquad), size_class(ncells))] =
         best_call[1] < best_call[0] ? 1 : 0;
   }
   return FEMTC_OK;

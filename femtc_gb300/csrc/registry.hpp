@@ -21,6 +21,7 @@ struct CellVariant
   int slab;    // 1: slab-merged CUDA-core kernel (uses sq, sbc)
   int esize;   // bytes per stored value
   int lanes;   // slab kernels: lanes sharing one slab
+  int eo = 0;  // 1: even-odd contractions (tables with the GLL-to-Gauss symmetry)
 };
 
 using FaultReader = unsigned (*)(); // returns and clears the unit's fault word
@@ -32,6 +33,12 @@ void register_cell_f32_mass_l2(std::vector<CellVariant>&, std::vector<FaultReade
 void register_cell_f32_stiffness_l1(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32_stiffness_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32_helmholtz(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64eo_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64eo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32eo_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f32eo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64eeo_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64eeo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_f16x2_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);

@@ -136,6 +136,22 @@ int femtc_stiffness_apply_host(int dtype, int semantics, int degree,
                                int nquad, const void* tables, const void* u,
                                void* y, const void* G, size_t ncells);
 
+/* Even-odd contractions (default on).  FP64, FP32 and double-float (F64E)
+ * launches with exact semantics and one lane per slab
+ * whose tables have the symmetry of Lagrange bases on symmetric nodes at
+ * symmetric points -- Phi(Q-1-q, N-1-i) = Phi(q,i) and
+ * Gamma(Q-1-q, N-1-i) = -Gamma(q,i) to 1e-12 of the largest entry, as
+ * femtc_tabulate's tables have -- run kernels that split every 1D
+ * contraction into even and odd halves (about 30-45% fewer arithmetic
+ * operations).  Other tables run the plain kernels.  0 forces the plain
+ * kernels.  No reference counterpart. */
+int femtc_set_even_odd(int enable);
+/* 1 when a launch of (op, dtype, semantics, degree, nquad) with these host
+ * tables would run the even-odd kernels, 0 the plain ones; negative status
+ * on bad arguments. */
+int femtc_even_odd_used(int op, int dtype, int semantics, int degree, int nquad,
+                        const void* tables);
+
 /* How the host-buffer entry points move data.  0 (default): when u, y and
  * the geometry are all pinned host memory (cudaHostAlloc /
  * cudaHostRegister), the kernel reads u and the geometry and writes y
@@ -173,8 +189,10 @@ int femtc_autotune(int op, int dtype, int semantics, int degree, int nquad,
 /* The same for the host-buffer path: u, y and geo are pinned host buffers.
  * Tile shapes are timed with the kernels reading and writing them over the
  * host link (zero-copy); then whole calls of the zero-copy path and of the
- * staging-copy pipeline are timed, and host-path mode 0 (auto) uses the
- * faster of the two for this variant from then on. */
+ * staging-copy pipeline are timed (alternating, best call of each), and
+ * host-path mode 0 (auto) uses the faster of the two from then on for this
+ * variant and calls of a similar size (cell counts within the same power
+ * of four). */
 int femtc_autotune_host(int op, int dtype, int semantics, int degree,
                         int nquad, const void* tables, const void* u, void* y,
                         const void* geo, size_t ncells, int* cb,

@@ -108,3 +108,22 @@ def test_helmholtz_supported_and_rejected(femtc):
     assert lib.femtc_helmholtz_apply(femtc.F32, 3, 4, t.ctypes.data, None, 16, 16, 1, None) == -1
     assert lib.femtc_helmholtz_geometry(0, 1.0, 16, 1.0, 16, 16, 1, None) == -1
     assert lib.femtc_helmholtz_geometry(4, 1.0, 16, 1.0, 16, 24, 1, None) == -1  # misaligned
+
+
+def test_even_odd_selection(femtc):
+    """Host-side choice of the even-odd kernels: FP64 exact with the
+    tabulated (symmetric) tables, not with random tables, not for FP32, not
+    when switched off, not for stiffness N = 8 (the plain form there)."""
+    t4 = femtc.tabulate(4, 6)[0]
+    assert femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, t4)
+    assert femtc.even_odd_used(femtc.MASS, femtc.F64, femtc.EXACT, 7, 9, femtc.tabulate(7, 9)[0])
+    assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 7, 9,
+                                   femtc.tabulate(7, 9)[0])
+    assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F32, femtc.EXACT, 4, 6, t4)
+    rnd = np.random.default_rng(0).uniform(-1, 1, t4.size)
+    assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, rnd)
+    femtc.set_even_odd(False)
+    try:
+        assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, t4)
+    finally:
+        femtc.set_even_odd(True)

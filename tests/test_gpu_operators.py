@@ -227,3 +227,44 @@ def test_double_float_form_vs_oracle(femtc, orc, dev, op, P, dq):
         y = run_gpu(femtc, dev, op, femtc.F64E, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
         ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
         assert relerr(y, ref) <= 1e-12, relerr(y, ref)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f64e"])
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", range(1, 8))
+@pytest.mark.parametrize("dq", [0, 1, 2])
+def test_fp64_even_odd_and_plain_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
+    """FP64 and double-float, exact semantics, tabulated (symmetric)
+    tables: the even-odd kernels (default) and the plain kernels (switched
+    off) both within 1e-12 of the oracle, and within 1e-13 of one another."""
+    from femtc_gb300 import workloads as W
+    dt = femtc.F64 if dtype == "f64" else femtc.F64E
+    Q = P + 1 + dq
+    if not femtc.supported(op, dt, femtc.EXACT, P, Q):
+        pytest.skip("variant not built")
+    w = W.make_custom("eo", op, P, Q, 1001, seed=31 * P + dq + 7 * op)
+    ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
+    y_eo = run_gpu(femtc, dev, op, dt, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+    femtc.set_even_odd(False)
+    try:
+        y_plain = run_gpu(femtc, dev, op, dt, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+    finally:
+        femtc.set_even_odd(True)
+    assert relerr(y_eo, ref) <= 1e-12
+    assert relerr(y_plain, ref) <= 1e-12
+    assert relerr(y_eo, y_plain) <= 1e-13
+
+
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", [2, 4, 6])
+def test_fp64_exact_nonsymmetric_tables(femtc, orc, dev, op, P):
+    """Tables without the symmetry (random) run the plain kernels: still
+    within 1e-12 of the oracle."""
+    from femtc_gb300 import workloads as W
+    Q = P + 2
+    w = W.make_custom("ns", op, P, Q, 333, seed=P + 50 * op)
+    rng = np.random.default_rng(P)
+    tables = rng.uniform(-1.0, 1.0, size=w.tables.shape)
+    ref = oracle_apply(orc, op, orc.EXACT, P, Q, tables, w.u, w.geo)
+    y = run_gpu(femtc, dev, op, femtc.F64, femtc.EXACT, P, Q, tables, w.u, w.geo)
+    assert relerr(y, ref) <= 1e-12

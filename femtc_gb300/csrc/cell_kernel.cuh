@@ -530,6 +530,20 @@ __host__ __device__ constexpr int slab_lanes()
   return sizeof(T) == 4 ? 2 : 1; // FP32: more busy lanes; FP64: pipe-bound
 }
 
+// The share of one tile's work a thread takes in the tile passes: cells
+// [c0, c1) of a tile of ncb cells, work item tid, tid + nthr, ...  The whole
+// CTA ({0, ncb, threadIdx.x, blockDim.x}) or one warp ({its cells, lane,
+// 32}).
+struct Part
+{
+  int ncb, c0, c1, tid, nthr;
+};
+
+__device__ __forceinline__ Part cta_part(int ncb)
+{
+  return Part{ncb, 0, ncb, (int)threadIdx.x, (int)blockDim.x};
+}
+
 // EVOD: even-odd contractions (mv_eo) for tables with the GLL-to-Gauss
 // symmetry; one lane per slab, exact semantics.
 template <typename T, int N, int Q, int OP, int SEM, int LANES = slab_lanes<T>(),
@@ -545,6 +559,12 @@ struct SlabTile
   static constexpr bool kGrad = (OP != OP_MASS);
   static_assert(OP != OP_HELMHOLTZ || SEM == SEM_EXACT, "Helmholtz: exact semantics only");
   static_assert(!EVOD || (SEM == SEM_EXACT && LANES == 1), "even-odd: exact, one lane per slab");
+  // Streaming loop: work split by warps (stream_tiles_warp) where its extra
+  // live state costs no occupancy -- FP32 and N <= 4; the register-heavy
+  // FP64 and double-float tiles of higher degree, bound by their arithmetic
+  // pipes, keep the CTA-wide loop (stream_tiles).  The host's tile model
+  // (lane_efficiency) follows the same rule.
+  static constexpr bool kWarpSplit = sizeof(T) == 4 || N <= 4;
   static constexpr int NBUF =
       (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
@@ -636,13 +656,13 @@ struct SlabTile
   // even and odd parts of the slab's rows.
   static __device__ __forceinline__ void forward_eo(const TabView<T>& p,
                                                     const ST* __restrict__ su,
-                                                    T* __restrict__ sw, int ncb)
+                                                    T* __restrict__ sw, const Part& w)
   {
     using E = EO<Q, N>; // forward tables: Q x N
     const T* __restrict__ PF = p.P;
     const T* __restrict__ DF = p.D;
-    const int ns = ncb * N, bstride = ncb * p.sbc;
-    for (int sl = threadIdx.x; sl < ns; sl += blockDim.x)
+    const int bstride = w.ncb * p.sbc;
+    for (int sl = w.c0 * N + w.tid; sl < w.c1 * N; sl += w.nthr)
     {
       const int c = sl / N, i0 = sl - c * N;
       T x[N2];
@@ -744,14 +764,21 @@ struct SlabTile
                                                  const ST* __restrict__ su,
                                                  T* __restrict__ sw, int ncb)
   {
+    forward(p, su, sw, cta_part(ncb));
+  }
+
+  static __device__ __forceinline__ void forward(const TabView<T>& p,
+                                                 const ST* __restrict__ su,
+                                                 T* __restrict__ sw, const Part& w)
+  {
     if constexpr (EVOD)
     {
-      forward_eo(p, su, sw, ncb);
+      forward_eo(p, su, sw, w);
       return;
     }
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
-    const int ns = ncb * N * S, bstride = ncb * p.sbc;
+    const int bstride = w.ncb * p.sbc;
     // With S lanes per slab the q2 columns of a lane depend on the lane, so
     // their table entries are not compile-time constants: load them into
     // registers once per call (lane_s == threadIdx.x % S for every slab of
@@ -770,7 +797,7 @@ struct SlabTile
           dc[jq][i2] = q2 < Q ? D[q2 + i2 * Q] : T(0);
         }
     }
-    for (int ts = threadIdx.x; ts < ns; ts += blockDim.x)
+    for (int ts = w.c0 * N * S + w.tid; ts < w.c1 * N * S; ts += w.nthr)
     {
       const int sl = ts / S, lane_s = ts - sl * S;
       const int c = sl / N, i0 = sl - c * N;
@@ -840,13 +867,21 @@ struct SlabTile
                                                const ST* __restrict__ geo,
                                                long long geo_cell0)
   {
+    fused(p, sw, cta_part(ncb), geo, geo_cell0);
+  }
+
+  static __device__ __forceinline__ void fused(const TabView<T>& p,
+                                               T* __restrict__ sw, const Part& w,
+                                               const ST* __restrict__ geo,
+                                               long long geo_cell0)
+  {
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
     // backward tables: the even-odd ones, else the forward ones transposed
     const T* __restrict__ PB = EVOD ? p.PB : p.P;
     const T* __restrict__ DB = EVOD ? p.DB : p.D;
-    const int np = ncb * Q2, bstride = ncb * p.sbc;
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
+    const int bstride = w.ncb * p.sbc;
+    for (int t = w.c0 * Q2 + w.tid; t < w.c1 * Q2; t += w.nthr)
     {
       const int c = t / Q2, r = t - c * Q2;
       T* b0 = sw + c * p.sbc + r;
@@ -962,13 +997,13 @@ struct SlabTile
   // y(i2) = A + B and y(N-1-i2) = A - B (see mv_eo for s and d).
   static __device__ __forceinline__ void backward_eo(const TabView<T>& p,
                                                      const T* __restrict__ sw,
-                                                     ST* __restrict__ sy, int ncb)
+                                                     ST* __restrict__ sy, const Part& w)
   {
     using E = EO<N, Q>; // backward tables: N x Q
     const T* __restrict__ PB = p.PB;
     const T* __restrict__ DB = p.DB;
-    const int ns = ncb * N, bstride = ncb * p.sbc;
-    for (int sl = threadIdx.x; sl < ns; sl += blockDim.x)
+    const int bstride = w.ncb * p.sbc;
+    for (int sl = w.c0 * N + w.tid; sl < w.c1 * N; sl += w.nthr)
     {
       const int c = sl / N, i0 = sl - c * N;
       const T* b0 = sw + c * p.sbc + i0 * p.sq;
@@ -1077,17 +1112,25 @@ struct SlabTile
                                                   const T* __restrict__ sw,
                                                   ST* __restrict__ sy, int ncb)
   {
+    backward(p, sw, sy, cta_part(ncb));
+  }
+
+  static __device__ __forceinline__ void backward(const TabView<T>& p,
+                                                  const T* __restrict__ sw,
+                                                  ST* __restrict__ sy, const Part& w)
+  {
     if constexpr (EVOD)
     {
-      backward_eo(p, sw, sy, ncb);
+      backward_eo(p, sw, sy, w);
       return;
     }
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
-    // every lane of a warp takes part in the shuffle reduction, so the loop
-    // runs to a bound that is a multiple of the CTA size
-    const int ns = ncb * N * S, bstride = ncb * p.sbc;
-    const int nsr = (ns + blockDim.x - 1) / blockDim.x * blockDim.x;
+    // every lane of a warp takes part in the shuffle reduction, so all
+    // threads of the part run the same number of rounds
+    const int bstride = w.ncb * p.sbc;
+    const int base = w.c0 * N * S, cnt = (w.c1 - w.c0) * N * S;
+    const int rounds = (cnt + w.nthr - 1) / w.nthr;
     // axis-2 backward table entries of this lane's q2 columns (see forward)
     const T* T2 = (OP == OP_STIFFNESS && SEM == SEM_REFERENCE) ? D : P;
     T tc[PRE ? QS : 1][PRE ? N : 1], ec[PRE ? QS : 1][PRE ? N : 1];
@@ -1104,9 +1147,11 @@ struct SlabTile
           ec[jq][i2] = q2 < Q ? D[i2 * BSM + q2 * BSK] : T(0);
         }
     }
-    for (int ts = threadIdx.x; ts < nsr; ts += blockDim.x)
+    for (int r = 0; r < rounds; ++r)
     {
-      const bool live = ts < ns;
+      const int idx = r * w.nthr + w.tid;
+      const bool live = idx < cnt;
+      const int ts = base + idx;
       const int sl = live ? ts / S : 0, lane_s = ts - (ts / S) * S;
       const int c = sl / N, i0 = sl - c * N;
       const T* b0 = sw + c * p.sbc + i0 * p.sq;
@@ -1196,11 +1241,212 @@ struct SlabTile
   }
 };
 
+// One warp copies n elements between global (or host) memory and shared
+// memory: 16-byte vector accesses when both addresses and n allow, else
+// scalar; unrolled so that several requests are in flight per lane.
+template <typename ST>
+__device__ __forceinline__ void warp_copy(ST* __restrict__ dst, const ST* __restrict__ src, int n,
+                                          int lane)
+{
+  constexpr int W = 16 / sizeof(ST);
+  if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0 &&
+      n % W == 0)
+  {
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+#pragma unroll 4
+    for (int i = lane; i < n / W; i += 32)
+      d4[i] = s4[i];
+  }
+  else
+  {
+#pragma unroll 4
+    for (int i = lane; i < n; i += 32)
+      dst[i] = src[i];
+  }
+}
+
+// One warp moves the DOF slabs of cells [c0, c1) between global memory
+// (cells packed, cell c0 at g) and the shared slots (slab stride US): one
+// contiguous run when the slots are packed (odd N), else slab by slab
+// with 16-byte vectors (even N: a slab is a multiple of 16 bytes).
+template <int N, int US, bool TO_SMEM, typename ST>
+__device__ __forceinline__ void warp_slabs(ST* __restrict__ sm, ST* __restrict__ g, int c0,
+                                           int c1, int lane)
+{
+  constexpr int N2 = N * N, W = 16 / sizeof(ST);
+  if constexpr (US == N2)
+  {
+    if constexpr (TO_SMEM)
+      warp_copy(sm + c0 * N * US, g, (c1 - c0) * N * N2, lane);
+    else
+      warp_copy(g, sm + c0 * N * US, (c1 - c0) * N * N2, lane);
+  }
+  else
+  {
+    static_assert(N2 % W == 0, "padded slots hold whole 16-byte vectors");
+    constexpr int VS = N2 / W; // vectors per slab
+    const int nv = (c1 - c0) * N * VS;
+#pragma unroll 4
+    for (int v = lane; v < nv; v += 32)
+    {
+      const int sl = v / VS, k = v - sl * VS;
+      uint4* a = reinterpret_cast<uint4*>(sm + (c0 * N + sl) * US) + k;
+      uint4* b = reinterpret_cast<uint4*>(g + sl * N2) + k;
+      if constexpr (TO_SMEM)
+        *a = *b;
+      else
+        *b = *a;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Streaming loop of the slab tiles with the work split by warps: each warp
+// owns a block of consecutive cells of every tile (its part) and runs the
+// forward, fused and backward passes on them with warp-level
+// synchronisation only, then writes its cells' outputs with coalesced
+// stores.  The CTA shares the TMA stages, handed over with two mbarriers
+// per stage: `full` (the copy of a tile has landed) and `empty` (every warp
+// has read the stage's DOF and geometry data; warp 0 waits on it before it
+// refills the stage).  Without CTA-wide barriers per tile, warps overlap
+// one another's passes instead of idling until the slowest is done.
+// ---------------------------------------------------------------------------
+template <typename T, typename Tile, int N, int Q, int NC>
+__device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
+{
+  using ST = storage_t<T>;
+  constexpr int N2 = N * N, N3 = N * N * N, Q3NC = Q * Q * Q * NC;
+  constexpr int US = Tile::US;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int cb = p.cb;
+  const bool staged = p.geo_staged != 0;
+  const long long ntiles = (p.ncells + cb - 1) / cb;
+  const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem); // [2]
+  uint64_t* empty = full + 2;                         // [2]
+  auto su = [&](int s) { return reinterpret_cast<ST*>(smem + (s ? L.u1 : L.u0)); };
+  auto sg = [&](int s) { return reinterpret_cast<ST*>(smem + (s ? L.g1 : L.g0)); };
+  ST* sy = reinterpret_cast<ST*>(smem + L.y);
+  T* sw = reinterpret_cast<T*>(smem + L.w);
+  const unsigned bslab = N2 * sizeof(ST);
+  const unsigned bu = (unsigned)cb * N3 * sizeof(ST);
+  const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(ST) : 0u;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const int cw = (cb + nwarps - 1) / nwarps; // cells per warp
+  const int wc0 = min(cb, warp * cw), wc1 = min(cb, wc0 + cw);
+  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3]};
+
+  if (threadIdx.x == 0)
+  {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], nwarps);
+    mbar_init(&empty[1], nwarps);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto is_full = [&](long long t) { return !p.host_io && (t + 1) * cb <= p.ncells; };
+  // warp 0: TMA loads of tile t into stage s (the whole tile)
+  auto issue = [&](long long t, int s) {
+    if (lane == 0)
+    {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&full[s], bu + bg);
+      if (staged)
+        bulk_g2s(sg(s), p.geo + t * cb * Q3NC, bg, &full[s]);
+      if constexpr (!Tile::kSlabCopies)
+        bulk_g2s(su(s), p.u + t * cb * N3, bu, &full[s]);
+    }
+    if constexpr (Tile::kSlabCopies)
+    {
+      __syncwarp();
+      const long long slab0 = t * cb * N;
+      for (int k = lane; k < cb * N; k += 32)
+        bulk_g2s(su(s) + k * US, p.u + (slab0 + k) * N2, bslab, &full[s]);
+    }
+  };
+
+  bool ok = true;
+  long long issued = -1, waited = -1; // iterations whose TMA copy was issued / landed
+  long long tile = blockIdx.x;
+  if (warp == 0 && tile < ntiles && is_full(tile))
+  {
+    issue(tile, 0);
+    issued = 0;
+  }
+  for (int it = 0; tile < ntiles; tile += gridDim.x, ++it)
+  {
+    const int s = it & 1;
+    const long long next = tile + gridDim.x;
+    // warp 0 refills the other stage once every warp has released it
+    if (warp == 0 && next < ntiles && is_full(next))
+    {
+      if (it >= 1)
+        ok = __shfl_sync(0xffffffffu,
+                         (int)mbar_wait(&empty[s ^ 1], (unsigned)((it - 1) >> 1) & 1u), 0) &&
+             ok;
+      if (ok)
+      {
+        issue(next, s ^ 1);
+        issued = it + 1;
+      }
+    }
+    const int ncb = (int)((p.ncells - tile * cb) < cb ? (p.ncells - tile * cb) : cb);
+    const int c0 = min(ncb, wc0), c1 = min(ncb, wc1);
+    if (is_full(tile))
+      ok = __shfl_sync(0xffffffffu, (int)mbar_wait(&full[s], (unsigned)(it >> 1) & 1u), 0) && ok;
+    else
+    {
+      // host-resident or ragged tile: this warp loads its own cells
+      warp_slabs<N, US, true>(su(s), const_cast<ST*>(p.u) + (tile * cb + c0) * N3, c0, c1,
+                              lane);
+      if (staged)
+        warp_copy(sg(s) + c0 * Q3NC, p.geo + (tile * cb + c0) * Q3NC, (c1 - c0) * Q3NC, lane);
+      __syncwarp();
+    }
+    if (is_full(tile) && ok)
+      waited = it;
+    if (!ok)
+    {
+      // a bounded wait ran out: stop (the other warps' waits run out too);
+      // warp 0 first waits, bounded, for the copies it issued
+      if (lane == 0)
+        record_fault(FAULT_MBAR_TIMEOUT);
+      if (warp == 0)
+        for (long long k = waited + 1; k <= issued; ++k)
+          mbar_wait(&full[k & 1], (unsigned)(k >> 1) & 1u);
+      break;
+    }
+    const Part w{ncb, c0, c1, lane, 32};
+    Tile::forward(tv, su(s), sw, w);
+    __syncwarp();
+    if (staged)
+      Tile::fused(tv, sw, w, sg(s), 0);
+    else
+      Tile::fused(tv, sw, w, p.geo, tile * cb);
+    __syncwarp();
+    if (lane == 0)
+      mbar_arrive(&empty[s]); // this warp is done with stage s's u and geometry
+    Tile::backward(tv, sw, sy, w);
+    __syncwarp();
+    // this warp's outputs: coalesced stores from the output slabs
+    warp_slabs<N, US, false>(sy, p.y + (tile * cb + c0) * N3, c0, c1, lane);
+    __syncwarp();
+  }
+}
+
 template <typename T, int N, int Q, int OP, int SEM, int LANES, bool EVOD = false>
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  stream_tiles<T, SlabTile<T, N, Q, OP, SEM, LANES, EVOD>, N, Q, geo_nc(OP)>(p);
+  using Tile = SlabTile<T, N, Q, OP, SEM, LANES, EVOD>;
+  if constexpr (Tile::kWarpSplit)
+    stream_tiles_warp<T, Tile, N, Q, geo_nc(OP)>(p);
+  else
+    stream_tiles<T, Tile, N, Q, geo_nc(OP)>(p);
 }
 
 } // namespace femtc

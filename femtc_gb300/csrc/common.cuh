@@ -57,6 +57,12 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar,
       : "memory");
 }
 
+// One arrival (no transaction bytes) on an mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Returns false when the phase did not complete within kMbarSpinLimit polls.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
 {

@@ -272,11 +272,18 @@ double lane_efficiency(const CellVariant& v, int cb, int nt)
   int passes;
   if (v.slab)
   {
+    // FP32 and N <= 4: every warp runs its own block of ceil(cb / warps)
+    // cells (the warp-split streaming), so lanes are filled per warp; other
+    // slab kernels spread each pass over the CTA
     passes = 3; // slabs forward, pencils fused, slabs backward
     const double lanes = v.lanes;
-    np[0] = n * cb * lanes; wk[0] = q * n * (n + q) / lanes;
-    np[1] = q * q * cb;     wk[1] = 2 * q * n;
-    np[2] = n * cb * lanes; wk[2] = q * n * (n + q) / lanes;
+    const bool split = v.esize == 4 || v.n <= 4;
+    const double cw = split ? std::ceil((double)cb / (nt / 32)) : cb;
+    np[0] = n * cw * lanes; wk[0] = q * n * (n + q) / lanes;
+    np[1] = q * q * cw;     wk[1] = 2 * q * n;
+    np[2] = n * cw * lanes; wk[2] = q * n * (n + q) / lanes;
+    if (split)
+      nt = 32;
   }
   else
   {

@@ -230,11 +230,15 @@ BatchLayout default_batch_layout(const BatchKernelInfo& fam, int v, int threads,
     fam.bytes(v, l, &bu, &bg, &bw);
     if (128 + 3 * bu + 2 * bg + bw > budget)
       break;
-    // busy lanes of the slab passes and of the pencil pass
-    const double busy[2] = {double(cb * n * lanes), double(cb * q * q)};
+    // busy lanes of the slab passes and of the pencil pass: per warp (its
+    // block of cells) for the CUDA-core families, per CTA for tensor cores
+    const bool split = slab_family(fam.family);
+    const double cells = split ? std::ceil((double)cb / (threads / 32)) : cb;
+    const int width = split ? 32 : threads;
+    const double busy[2] = {cells * n * lanes, cells * q * q};
     double eff = 0.0;
     for (double x : busy)
-      eff += x / (std::ceil(x / threads) * threads);
+      eff += x / (std::ceil(x / width) * width);
     const double score = eff + 1e-4 * cb;
     if (score > best_score)
     {

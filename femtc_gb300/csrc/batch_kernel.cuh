@@ -253,6 +253,54 @@ __device__ __forceinline__ void batch_run_body(const BatchParams<T>& bp,
   __syncthreads();
 }
 
+// The same tile, this warp's part only (the CUDA-core families): its cells
+// [c0, c1) of the tile, warp-level synchronisation, the stage released on
+// `empty` after the fused pass, the outputs written with coalesced stores.
+// Work buffers are spaced by the variant's tile capacity, so a warp's
+// regions stay put from tile to tile of one variant.
+template <typename T, int FAMILY, int N, int OP>
+__device__ __forceinline__ void batch_run_warp_body(const BatchParams<T>& bp,
+                                                    const BatchTile& t, const BatchSmem& sm,
+                                                    int s, uint64_t* empty)
+{
+  using Tl = typename BatchFamily<T, FAMILY>::template Tile<N, OP>;
+  constexpr int Q = N + 1, NC = geo_nc(OP);
+  constexpr int N3 = N * N * N, Q3NC = Q * Q * Q * NC;
+  constexpr int US = Tl::US;
+  const BatchLayout& l = bp.lay[batch_variant(OP, N)];
+  const BatchItem<T>& it = bp.items[t.item];
+  const TabView<T> tv{bp.tabs[N - 2][0], bp.tabs[N - 2][1], l.sq, l.sbc, bp.tabs[N - 2][2],
+                      bp.tabs[N - 2][3]};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int cw = (l.cb + nwarps - 1) / nwarps;
+  const int c0 = min(t.ncb, warp * cw), c1 = min(t.ncb, warp * cw + cw);
+  T* su = reinterpret_cast<T*>(sm.u(s));
+  T* sg = reinterpret_cast<T*>(sm.g(s));
+  T* sy = reinterpret_cast<T*>(sm.y);
+  T* sw = reinterpret_cast<T*>(sm.w);
+  if (!t.full)
+  {
+    warp_slabs<N, US, true>(su, const_cast<T*>(it.u) + (t.cell0 + c0) * N3, c0, c1, lane);
+    if (l.staged)
+      warp_copy(sg + c0 * Q3NC, it.geo + (t.cell0 + c0) * Q3NC, (c1 - c0) * Q3NC, lane);
+    __syncwarp();
+  }
+  const Part w{l.cb, c0, c1, lane, 32};
+  Tl::forward(tv, su, sw, w);
+  __syncwarp();
+  if (l.staged)
+    Tl::fused(tv, sw, w, sg, 0);
+  else
+    Tl::fused(tv, sw, w, it.geo, t.cell0);
+  __syncwarp();
+  if (lane == 0)
+    mbar_arrive(&empty[s]);
+  Tl::backward(tv, sw, sy, w);
+  __syncwarp();
+  warp_slabs<N, US, false>(sy, it.y + (t.cell0 + c0) * N3, c0, c1, lane);
+  __syncwarp();
+}
+
 // Per-variant code is a separate function (one register allocation per
 // variant, the kernel's count the largest) for the plain CUDA-core family,
 // whose tiles need up to 255 registers: one function holding every variant
@@ -289,6 +337,23 @@ __device__ __forceinline__ void batch_issue(const BatchParams<T>& bp, const Batc
 }
 
 template <typename T, int FAMILY, int N, int OP>
+__device__ __noinline__ void batch_run_warp_call(const BatchParams<T>& bp, const BatchTile& t,
+                                                 const BatchSmem& sm, int s, uint64_t* empty)
+{
+  batch_run_warp_body<T, FAMILY, N, OP>(bp, t, sm, s, empty);
+}
+
+template <typename T, int FAMILY, int N, int OP>
+__device__ __forceinline__ void batch_run_warp(const BatchParams<T>& bp, const BatchTile& t,
+                                               const BatchSmem& sm, int s, uint64_t* empty)
+{
+  if constexpr (batch_inline<FAMILY>())
+    batch_run_warp_body<T, FAMILY, N, OP>(bp, t, sm, s, empty);
+  else
+    batch_run_warp_call<T, FAMILY, N, OP>(bp, t, sm, s, empty);
+}
+
+template <typename T, int FAMILY, int N, int OP>
 __device__ __forceinline__ void batch_run(const BatchParams<T>& bp, const BatchTile& t,
                                           const BatchSmem& sm, int s)
 {
@@ -316,6 +381,134 @@ __host__ __device__ constexpr int batch_min_blocks()
   return FAMILY == kFamilySlab ? 1 : 2;
 }
 
+// The CUDA-core families' loop: work split by warps as in
+// stream_tiles_warp (cell_kernel.cuh).  Stages: `full` (TMA landed, parity
+// per stage flips with each copy) and `empty` (every warp released the
+// stage; one phase per iteration).  Where the variant changes from one tile
+// to the next, the warps' regions of the stages and buffers move, so the
+// CTA meets at a barrier there -- an mbarrier with a bounded wait, so that a
+// warp that stopped on a fault cannot hang the others.
+template <typename T, int FAMILY>
+__device__ __forceinline__ void batch_loop_warp(const BatchParams<T>& bp,
+                                                const BatchSmem& sm)
+{
+  uint64_t* full = sm.bar;      // [2]
+  uint64_t* empty = sm.bar + 2; // [2]
+  uint64_t* vsync = sm.bar + 4; // variant switches
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0)
+  {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], nwarps);
+    mbar_init(&empty[1], nwarps);
+    mbar_init(vsync, nwarps);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto issue = [&](long long k, int s) {
+    const BatchTile t = bp.tiles[k];
+    switch (t.variant)
+    {
+#define X(NN, OPP)                                                             \
+  case batch_variant(OPP, NN):                                                 \
+    batch_issue<T, FAMILY, NN, OPP>(bp, t, sm, s);                             \
+    break;
+      FEMTC_BATCH_CASES(X)
+#undef X
+    default:
+      break;
+    }
+  };
+  auto tma_tile = [&](long long k) {
+    if (k >= bp.ntiles)
+      return false;
+    const BatchTile t = bp.tiles[k];
+    return t.item >= 0 && t.full != 0;
+  };
+
+  bool ok = true;
+  unsigned ph[2] = {0u, 0u}; // parity of the next `full` wait per stage
+  unsigned vph = 0u;         // parity of the next variant-switch wait
+  long long pend[2] = {-1, -1}; // per stage: a copy issued and not yet waited for
+  int prev_variant = -1;
+  long long k = blockIdx.x;
+  if (warp == 0 && tma_tile(k))
+  {
+    issue(k, 0);
+    pend[0] = k;
+  }
+  for (int it = 0; k < bp.ntiles; k += gridDim.x, ++it)
+  {
+    const int s = it & 1;
+    const long long next = k + gridDim.x;
+    if (warp == 0 && tma_tile(next))
+    {
+      if (it >= 1)
+        ok = __shfl_sync(0xffffffffu,
+                         (int)mbar_wait(&empty[s ^ 1], (unsigned)((it - 1) >> 1) & 1u), 0) &&
+             ok;
+      if (ok)
+      {
+        issue(next, s ^ 1);
+        pend[s ^ 1] = next;
+      }
+    }
+    const BatchTile t = bp.tiles[k];
+    if (t.item < 0)
+    {
+      if (lane == 0)
+        mbar_arrive(&empty[s]); // padding: keeps one `empty` phase per iteration
+      continue;
+    }
+    if (t.variant != prev_variant)
+    {
+      if (prev_variant >= 0)
+      {
+        if (lane == 0)
+          mbar_arrive(vsync);
+        ok = __shfl_sync(0xffffffffu, (int)mbar_wait(vsync, vph), 0) && ok;
+        vph ^= 1u;
+      }
+      prev_variant = t.variant;
+    }
+    if (t.full)
+    {
+      ok = __shfl_sync(0xffffffffu, (int)mbar_wait(&full[s], ph[s]), 0) && ok;
+      ph[s] ^= 1u;
+      if (ok)
+        pend[s] = -1;
+    }
+    if (!ok)
+    {
+      if (lane == 0)
+        record_fault(FAULT_MBAR_TIMEOUT);
+      if (warp == 0) // bounded waits for copies still in flight into the stages
+        for (int q = 0; q < 2; ++q)
+          if (pend[q] >= 0)
+            mbar_wait(&full[q], ph[q]);
+      break;
+    }
+    switch (t.variant)
+    {
+#define X(NN, OPP)                                                             \
+  case batch_variant(OPP, NN):                                                 \
+    batch_run_warp<T, FAMILY, NN, OPP>(bp, t, sm, s, empty);                   \
+    break;
+      FEMTC_BATCH_CASES(X)
+#undef X
+    default:
+      if (threadIdx.x == 0)
+        record_fault(FAULT_BAD_DESCRIPTOR);
+      if (lane == 0)
+        mbar_arrive(&empty[s]);
+      break;
+    }
+  }
+}
+
 template <typename T, int FAMILY>
 __global__ void __launch_bounds__(kCellThreads, batch_min_blocks<FAMILY>())
     batch_kernel(const __grid_constant__ BatchParams<T> bp)
@@ -329,6 +522,11 @@ __global__ void __launch_bounds__(kCellThreads, batch_min_blocks<FAMILY>())
   sm.g1 = sm.u1 + bp.stage_u;
   sm.y = sm.g1 + bp.stage_g;
   sm.w = sm.y + bp.stage_y;
+  if constexpr (slab_family(FAMILY))
+  {
+    batch_loop_warp<T, FAMILY>(bp, sm);
+    return;
+  }
   if (threadIdx.x == 0)
   {
     mbar_init(&sm.bar[0], 1);

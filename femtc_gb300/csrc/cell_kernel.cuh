@@ -531,9 +531,12 @@ __host__ __device__ constexpr int slab_lanes()
 }
 
 // The share of one tile's work a thread takes in the tile passes: cells
-// [c0, c1) of a tile of ncb cells, work item tid, tid + nthr, ...  The whole
-// CTA ({0, ncb, threadIdx.x, blockDim.x}) or one warp ({its cells, lane,
-// 32}).
+// [c0, c1) of a tile, work item tid, tid + nthr, ...  The whole CTA
+// ({ncb, 0, ncb, threadIdx.x, blockDim.x}) or one warp ({cb, its cells,
+// lane, 32}).  ncb sets the spacing of the work buffers (ncb cells each):
+// warps that run ahead of one another use the stage's capacity cb there, so
+// that a warp's regions stay the same from tile to tile (a ragged tile's
+// smaller spacing would move them onto cells another warp still reads).
 struct Part
 {
   int ncb, c0, c1, tid, nthr;
@@ -1420,7 +1423,7 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
           mbar_wait(&full[k & 1], (unsigned)(k >> 1) & 1u);
       break;
     }
-    const Part w{ncb, c0, c1, lane, 32};
+    const Part w{cb, c0, c1, lane, 32};
     Tile::forward(tv, su(s), sw, w);
     __syncwarp();
     if (staged)

@@ -121,7 +121,7 @@ def bytes_per_cell(op: int, n: int, q: int, es: int) -> float:
 
 # DRAM bytes (read + write) of one launch of the headline kernel, measured
 # by ncu on the full workload (profiles/stiffness_p4_32k_cells_slab_kernels.md)
-MEASURED_TRAFFIC = {("stiffness_p4", 32768, 0): 399.3e6, ("stiffness_p4", 32768, 1): 196.4e6}
+MEASURED_TRAFFIC = {("stiffness_p4", 32768, 0): 399.7e6, ("stiffness_p4", 32768, 1): 196.7e6}
 
 
 def traffic_for(workload, ncells, dtype):

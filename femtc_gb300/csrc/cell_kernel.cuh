@@ -154,16 +154,21 @@ struct Shape
 struct CellLayout
 {
   unsigned u0, g0, u1, g1, y, w, total;
-  __host__ __device__ CellLayout(unsigned bu, unsigned bg, unsigned bw)
+  unsigned stage; // bytes of one (DOF slab, geometry slab) stage
+  // ns stages (2 for the CTA-wide loop, more for the warp-split one)
+  __host__ __device__ CellLayout(unsigned bu, unsigned bg, unsigned bw, int ns = 2)
   {
-    u0 = 128; // the two mbarriers live in the first 128 bytes
+    stage = bu + bg;
+    u0 = 128; // the mbarriers live in the first 128 bytes
     g0 = u0 + bu;
-    u1 = g0 + bg;
+    u1 = u0 + stage;
     g1 = u1 + bu;
-    y = g1 + bg;
+    y = u0 + (unsigned)ns * stage;
     w = y + bu;
     total = w + ((bw + 15u) & ~15u);
   }
+  __host__ __device__ unsigned u(int s) const { return u0 + (unsigned)s * stage; }
+  __host__ __device__ unsigned g(int s) const { return g0 + (unsigned)s * stage; }
 };
 
 // Shared-memory stride (elements) of one i0 slab (N*N values) of the DOF and
@@ -332,7 +337,7 @@ __host__ __device__ inline CellLayout tile_layout(const CellParams<T>& p)
   const unsigned bu = (unsigned)p.cb * N * Tile::US * sizeof(ST);
   const unsigned bg =
       p.geo_staged ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(ST) : 0u;
-  return CellLayout(bu, bg, Tile::work_bytes(p));
+  return CellLayout(bu, bg, Tile::work_bytes(p), Tile::kStages);
 }
 
 template <typename T, typename Tile, int N, int Q, int NC>
@@ -345,6 +350,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   const int cb = p.cb;
   const bool staged = p.geo_staged != 0;
   const long long ntiles = (p.ncells + cb - 1) / cb;
+  static_assert(Tile::kStages == 2, "the CTA-wide loop keeps two stages");
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   // stage s buffers (selected arithmetically: no local-memory arrays)
@@ -568,6 +574,10 @@ struct SlabTile
   // pipes, keep the CTA-wide loop (stream_tiles).  The host's tile model
   // (lane_efficiency) follows the same rule.
   static constexpr bool kWarpSplit = sizeof(T) == 4 || N <= 4;
+  // TMA stages.  The warp-split loop takes any count; a third stage (two
+  // tiles in flight ahead of the one computed) measured slower than two:
+  // its shared memory costs more occupancy than the deeper prefetch gains.
+  static constexpr int kStages = 2;
   static constexpr int NBUF =
       (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
@@ -1326,10 +1336,11 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   const bool staged = p.geo_staged != 0;
   const long long ntiles = (p.ncells + cb - 1) / cb;
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem); // [2]
-  uint64_t* empty = full + 2;                         // [2]
-  auto su = [&](int s) { return reinterpret_cast<ST*>(smem + (s ? L.u1 : L.u0)); };
-  auto sg = [&](int s) { return reinterpret_cast<ST*>(smem + (s ? L.g1 : L.g0)); };
+  constexpr int NS = Tile::kStages;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem); // [NS]
+  uint64_t* empty = full + NS;                        // [NS]
+  auto su = [&](int s) { return reinterpret_cast<ST*>(smem + L.u(s)); };
+  auto sg = [&](int s) { return reinterpret_cast<ST*>(smem + L.g(s)); };
   ST* sy = reinterpret_cast<ST*>(smem + L.y);
   T* sw = reinterpret_cast<T*>(smem + L.w);
   const unsigned bslab = N2 * sizeof(ST);
@@ -1343,10 +1354,11 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
 
   if (threadIdx.x == 0)
   {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], nwarps);
-    mbar_init(&empty[1], nwarps);
+    for (int s = 0; s < NS; ++s)
+    {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], nwarps);
+    }
     fence_mbar_init();
   }
   __syncthreads();
@@ -1375,32 +1387,39 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   bool ok = true;
   long long issued = -1, waited = -1; // iterations whose TMA copy was issued / landed
   long long tile = blockIdx.x;
-  if (warp == 0 && tile < ntiles && is_full(tile))
+  // prologue: the first NS-1 tiles of this CTA
+  for (int j = 0; j + 1 < NS; ++j)
   {
-    issue(tile, 0);
-    issued = 0;
+    const long long t = tile + (long long)j * gridDim.x;
+    if (warp == 0 && t < ntiles && is_full(t))
+    {
+      issue(t, j);
+      issued = j;
+    }
   }
   for (int it = 0; tile < ntiles; tile += gridDim.x, ++it)
   {
-    const int s = it & 1;
-    const long long next = tile + gridDim.x;
-    // warp 0 refills the other stage once every warp has released it
-    if (warp == 0 && next < ntiles && is_full(next))
+    const int s = it % NS;
+    const long long ahead = tile + (long long)(NS - 1) * gridDim.x;
+    // warp 0 refills stage (it-1) % NS with the tile NS-1 iterations ahead
+    // once every warp has released it
+    if (warp == 0 && ahead < ntiles && is_full(ahead))
     {
       if (it >= 1)
         ok = __shfl_sync(0xffffffffu,
-                         (int)mbar_wait(&empty[s ^ 1], (unsigned)((it - 1) >> 1) & 1u), 0) &&
+                         (int)mbar_wait(&empty[(it - 1) % NS], (unsigned)((it - 1) / NS) & 1u),
+                         0) &&
              ok;
       if (ok)
       {
-        issue(next, s ^ 1);
-        issued = it + 1;
+        issue(ahead, (it + NS - 1) % NS);
+        issued = it + NS - 1;
       }
     }
     const int ncb = (int)((p.ncells - tile * cb) < cb ? (p.ncells - tile * cb) : cb);
     const int c0 = min(ncb, wc0), c1 = min(ncb, wc1);
     if (is_full(tile))
-      ok = __shfl_sync(0xffffffffu, (int)mbar_wait(&full[s], (unsigned)(it >> 1) & 1u), 0) && ok;
+      ok = __shfl_sync(0xffffffffu, (int)mbar_wait(&full[s], (unsigned)(it / NS) & 1u), 0) && ok;
     else
     {
       // host-resident or ragged tile: this warp loads its own cells
@@ -1420,7 +1439,7 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
         record_fault(FAULT_MBAR_TIMEOUT);
       if (warp == 0)
         for (long long k = waited + 1; k <= issued; ++k)
-          mbar_wait(&full[k & 1], (unsigned)(k >> 1) & 1u);
+          mbar_wait(&full[k % NS], (unsigned)(k / NS) & 1u);
       break;
     }
     const Part w{cb, c0, c1, lane, 32};

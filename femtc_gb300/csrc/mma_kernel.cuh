@@ -393,6 +393,7 @@ __device__ __forceinline__ void contract_pass_shared(
 template <int SPLIT, int N, int Q, int OP>
 struct MmaTile
 {
+  static constexpr int kStages = 2; // the CTA-wide loop (stream_tiles)
   using S = Shape<N, Q, OP, SEM_EXACT>;
   using T = float;
   static constexpr bool kSlabCopies = false;

@@ -287,7 +287,7 @@ double lane_efficiency(const CellVariant& v, int cb, int nt)
   }
   else
   {
-    passes = 5; // 16-pencil MMA blocks per warp
+    passes = 5; // 16-pencil MMA blocks per warp, spread over the CTA
     const double rows[5] = {n * n, n * q, q * q, n * q, n * n};
     for (int i = 0; i < 5; ++i)
     {

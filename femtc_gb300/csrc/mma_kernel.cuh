@@ -63,6 +63,13 @@ struct SplitTraits<SPLIT_F16X2>
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
   }
+  static __device__ __forceinline__ void mma8(float (&d)[4], const uint32_t (&a)[2], uint32_t b0)
+  {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.f16.f16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(b0));
+  }
 };
 
 template <>
@@ -97,6 +104,13 @@ struct SplitTraits<SPLIT_BF16X3>
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
   }
+  static __device__ __forceinline__ void mma8(float (&d)[4], const uint32_t (&a)[2], uint32_t b0)
+  {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(b0));
+  }
 };
 
 // Power-of-two scale that puts max|x| of a row in [2^13, 2^14) (FP16 split);
@@ -111,67 +125,80 @@ __device__ __forceinline__ float row_scale(float m)
   return __int_as_float(se << 23);
 }
 
+// K extent of the MMA instruction for a contraction of K terms: m16n8k8 for
+// K <= 8 (every contraction up to degree 6 at Q <= 8), else m16n8k16.  The
+// k8 form gathers and splits half the A values per thread.
+__host__ __device__ constexpr int kblock(int K) { return K <= 8 ? 8 : 16; }
+
 // A operand of one 16-row block: v[0..1] row g (k=2t,2t+1), v[2..3] row g+8,
-// v[4..5] row g (k=2t+8,2t+9), v[6..7] row g+8 -- the m16n8k16 A layout.
-template <int SPLIT>
+// and for KB = 16 v[4..5] row g (k=2t+8,2t+9), v[6..7] row g+8 -- the
+// m16n8k8 / m16n8k16 A layouts.
+template <int SPLIT, int KB = 16>
 struct AFrag
 {
   using Tr = SplitTraits<SPLIT>;
-  uint32_t r[Tr::terms][4];
+  static constexpr int NV = KB / 2, NR = KB / 4;
+  uint32_t r[Tr::terms][NR];
   float inv0, inv1; // undo the row scales of rows g and g+8
 
-  __device__ __forceinline__ void build(float (&v)[8])
+  __device__ __forceinline__ void build(float (&v)[NV])
   {
     float s0 = 1.0f, s1 = 1.0f;
     if constexpr (Tr::scaled)
     {
-      float m0 = fmaxf(fmaxf(fabsf(v[0]), fabsf(v[1])), fmaxf(fabsf(v[4]), fabsf(v[5])));
-      float m1 = fmaxf(fmaxf(fabsf(v[2]), fabsf(v[3])), fmaxf(fabsf(v[6]), fabsf(v[7])));
+      float m0 = fmaxf(fabsf(v[0]), fabsf(v[1]));
+      float m1 = fmaxf(fabsf(v[2]), fabsf(v[3]));
+      if constexpr (KB == 16)
+      {
+        m0 = fmaxf(m0, fmaxf(fabsf(v[4]), fabsf(v[5])));
+        m1 = fmaxf(m1, fmaxf(fabsf(v[6]), fabsf(v[7])));
+      }
       m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, 1));
       m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, 2));
       m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, 1));
       m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, 2));
       s0 = row_scale(m0);
       s1 = row_scale(m1);
-      v[0] *= s0; v[1] *= s0; v[4] *= s0; v[5] *= s0;
-      v[2] *= s1; v[3] *= s1; v[6] *= s1; v[7] *= s1;
+#pragma unroll
+      for (int i = 0; i < NV; ++i)
+        v[i] *= ((i >> 1) & 1) ? s1 : s0;
     }
     inv0 = 1.0f / s0;
     inv1 = 1.0f / s1;
 #pragma unroll
     for (int j = 0; j < Tr::terms; ++j)
     {
-      float h[8];
+      float h[NV];
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
+      for (int i = 0; i < NV; ++i)
       {
         h[i] = (j + 1 < Tr::terms) ? Tr::round(v[i]) : v[i];
         v[i] -= h[i];
       }
-      r[j][0] = Tr::pack(h[0], h[1]);
-      r[j][1] = Tr::pack(h[2], h[3]);
-      r[j][2] = Tr::pack(h[4], h[5]);
-      r[j][3] = Tr::pack(h[6], h[7]);
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        r[j][q] = Tr::pack(h[2 * q], h[2 * q + 1]);
     }
   }
 };
 
 // B operand of one table orientation and n-tile, split into terms:
 // B[k][n] = tab[n*SN + k*SK] for k < K, n < M (zero elsewhere).
-template <int SPLIT>
+template <int SPLIT, int KB = 16>
 struct BFrag
 {
   using Tr = SplitTraits<SPLIT>;
-  uint32_t r[Tr::terms][2];
+  static constexpr int NV = KB / 4, NR = KB / 8;
+  uint32_t r[Tr::terms][NR];
 
   template <int K, int M, int SN, int SK>
   __device__ __forceinline__ void build(const float* __restrict__ tab, int ntile)
   {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int n = ntile * 8 + g;
-    float v[4];
+    float v[NV];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < NV; ++i)
     {
       const int k = 2 * t + (i & 1) + (i >> 1) * 8;
       v[i] = (k < K && n < M) ? tab[n * SN + k * SK] : 0.0f;
@@ -179,15 +206,16 @@ struct BFrag
 #pragma unroll
     for (int j = 0; j < Tr::terms; ++j)
     {
-      float h[4];
+      float h[NV];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < NV; ++i)
       {
         h[i] = (j + 1 < Tr::terms) ? Tr::round(v[i]) : v[i];
         v[i] -= h[i];
       }
-      r[j][0] = Tr::pack(h[0], h[1]);
-      r[j][1] = Tr::pack(h[2], h[3]);
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        r[j][q] = Tr::pack(h[2 * q], h[2 * q + 1]);
     }
   }
 };
@@ -197,7 +225,8 @@ template <int SPLIT, int K, int M, bool FWD, int Q>
 struct Table
 {
   static constexpr int NT = (M + 7) / 8;
-  BFrag<SPLIT> f[NT];
+  static constexpr int KB = kblock(K);
+  BFrag<SPLIT, KB> f[NT];
   __device__ __forceinline__ void build(const float* __restrict__ tab)
   {
 #pragma unroll
@@ -222,7 +251,7 @@ struct Acc
       d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.0f;
   }
   template <int K, int M, bool FWD, int Q>
-  __device__ __forceinline__ void mma(const AFrag<SPLIT>& a,
+  __device__ __forceinline__ void mma(const AFrag<SPLIT, kblock(K)>& a,
                                       const Table<SPLIT, K, M, FWD, Q>& b)
   {
     using Tr = SplitTraits<SPLIT>;
@@ -230,10 +259,16 @@ struct Acc
     for (int j = 0; j < NT; ++j)
 #pragma unroll
       for (int p = 0; p < Tr::nprod; ++p)
-        Tr::mma(d[j], a.r[Tr::pa(p)], b.f[j].r[Tr::pb(p)][0], b.f[j].r[Tr::pb(p)][1]);
+      {
+        if constexpr (kblock(K) == 16)
+          Tr::mma(d[j], a.r[Tr::pa(p)], b.f[j].r[Tr::pb(p)][0], b.f[j].r[Tr::pb(p)][1]);
+        else
+          Tr::mma8(d[j], a.r[Tr::pa(p)], b.f[j].r[Tr::pb(p)][0]);
+      }
   }
   // undo the A-row scales (rows g and g+8) and add into `o`
-  __device__ __forceinline__ void unscale_into(const AFrag<SPLIT>& a, float (&o)[NT][4]) const
+  template <int KB>
+  __device__ __forceinline__ void unscale_into(const AFrag<SPLIT, KB>& a, float (&o)[NT][4]) const
   {
 #pragma unroll
     for (int j = 0; j < NT; ++j)
@@ -251,14 +286,14 @@ struct Acc
 template <int K, typename Idx>
 __device__ __forceinline__ void gather(const float* __restrict__ src, Idx idx,
                                        int stride, int base, int np,
-                                       float (&v)[8])
+                                       float (&v)[kblock(K) / 2])
 {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int r0 = base + g, r1 = base + g + 8;
   const bool ok0 = r0 < np, ok1 = r1 < np;
   const int b0 = ok0 ? idx(r0) : 0, b1 = ok1 ? idx(r1) : 0;
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < kblock(K) / 2; ++i)
   {
     const int k = 2 * t + (i & 1) + ((i >> 2) & 1) * 8;
     const bool row1 = (i >> 1) & 1;
@@ -312,6 +347,21 @@ __device__ __forceinline__ void zero(float (&o)[NT][4])
     o[j][0] = o[j][1] = o[j][2] = o[j][3] = 0.0f;
 }
 
+// The rows (pencils) of a pass one warp covers: 16-row blocks starting at
+// r0 + b0*16, every bs-th block, below r1.  Whole CTA: {0, np, warp,
+// warps}; one warp of the warp-split loop: {its cells' rows, 0, 1}.
+struct Rows
+{
+  int r0, r1, b0, bs;
+};
+
+__device__ __forceinline__ Rows rows_of(const Part& w, int rows_per_cell)
+{
+  if (w.nthr == 32 && blockDim.x != 32) // one warp's cells
+    return Rows{w.c0 * rows_per_cell, w.c1 * rows_per_cell, 0, 1};
+  return Rows{0, w.c1 * rows_per_cell, (int)(threadIdx.x >> 5), (int)(blockDim.x >> 5)};
+}
+
 // One contraction of a pass with up to two (input, table) terms summed:
 // out = T_a^(dir) in_a [+ T_b^(dir) in_b].
 template <int SPLIT, int K, int M, bool FWD, int Q, bool TWO = false,
@@ -320,18 +370,18 @@ __device__ __forceinline__ void contract_pass(
     const float* __restrict__ in_a, const Table<SPLIT, K, M, FWD, Q>& ta,
     const float* __restrict__ in_b, const Table<SPLIT, K, M, FWD, Q>& tb,
     InIdx iidx, int istride, float* __restrict__ out, OutIdx oidx,
-    int ostride, int np)
+    int ostride, const Rows& rw)
 {
   constexpr int NT = (M + 7) / 8;
-  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int base = warp * 16; base < np; base += nwarps * 16)
+  const int np = rw.r1;
+  for (int base = rw.r0 + rw.b0 * 16; base < np; base += rw.bs * 16)
   {
     float o[NT][4];
     zero(o);
     {
-      float v[8];
+      float v[kblock(K) / 2];
       gather<K>(in_a, iidx, istride, base, np, v);
-      AFrag<SPLIT> a;
+      AFrag<SPLIT, kblock(K)> a;
       a.build(v);
       Acc<SPLIT, NT> acc;
       acc.zero();
@@ -340,9 +390,9 @@ __device__ __forceinline__ void contract_pass(
     }
     if constexpr (TWO)
     {
-      float v[8];
+      float v[kblock(K) / 2];
       gather<K>(in_b, iidx, istride, base, np, v);
-      AFrag<SPLIT> a;
+      AFrag<SPLIT, kblock(K)> a;
       a.build(v);
       Acc<SPLIT, NT> acc;
       acc.zero();
@@ -359,15 +409,16 @@ template <int SPLIT, int K, int M, bool FWD, int Q, typename InIdx, typename Out
 __device__ __forceinline__ void contract_pass_shared(
     const float* __restrict__ in, const Table<SPLIT, K, M, FWD, Q>& ta,
     const Table<SPLIT, K, M, FWD, Q>& tb, InIdx iidx, int istride,
-    float* __restrict__ out_a, float* __restrict__ out_b, OutIdx oidx, int ostride, int np)
+    float* __restrict__ out_a, float* __restrict__ out_b, OutIdx oidx, int ostride,
+    const Rows& rw)
 {
   constexpr int NT = (M + 7) / 8;
-  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int base = warp * 16; base < np; base += nwarps * 16)
+  const int np = rw.r1;
+  for (int base = rw.r0 + rw.b0 * 16; base < np; base += rw.bs * 16)
   {
-    float v[8];
+    float v[kblock(K) / 2];
     gather<K>(in, iidx, istride, base, np, v);
-    AFrag<SPLIT> a;
+    AFrag<SPLIT, kblock(K)> a;
     a.build(v);
     {
       Acc<SPLIT, NT> acc;
@@ -393,7 +444,11 @@ __device__ __forceinline__ void contract_pass_shared(
 template <int SPLIT, int N, int Q, int OP>
 struct MmaTile
 {
-  static constexpr int kStages = 2; // the CTA-wide loop (stream_tiles)
+  static constexpr int kStages = 2;
+  // CTA-wide streaming (stream_tiles).  The passes also run on one warp's
+  // cells (Part/Rows), but the warp-split loop measured 10-20% slower for
+  // these tiles: a warp's own rows fill fewer whole 16-row blocks.
+  static constexpr bool kWarpSplit = false;
   using S = Shape<N, Q, OP, SEM_EXACT>;
   using T = float;
   static constexpr bool kSlabCopies = false;
@@ -404,13 +459,28 @@ struct MmaTile
     return (unsigned)p.cb * S::work * sizeof(float);
   }
 
+  // between passes: the CTA, or one warp for its own cells
+  static __device__ __forceinline__ void sync(const Part& pt)
+  {
+    if (pt.nthr == 32)
+      __syncwarp();
+    else
+      __syncthreads();
+  }
+
   static __device__ __forceinline__ void forward(const TabView<float>& p,
                                                  const float* __restrict__ su,
                                                  float* __restrict__ w, int ncb)
   {
-    pass1(p, su, w, ncb);
-    __syncthreads();
-    pass2(p, w, ncb);
+    forward(p, su, w, cta_part(ncb));
+  }
+  static __device__ __forceinline__ void forward(const TabView<float>& p,
+                                                 const float* __restrict__ su,
+                                                 float* __restrict__ w, const Part& pt)
+  {
+    pass1(p, su, w, pt);
+    sync(pt);
+    pass2(p, w, pt);
   }
 
   static __device__ __forceinline__ void fused(const TabView<float>& p,
@@ -418,26 +488,40 @@ struct MmaTile
                                                const float* __restrict__ geo,
                                                long long geo_cell0)
   {
-    pass3(p, w, ncb, geo, geo_cell0);
-    __syncthreads();
-    pass4(p, w, ncb);
+    fused(p, w, cta_part(ncb), geo, geo_cell0);
+  }
+  static __device__ __forceinline__ void fused(const TabView<float>& p,
+                                               float* __restrict__ w, const Part& pt,
+                                               const float* __restrict__ geo,
+                                               long long geo_cell0)
+  {
+    pass3(p, w, pt, geo, geo_cell0);
+    sync(pt);
+    pass4(p, w, pt);
   }
 
   static __device__ __forceinline__ void backward(const TabView<float>& p,
                                                   const float* __restrict__ w,
                                                   float* __restrict__ sy, int ncb)
   {
-    pass5(p, w, sy, ncb);
+    pass5(p, w, sy, cta_part(ncb));
+  }
+  static __device__ __forceinline__ void backward(const TabView<float>& p,
+                                                  const float* __restrict__ w,
+                                                  float* __restrict__ sy, const Part& pt)
+  {
+    pass5(p, w, sy, pt);
   }
 
   // Pass 1: axis 2, u[c][i0][i1][i2] -> A[c][i0][i1][q2]
   static __device__ __forceinline__ void pass1(const TabView<float>& p,
                                                const float* __restrict__ su,
-                                               float* __restrict__ w, int ncb)
+                                               float* __restrict__ w, const Part& pt)
   {
+    const int ncb = pt.ncb;
     float* A0 = w;
     float* A1 = w + ncb * S::SA;
-    const int np = ncb * N * N;
+    const Rows np = rows_of(pt, N * N);
     auto iidx = [](int r) { const int c = r / (N * N); return c * S::N3 + (r - c * (N * N)) * N; };
     auto oidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
     Table<SPLIT, N, Q, true, Q> phi;
@@ -456,14 +540,15 @@ struct MmaTile
 
   // Pass 2: axis 1, A[c][i0][i1][q2] -> B[c][i0][q1][q2]
   static __device__ __forceinline__ void pass2(const TabView<float>& p,
-                                               float* __restrict__ w, int ncb)
+                                               float* __restrict__ w, const Part& pt)
   {
+    const int ncb = pt.ncb;
     const float* A0 = w;
     const float* A1 = w + ncb * S::SA;
     float* B0 = w + ncb * S::nA * S::SA;
     float* B1 = B0 + ncb * S::SB;
     float* B2 = B1 + ncb * S::SB;
-    const int np = ncb * N * Q;
+    const Rows np = rows_of(pt, N * Q);
     auto iidx = [](int r) {
       const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
       return c * S::SA + i0 * N * S::QP + q2;
@@ -491,23 +576,24 @@ struct MmaTile
   // Pass 3 (fused, registers only between the two MMAs): axis 0 forward,
   // D scaling / G transform, axis 0 backward; in place in B.
   static __device__ __forceinline__ void pass3(const TabView<float>& p,
-                                               float* __restrict__ w, int ncb,
+                                               float* __restrict__ w, const Part& pt,
                                                const float* __restrict__ geo,
                                                long long geo_cell0)
   {
     constexpr int NTQ = (Q + 7) / 8, NTN = (N + 7) / 8;
+    const int ncb = pt.ncb;
     float* B0 = w + ncb * S::nA * S::SA;
     float* B1 = B0 + ncb * S::SB;
     float* B2 = B1 + ncb * S::SB;
-    const int np = ncb * Q * Q;
+    const Rows rw = rows_of(pt, Q * Q);
+    const int np = rw.r1;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     auto bidx = [](int r) { const int c = r / (Q * Q); return c * S::SB + (r - c * (Q * Q)); };
     Table<SPLIT, N, Q, true, Q> fphi;
     Table<SPLIT, Q, N, false, Q> bphi;
     fphi.build(p.P);
     bphi.build(p.P);
-    for (int base = warp * 16; base < np; base += nwarps * 16)
+    for (int base = rw.r0 + rw.b0 * 16; base < np; base += rw.bs * 16)
     {
       const int r0 = base + g, r1 = base + g + 8;
       // geometry offsets of rows r0, r1: point (c, q0, rr) at
@@ -519,9 +605,9 @@ struct MmaTile
       const long long go0 = r0 < np ? gofs(r0) : -1, go1 = r1 < np ? gofs(r1) : -1;
       if constexpr (OP == OP_MASS)
       {
-        float v[8];
+        float v[kblock(N) / 2];
         gather<N>(B0, bidx, Q * Q, base, np, v);
-        AFrag<SPLIT> a;
+        AFrag<SPLIT, kblock(N)> a;
         a.build(v);
         Acc<SPLIT, NTQ> acc;
         acc.zero();
@@ -539,9 +625,9 @@ struct MmaTile
             const long long go = (e < 2) ? go0 : go1;
             f[j][e] = (q0 < Q && go >= 0) ? f[j][e] * geo[go + q0 * Q * Q] : 0.0f;
           }
-        float vb[8];
+        float vb[kblock(Q) / 2];
         to_operand<NTQ>(f, vb);
-        AFrag<SPLIT> ab;
+        AFrag<SPLIT, kblock(Q)> ab;
         ab.build(vb);
         Acc<SPLIT, NTN> accb;
         accb.zero();
@@ -560,9 +646,9 @@ struct MmaTile
         zero(fy);
         zero(fz);
         {
-          float v[8];
+          float v[kblock(N) / 2];
           gather<N>(B0, bidx, Q * Q, base, np, v); // AA -> d/dx: Gamma on axis 0
-          AFrag<SPLIT> a;
+          AFrag<SPLIT, kblock(N)> a;
           a.build(v);
           Acc<SPLIT, NTQ> acc;
           acc.zero();
@@ -570,9 +656,9 @@ struct MmaTile
           acc.unscale_into(a, fx);
         }
         {
-          float v[8];
+          float v[kblock(N) / 2];
           gather<N>(B1, bidx, Q * Q, base, np, v); // AG -> d/dy
-          AFrag<SPLIT> a;
+          AFrag<SPLIT, kblock(N)> a;
           a.build(v);
           Acc<SPLIT, NTQ> acc;
           acc.zero();
@@ -580,9 +666,9 @@ struct MmaTile
           acc.unscale_into(a, fy);
         }
         {
-          float v[8];
+          float v[kblock(N) / 2];
           gather<N>(B2, bidx, Q * Q, base, np, v); // BA -> d/dz
-          AFrag<SPLIT> a;
+          AFrag<SPLIT, kblock(N)> a;
           a.build(v);
           Acc<SPLIT, NTQ> acc;
           acc.zero();
@@ -620,23 +706,26 @@ struct MmaTile
   }
 
   // accumulator fragment (rows g, g+8; cols 2t,2t+1 [+8]) -> A values
-  template <int NTQ>
-  static __device__ __forceinline__ void to_operand(const float (&f)[NTQ][4], float (&v)[8])
+  template <int NTQ, int NV>
+  static __device__ __forceinline__ void to_operand(const float (&f)[NTQ][4], float (&v)[NV])
   {
     v[0] = f[0][0];
     v[1] = f[0][1];
     v[2] = f[0][2];
     v[3] = f[0][3];
-    if constexpr (NTQ > 1)
+    if constexpr (NV == 8)
     {
-      v[4] = f[1][0];
-      v[5] = f[1][1];
-      v[6] = f[1][2];
-      v[7] = f[1][3];
-    }
-    else
-    {
-      v[4] = v[5] = v[6] = v[7] = 0.0f;
+      if constexpr (NTQ > 1)
+      {
+        v[4] = f[1][0];
+        v[5] = f[1][1];
+        v[6] = f[1][2];
+        v[7] = f[1][3];
+      }
+      else
+      {
+        v[4] = v[5] = v[6] = v[7] = 0.0f;
+      }
     }
   }
 
@@ -645,9 +734,9 @@ struct MmaTile
       const float (&f)[NTQ][4], const Table<SPLIT, Q, N, false, Q>& tb,
       float* __restrict__ dst, Idx idx, int base, int np)
   {
-    float v[8];
+    float v[kblock(Q) / 2];
     to_operand<NTQ>(f, v);
-    AFrag<SPLIT> a;
+    AFrag<SPLIT, kblock(Q)> a;
     a.build(v);
     Acc<SPLIT, NTN> acc;
     acc.zero();
@@ -660,14 +749,15 @@ struct MmaTile
 
   // Pass 4: backward axis 1, B[c][i0][q1][q2] -> A[c][i0][i1][q2]
   static __device__ __forceinline__ void pass4(const TabView<float>& p,
-                                               float* __restrict__ w, int ncb)
+                                               float* __restrict__ w, const Part& pt)
   {
+    const int ncb = pt.ncb;
     float* A0 = w;
     float* A1 = w + ncb * S::SA;
     const float* B0 = w + ncb * S::nA * S::SA;
     const float* B1 = B0 + ncb * S::SB;
     const float* B2 = B1 + ncb * S::SB;
-    const int np = ncb * N * Q;
+    const Rows np = rows_of(pt, N * Q);
     auto iidx = [](int r) {
       const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
       return c * S::SB + i0 * Q * Q + q2;
@@ -695,11 +785,12 @@ struct MmaTile
   // Pass 5: backward axis 2, A[c][i0][i1][q2] -> y[c][i0][i1][i2]
   static __device__ __forceinline__ void pass5(const TabView<float>& p,
                                                const float* __restrict__ w,
-                                               float* __restrict__ sy, int ncb)
+                                               float* __restrict__ sy, const Part& pt)
   {
+    const int ncb = pt.ncb;
     const float* A0 = w;
     const float* A1 = w + ncb * S::SA;
-    const int np = ncb * N * N;
+    const Rows np = rows_of(pt, N * N);
     auto iidx = [](int r) { const int c = r / (N * N); return c * S::SA + (r - c * (N * N)) * S::QP; };
     auto oidx = [](int r) { const int c = r / (N * N); return c * S::N3 + (r - c * (N * N)) * N; };
     Table<SPLIT, Q, N, false, Q> phi;

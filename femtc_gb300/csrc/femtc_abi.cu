@@ -598,7 +598,7 @@ size_t elem_size(int dtype)
 // Host-buffer path state: the device it was set up on, a compute stream,
 // copy-in / copy-out streams and chunk events of the staging pipeline, and
 // grow-only device staging buffers.
-constexpr int kHostChunks = 16; // events per pipeline (chunks per call, at most)
+constexpr int kHostChunks = 32; // events per pipeline (chunks per call, at most)
 struct HostPath
 {
   std::mutex m;
@@ -762,8 +762,10 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
         return fail(FEMTC_ERR_CUDA, "cudaEventCreate failed");
   }
   // Chunks of whole waves of tiles (CTAs per SM x SMs x cells per tile), so
-  // no chunk's kernel ends on a mostly idle wave; about 8 chunks per call,
-  // each a multiple of 4 cells.
+  // no chunk's kernel ends on a mostly idle wave, and as many chunks as the
+  // pipeline holds: the copies in outweigh the kernels, and what is not
+  // overlapped is the first chunk's copy in and the last chunk's kernel and
+  // copy out.  Each chunk is a multiple of 4 cells.
   size_t per;
   {
     const auto sel = select_variant(op, dtype, sem, degree + 1, nquad);
@@ -772,8 +774,8 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
                               &blocks) != FEMTC_OK)
       blocks = 1;
     const size_t wave = std::max<size_t>(4, (size_t)blocks * sm_count() * sel.second.cb);
-    size_t waves = std::max<size_t>(1, (ncells + 8 * wave - 1) / (8 * wave));
-    per = waves * wave;
+    const size_t total = (ncells + wave - 1) / wave; // waves of the call
+    per = std::max<size_t>(1, (total + kHostChunks - 1) / kHostChunks) * wave;
     while ((ncells + per - 1) / per > (size_t)kHostChunks)
       per += wave;
     per = (per + 3) / 4 * 4;

@@ -141,7 +141,11 @@ struct Shape
   static constexpr int NC = geo_nc(OP);
   static constexpr int QP = Q | 1; // odd row length: conflict-free pencils
   static constexpr int SA = N * N * QP; // [i0][i1][q2] buffers
-  static constexpr int SB = N * Q * Q;  // [i0][q1][q2] buffers
+  // [i0][q1][q2] buffers: odd q1 stride BQ and odd i0 stride QQP (fewer
+  // shared-memory bank conflicts of the fragment gathers along q1 and i0)
+  static constexpr int BQ = Q | 1;
+  static constexpr int QQP = (Q * BQ) | 1;
+  static constexpr int SB = N * QQP;
   static constexpr int nA = (OP == OP_STIFFNESS && SEM == SEM_EXACT) ? 2 : 1;
   static constexpr int nB =
       (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);

@@ -555,7 +555,7 @@ struct MmaTile
     };
     auto oidx = [](int r) {
       const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
-      return c * S::SB + i0 * Q * Q + q2;
+      return c * S::SB + i0 * S::QQP + q2;
     };
     Table<SPLIT, N, Q, true, Q> phi;
     phi.build(p.P);
@@ -564,12 +564,12 @@ struct MmaTile
       Table<SPLIT, N, Q, true, Q> gam;
       gam.build(p.D);
       // A0 feeds both Phi (-> B0) and Gamma (-> B1): one gather and split
-      contract_pass_shared<SPLIT, N, Q, true, Q>(A0, phi, gam, iidx, S::QP, B0, B1, oidx, Q, np);
-      contract_pass<SPLIT, N, Q, true, Q>(A1, phi, A1, phi, iidx, S::QP, B2, oidx, Q, np);
+      contract_pass_shared<SPLIT, N, Q, true, Q>(A0, phi, gam, iidx, S::QP, B0, B1, oidx, S::BQ, np);
+      contract_pass<SPLIT, N, Q, true, Q>(A1, phi, A1, phi, iidx, S::QP, B2, oidx, S::BQ, np);
     }
     else
     {
-      contract_pass<SPLIT, N, Q, true, Q>(A0, phi, A0, phi, iidx, S::QP, B0, oidx, Q, np);
+      contract_pass<SPLIT, N, Q, true, Q>(A0, phi, A0, phi, iidx, S::QP, B0, oidx, S::BQ, np);
     }
   }
 
@@ -588,7 +588,10 @@ struct MmaTile
     const Rows rw = rows_of(pt, Q * Q);
     const int np = rw.r1;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    auto bidx = [](int r) { const int c = r / (Q * Q); return c * S::SB + (r - c * (Q * Q)); };
+    auto bidx = [](int r) {
+      const int c = r / (Q * Q), rr = r - c * (Q * Q), q1 = rr / Q;
+      return c * S::SB + q1 * S::BQ + (rr - q1 * Q);
+    };
     Table<SPLIT, N, Q, true, Q> fphi;
     Table<SPLIT, Q, N, false, Q> bphi;
     fphi.build(p.P);
@@ -606,7 +609,7 @@ struct MmaTile
       if constexpr (OP == OP_MASS)
       {
         float v[kblock(N) / 2];
-        gather<N>(B0, bidx, Q * Q, base, np, v);
+        gather<N>(B0, bidx, S::QQP, base, np, v);
         AFrag<SPLIT, kblock(N)> a;
         a.build(v);
         Acc<SPLIT, NTQ> acc;
@@ -635,7 +638,7 @@ struct MmaTile
         float o[NTN][4];
         zero(o);
         accb.unscale_into(ab, o);
-        scatter<N, NTN>(B0, bidx, Q * Q, base, np, o);
+        scatter<N, NTN>(B0, bidx, S::QQP, base, np, o);
       }
       else
       {
@@ -647,7 +650,7 @@ struct MmaTile
         zero(fz);
         {
           float v[kblock(N) / 2];
-          gather<N>(B0, bidx, Q * Q, base, np, v); // AA -> d/dx: Gamma on axis 0
+          gather<N>(B0, bidx, S::QQP, base, np, v); // AA -> d/dx: Gamma on axis 0
           AFrag<SPLIT, kblock(N)> a;
           a.build(v);
           Acc<SPLIT, NTQ> acc;
@@ -657,7 +660,7 @@ struct MmaTile
         }
         {
           float v[kblock(N) / 2];
-          gather<N>(B1, bidx, Q * Q, base, np, v); // AG -> d/dy
+          gather<N>(B1, bidx, S::QQP, base, np, v); // AG -> d/dy
           AFrag<SPLIT, kblock(N)> a;
           a.build(v);
           Acc<SPLIT, NTQ> acc;
@@ -667,7 +670,7 @@ struct MmaTile
         }
         {
           float v[kblock(N) / 2];
-          gather<N>(B2, bidx, Q * Q, base, np, v); // BA -> d/dz
+          gather<N>(B2, bidx, S::QQP, base, np, v); // BA -> d/dz
           AFrag<SPLIT, kblock(N)> a;
           a.build(v);
           Acc<SPLIT, NTQ> acc;
@@ -744,7 +747,7 @@ struct MmaTile
     float o[NTN][4];
     zero(o);
     acc.unscale_into(a, o);
-    scatter<N, NTN>(dst, idx, Q * Q, base, np, o);
+    scatter<N, NTN>(dst, idx, S::QQP, base, np, o);
   }
 
   // Pass 4: backward axis 1, B[c][i0][q1][q2] -> A[c][i0][i1][q2]
@@ -760,7 +763,7 @@ struct MmaTile
     const Rows np = rows_of(pt, N * Q);
     auto iidx = [](int r) {
       const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
-      return c * S::SB + i0 * Q * Q + q2;
+      return c * S::SB + i0 * S::QQP + q2;
     };
     auto oidx = [](int r) {
       const int c = r / (N * Q), rr = r - c * (N * Q), i0 = rr / Q, q2 = rr - i0 * Q;
@@ -770,15 +773,15 @@ struct MmaTile
     phi.build(p.P);
     if constexpr (OP == OP_MASS)
     {
-      contract_pass<SPLIT, Q, N, false, Q>(B0, phi, B0, phi, iidx, Q, A0, oidx, S::QP, np);
+      contract_pass<SPLIT, Q, N, false, Q>(B0, phi, B0, phi, iidx, S::BQ, A0, oidx, S::QP, np);
     }
     else
     {
       Table<SPLIT, Q, N, false, Q> gam;
       gam.build(p.D);
       // U1 = Phi^T X + Gamma^T Y ; U2 = Phi^T Z
-      contract_pass<SPLIT, Q, N, false, Q, true>(B0, phi, B1, gam, iidx, Q, A0, oidx, S::QP, np);
-      contract_pass<SPLIT, Q, N, false, Q>(B2, phi, B2, phi, iidx, Q, A1, oidx, S::QP, np);
+      contract_pass<SPLIT, Q, N, false, Q, true>(B0, phi, B1, gam, iidx, S::BQ, A0, oidx, S::QP, np);
+      contract_pass<SPLIT, Q, N, false, Q>(B2, phi, B2, phi, iidx, S::BQ, A1, oidx, S::QP, np);
     }
   }
 

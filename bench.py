@@ -366,7 +366,7 @@ def run_batch(args, rank, world, dev, pg):
         return worst
 
     for dtype in (F.F32, F.BF16X3, F.F16X2):
-        b = F.Batch(dtype, meshes, tune=True)
+        b = F.Batch(dtype, meshes, tune=not args.no_batch_tune)
         res = {}
         for mode in ("graph", "eager", "separate"):
             def step():
@@ -500,6 +500,8 @@ def main():
                     help="serve: operator form of the inner CG (FP64 refinement outside)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch-tune", action="store_true",
+                    help="batch64: built-in tile layouts (no autotuning launches; profiling)")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
     ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3,f64e,f64plain",
                     help="comma list of forms to time; the first is the headline")

@@ -395,11 +395,6 @@ std::pair<const CellVariant*, TileCfg> select_variant(int op, int dtype, int sem
   return {v, default_tile(*v)};
 }
 
-TileCfg tile_config(const CellVariant& v)
-{
-  return select_variant(v.op, v.dtype, v.sem, v.n, v.q).second;
-}
-
 // -------------------------------------------------------- launch helpers --
 struct FnState
 {

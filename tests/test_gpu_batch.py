@@ -12,15 +12,20 @@ pytestmark = pytest.mark.gpu
 TOL = {1: 2e-6, 2: 1e-6, 3: 1e-6}
 
 
-def make_meshes(femtc, dev, dtype, seed=0, scale=1):
+def make_meshes(femtc, dev, dtype, seed=0, scale=1, random_tables=False):
     import torch
     from femtc_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     meshes, hosts = [], []
+    rtabs = {}
     for P in range(1, 8):
         for op in (0, 1):
             ncells = int(rng.integers(1, 300)) * scale + (P * 7 + op) % 5
             w = W.make_custom("b", op, P, P + 2, ncells, seed=100 * P + op + seed)
+            if random_tables:  # no symmetry: the plain (not even-odd) kernels
+                if P not in rtabs:
+                    rtabs[P] = np.random.default_rng(P).uniform(-1.0, 1.0, w.tables.shape)
+                w.tables = rtabs[P]
             u = torch.from_numpy(w.u).to(dev, torch.float32)
             g = torch.from_numpy(w.geo).to(dev, torch.float32)
             y = torch.full_like(u, float("nan"))
@@ -55,6 +60,26 @@ def test_batch_matches_oracle_and_single_calls(femtc, orc, dev, dtype, tune):
         torch.cuda.synchronize()
         alone = ys.double().cpu().numpy()
         assert np.abs(alone - yb).max() <= 1e-6 * np.abs(ref).max()
+    b.close()
+
+
+def test_batch_plain_family_nonsymmetric_tables(femtc, orc, dev):
+    """FP32 meshes whose tables lack the GLL-to-Gauss symmetry run the plain
+    CUDA-core family (the symmetric ones take the even-odd family): every
+    mesh against the oracle.  Random tables of both signs cancel more than
+    the tabulated ones, so the FP32 tolerance here is 2e-5."""
+    import torch
+    meshes, hosts = make_meshes(femtc, dev, 1, seed=7, random_tables=True)
+    b = femtc.Batch(1, meshes)
+    b.launch()
+    torch.cuda.synchronize()
+    assert femtc.device_status() == 0
+    for (op, P, Q, tab, u, y, g, n), w in zip(meshes, hosts):
+        fn = orc.mass if op == 0 else orc.stiffness
+        ref = fn(orc.EXACT, P, Q, tab.astype(np.float64), w.u.astype(np.float32).astype(np.float64),
+                 w.geo.astype(np.float32).astype(np.float64))
+        err = np.abs(y.double().cpu().numpy() - ref).max() / np.abs(ref).max()
+        assert err <= 2e-5, (op, P, err)
     b.close()
 
 

@@ -28,6 +28,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -37,9 +38,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# FP64 FMA throughput measured on this machine's GB300 with a dependent-chain
-# FMA kernel (profiles/gb300_pipe_peaks.md); the generated peaks file
-# carries no FP64 figure.
+# FP64 FMA throughput measured on a GB300 with a dependent-chain FMA kernel
+# (profiles/gb300_pipe_peaks.md); the measured-peaks file (HBM copy, bf16
+# GEMM) carries no FP64 figure.
 FP64_PEAK_TFLOPS = 1.20
 FALLBACK_HBM_GBS = 6800.0
 
@@ -157,7 +158,7 @@ class ClockSampler:
     def __init__(self, index: int):
         self.proc = None
         self.index = index
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"femtc_clocks_{os.getpid()}_{index}.csv")
 
     def __enter__(self):
         try:

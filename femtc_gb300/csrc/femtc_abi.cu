@@ -1106,8 +1106,19 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
   if (ncells == 0)
     return fail(FEMTC_ERR_INVALID, "autotune needs at least one cell");
   // candidates: for each (staging, threads), the cell counts per tile with
-  // the best lane efficiency that fit in shared memory
+  // the best lane efficiency that fit in shared memory, and -- for calls of
+  // a few waves, where whole SMs idle when the tile count is just past a
+  // multiple of the SM count -- the cell counts that give about 1, 2 or 3
+  // tiles per SM
   std::vector<std::pair<const CellVariant*, TileCfg>> cands;
+  std::vector<int> wave_cb;
+  for (int k = 1; k <= 3; ++k)
+  {
+    const size_t per = (ncells + (size_t)k * sm_count() - 1) / ((size_t)k * sm_count());
+    const int c = (int)std::min<size_t>(128, (per + 3) / 4 * 4);
+    if (c >= 4)
+      wave_cb.push_back(c);
+  }
   for (int lanes = 1; lanes <= 2; ++lanes)
   {
     const CellVariant* lv = find_cell(op, dtype, semantics, degree + 1, nquad, lanes);
@@ -1128,6 +1139,15 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
                   [](const auto& a, const auto& b) { return a.first > b.first; });
         for (size_t i = 0; i < opts.size() && i < 4; ++i)
           cands.push_back({lv, opts[i].second});
+        for (int c : wave_cb)
+        {
+          const TileCfg t = with_layout(*lv, c, staged, nt);
+          bool dup = false;
+          for (size_t i = 0; i < opts.size() && i < 4; ++i)
+            dup = dup || opts[i].second.cb == c;
+          if (!dup && smem_of(*lv, t) <= 227u * 1024u)
+            cands.push_back({lv, t});
+        }
       }
   }
   if (cands.empty())

@@ -43,6 +43,7 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # GEMM) carries no FP64 figure.
 FP64_PEAK_TFLOPS = 1.20
 FALLBACK_HBM_GBS = 6800.0
+L2_BYTES = 129e6  # GB300 L2
 
 
 def flops_per_cell(op: int, n: int, q: int) -> float:
@@ -92,15 +93,17 @@ def _eo_mv_instr(m: int, k: int, sig: int) -> int:
     return 2 * k2 + m2 * (2 * k2 + km + 2) + mm * mid
 
 
-def pipe_instr_per_cell(op: int, n: int, q: int, even_odd: bool) -> float:
+def pipe_instr_per_cell(op: int, n: int, q: int, even_odd: bool, affine: bool = False) -> float:
     """FP64-pipe instructions per cell: every FMA, MUL and ADD takes one
     issue slot of the pipe, so this (not the flop count) is what the pipe's
     busy fraction measures.  Plain kernels: one FMA per multiply-add plus
-    the point-wise work; even-odd kernels: as their code runs."""
+    the point-wise work; even-odd kernels: as their code runs.  Affine mass
+    scales each pencil's N inputs by detJ instead of its Q points."""
     grad = op != 0
+    pw = (9 * q ** 3) if grad else (n ** 3 if affine else q ** 3)  # point-wise work
     if not even_odd:
         macs = flops_per_cell(op, n, q) - (15 if grad else 1) * q ** 3
-        return macs / 2 + (9 if grad else 1) * q ** 3
+        return macs / 2 + pw
     n2, nm, q2, qm = n // 2, n % 2, q // 2, q % 2
     mv_f = lambda s: _eo_mv_instr(q, n, s)
     mv_b = lambda s: _eo_mv_instr(n, q, s)
@@ -108,16 +111,17 @@ def pipe_instr_per_cell(op: int, n: int, q: int, even_odd: bool) -> float:
     pair_row = (2 * n2 + nm + 2) * (2 if grad else 1)
     mid_row = (n2 + nm) + (n2 if grad else 0)
     fwd = n * 2 * n2 + q2 * (n * pair_row + 2 * emit) + qm * (n * mid_row + emit)
-    fused = (3 * mv_f(1) + 9 * q + 3 * mv_b(1)) if grad else (mv_f(1) + q + mv_b(1))
+    fused = (3 * mv_f(1) + 3 * mv_b(1)) if grad else (mv_f(1) + mv_b(1))
     col = mv_b(1) + ((mv_b(-1) + n + mv_b(1)) if grad else 0)
     pair_acc = n * ((2 + 2 * n2 + nm) * (2 if grad else 1))
     mid_col = n * (n2 * (2 if grad else 1) + nm)
     bwd = q2 * (2 * col + pair_acc) + qm * (col + mid_col) + n * 2 * n2
-    return float(n * fwd + q * q * fused + n * bwd)
+    return float(n * fwd + q * q * fused + pw + n * bwd)
 
 
-def bytes_per_cell(op: int, n: int, q: int, es: int) -> float:
-    return es * (2 * n ** 3 + (1 if op == 0 else 6) * q ** 3)
+def bytes_per_cell(op: int, n: int, q: int, es: int, affine: bool = False) -> float:
+    """u in, y out, and the geometry: per point, or one set per cell (affine)."""
+    return es * (2 * n ** 3 + (1 if op == 0 else 6) * (1 if affine else q ** 3))
 
 
 # DRAM bytes (read + write) of one launch of the headline kernel, measured
@@ -283,13 +287,15 @@ def run_reference(args, rank, world):
 
 
 def cpu_baseline(w, seconds=10.0):
-    """Time the oracle's C restatement on the host cores on a bounded sample."""
+    """Time the oracle's C restatement on the host cores on a bounded sample
+    (affine workloads: the per-point operator on the same mesh, the only
+    form the reference has)."""
     import oracle
     oracle.lib()
     cores = os.cpu_count() or 1
-    fn = oracle.mass if w.op == 0 else oracle.stiffness
+    fn = oracle.mass if w.base_op == 0 else oracle.stiffness
     sample = w.ncells
-    u, g = w.u[:sample], w.geo[:sample]
+    u, g = w.u[:sample], w.point_geometry(sample)
     fn(oracle.EXACT, w.degree, w.nquad, w.tables, u, g, nthreads=cores)  # warm
     reps, t0 = 0, time.perf_counter()
     while True:
@@ -504,6 +510,9 @@ def main():
     ap.add_argument("--no-batch-tune", action="store_true",
                     help="batch64: built-in tile layouts (no autotuning launches; profiling)")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
+    ap.add_argument("--geometry", default="per-point", choices=["per-point", "affine"],
+                    help="affine: the same degree and cell count on affine cells through the "
+                         "affine operator forms (one geometry set per cell), F64 and F32")
     ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3,f64e,f64plain",
                     help="comma list of forms to time; the first is the headline")
     ap.add_argument("--tile-db", default=None,
@@ -535,8 +544,10 @@ def main():
             pg.destroy_process_group()
         return
 
-    w = W.make(args.workload, ncells=args.cells)
-    n, q, op = w.n, w.nquad, w.op
+    w = (W.make_affine if args.geometry == "affine" else W.make)(args.workload, ncells=args.cells)
+    # op: the entry point's operator code; base: mass (0) or stiffness (1)
+    n, q, op, base = w.n, w.nquad, w.op, w.base_op
+    tabs = w.op_tables()
     stream = torch.cuda.current_stream()
     names = {v: k for k, v in F.DTYPE_NAMES.items()}
     # "f64plain": FP64 with the even-odd contractions switched off (the plain
@@ -563,8 +574,9 @@ def main():
     y_oracle = None
     if rank == 0:
         import oracle
-        fn = oracle.mass if op == 0 else oracle.stiffness
-        y_oracle = fn(oracle.EXACT, w.degree, q, w.tables, w.u[:err_cells], w.geo[:err_cells])
+        fn = oracle.mass if base == 0 else oracle.stiffness
+        y_oracle = fn(oracle.EXACT, w.degree, q, w.tables, w.u[:err_cells],
+                      w.point_geometry(err_cells))
 
     tuned = False
     if args.tile_db and os.path.exists(args.tile_db):
@@ -583,12 +595,19 @@ def main():
         y = torch.empty_like(u)
 
         def step():
-            F.apply(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
+            F.apply(op, dtype, F.EXACT, w.degree, q, tabs, u, y, g, w.ncells, stream)
 
         if not tuned and key != F64PLAIN:  # the project's autotuner, outside the timed region
-            F.autotune(op, dtype, F.EXACT, w.degree, q, w.tables, u, y, g, w.ncells, stream)
+            F.autotune(op, dtype, F.EXACT, w.degree, q, tabs, u, y, g, w.ncells, stream)
         tile = F.get_tile_config(op, dtype, F.EXACT, w.degree, q)
 
+        # inputs under 1.5x the L2 could be served from it in part by the
+        # previous launch: a 512 MB write between launches evicts them, and
+        # the time is the sum of the launches' own events
+        es = 8 if dtype in F.FP64_STORAGE else 4
+        flush = None
+        if bytes_per_cell(base, n, q, es, w.affine) * w.ncells < 1.5 * L2_BYTES:
+            flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
         for _ in range(args.warmup):
             step()
         barrier()
@@ -603,6 +622,8 @@ def main():
         l0 = F.operator_launches()
         t_start.record(stream)
         for i in range(args.steps):
+            if flush is not None:
+                flush.fill_(i & 255)
             ev[i][0].record(stream)
             step()
             ev[i][1].record(stream)
@@ -611,14 +632,19 @@ def main():
         barrier()
         if sampler:
             sampler.__exit__(None, None, None)
-        total_ms = maxreduce(t_start.elapsed_time(t_end))
+        if flush is None:
+            total_ms = maxreduce(t_start.elapsed_time(t_end))
+        else:
+            total_ms = maxreduce(sum(a.elapsed_time(b) for a, b in ev))
         kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
         err = None
         if y_oracle is not None:
             yo = y[:err_cells].double().cpu().numpy()
             err = float(np.abs(yo - y_oracle).max() / np.abs(y_oracle).max())
         results[key] = dict(total_ms=total_ms, kern_ms=kern_ms, err=err, tile=tile,
-                            clocks=sampler.summary() if sampler else None)
+                            clocks=sampler.summary() if sampler else None,
+                            l2_flush=flush is not None)
+        del flush
         F.set_even_odd(True)
         if F.device_status() != 0:
             raise RuntimeError("device fault word set during the benchmark")
@@ -640,10 +666,10 @@ def main():
         yh = torch.empty_like(uh).pin_memory()
 
         def estep():
-            F.apply_host(op, dtype, F.EXACT, w.degree, q, w.tables, uh, yh, gh, w.ncells)
+            F.apply_host(op, dtype, F.EXACT, w.degree, q, tabs, uh, yh, gh, w.ncells)
 
         # tile tuning of the zero-copy path (setup, outside the timed region)
-        F.autotune_host(op, dtype, F.EXACT, w.degree, q, w.tables, uh, yh, gh, w.ncells)
+        F.autotune_host(op, dtype, F.EXACT, w.degree, q, tabs, uh, yh, gh, w.ncells)
         for mode in (0, 2, 1):  # auto (tuned choice), zero-copy, staging pipeline
             F.set_host_path(mode)
             for _ in range(args.warmup):
@@ -663,16 +689,16 @@ def main():
 
     r = results[head]
     value = world * args.steps * w.ndofs / (r["total_ms"] * 1e-3) / 1e9
-    fpc = flops_per_cell(op, n, q)
+    fpc = flops_per_cell(base, n, q)
     # the FP64 pipe's roof counts the operations the kernel runs: the even-odd
     # kernels execute fewer than the reference's flop convention
-    head_eo = head == F.F64 and F.even_odd_used(op, F.F64, F.EXACT, w.degree, q, w.tables)
-    fpc_head = flops_per_cell_even_odd(op, n, q) if head_eo else fpc
-    bpc = bytes_per_cell(op, n, q, 8 if head == F.F64 else 4)
+    head_eo = head == F.F64 and F.even_odd_used(op, F.F64, F.EXACT, w.degree, q, tabs)
+    fpc_head = flops_per_cell_even_odd(base, n, q) if head_eo else fpc
+    bpc = bytes_per_cell(base, n, q, 8 if head == F.F64 else 4, w.affine)
     ach_tf = fpc_head * w.ncells / (r["kern_ms"] * 1e-3) / 1e12
     # FP64 pipe: instructions issued per second against its peak (half the
     # FMA flop rate: one FMA = two flops = one instruction)
-    pipe_frac = (pipe_instr_per_cell(op, n, q, head_eo) * w.ncells / (r["kern_ms"] * 1e-3)
+    pipe_frac = (pipe_instr_per_cell(base, n, q, head_eo, w.affine) * w.ncells / (r["kern_ms"] * 1e-3)
                  / (FP64_PEAK_TFLOPS * 1e12 / 2)) if head == F.F64 else None
     ach_gbs = bpc * w.ncells / (r["kern_ms"] * 1e-3) / 1e9
     hbm, hbm_src = peaks()
@@ -683,7 +709,7 @@ def main():
         variants[dname[key]] = {
             "gdofs": world * args.steps * w.ndofs / (res["total_ms"] * 1e-3) / 1e9,
             "kernel_ms": res["kern_ms"],
-            "hbm_gbs": bytes_per_cell(op, n, q, es) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
+            "hbm_gbs": bytes_per_cell(base, n, q, es, w.affine) * w.ncells / (res["kern_ms"] * 1e-3) / 1e9,
             "tflops_reference_convention": fpc * w.ncells / (res["kern_ms"] * 1e-3) / 1e12,
             "max_rel_err_vs_fp64_oracle": res["err"],
             "tile": {"cells": res["tile"][0], "geo_staged": res["tile"][1], "threads": res["tile"][2],
@@ -691,16 +717,21 @@ def main():
         }
     if rank == 0:
         line = {
-            "metric": f"GDoF/s {'stiffness' if op == 1 else 'mass'} action (P={w.degree}, Q={q})",
+            "metric": f"GDoF/s {'stiffness' if base == 1 else 'mass'} action (P={w.degree}, Q={q})",
             "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": F.DTYPE_NAMES[head], "data": "synthetic",
-            "config": {"workload": args.workload, "cells": w.ncells, "degree": w.degree, "nquad": q,
+            "config": {"workload": w.name, "cells": w.ncells, "degree": w.degree, "nquad": q,
                        "dofs": w.ndofs, "parallelism": f"replicas{world}",
-                       "l2": f"inputs {bpc * w.ncells / 1e6:.0f} MB > 129 MB L2, no flush"},
+                       "geometry": ("affine: one factor set per cell, weights in the backward "
+                                    "tables" if w.affine else "per quadrature point"),
+                       "l2": (f"inputs {bpc * w.ncells / 1e6:.0f} MB "
+                              + ("< 1.5 x 129 MB L2: a 512 MB write between launches flushes "
+                                 "it; time = sum of the launches' events" if r["l2_flush"]
+                                 else "> 1.5 x 129 MB L2, no flush"))},
             "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src,
-                                 traffic_for(args.workload, w.ncells, head),
+                                 traffic_for(w.name, w.ncells, head),
                                  flop_count=("even-odd kernel operations per cell "
                                              f"{fpc_head:.0f} (reference convention {fpc:.0f})")
                                  if head == F.F64 else None, pipe_frac=pipe_frac),

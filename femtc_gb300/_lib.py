@@ -18,6 +18,7 @@ from . import buildlib as _build
 F64, F32, F16X2, BF16X3, F64E = 0, 1, 2, 3, 4
 EXACT, REFERENCE = 0, 1
 MASS, STIFFNESS, HELMHOLTZ = 0, 1, 2
+MASS_AFFINE, STIFFNESS_AFFINE = 3, 4  # one geometry set per cell (affine cells)
 
 DTYPE_NAMES = {F64: "f64", F32: "f32", F16X2: "f16x2", BF16X3: "bf16x3", F64E: "f64e"}
 FP64_STORAGE = (F64, F64E)
@@ -50,6 +51,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_even_odd_used": ([c_int] * 5 + [vp], c_int),
         "femtc_helmholtz_geometry": ([c_int, ctypes.c_double, vp, ctypes.c_double, vp, vp, c_size, vp],
                                      c_int),
+        "femtc_affine_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
+        "femtc_affine_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_mass_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_stiffness_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_set_tile_config": ([c_int] * 9, c_int),
@@ -153,12 +156,36 @@ def tabulate(degree: int, nquad: int):
 
 def apply(op: int, dtype: int, semantics: int, degree: int, nquad: int,
           tables, u, y, geo, ncells: int, stream=None) -> None:
-    """Device-resident operator action through femtc_{mass,stiffness}_apply."""
+    """Device-resident operator action through femtc_{mass,stiffness}_apply
+    (affine forms: femtc_affine_apply, exact semantics, tables with the
+    weights appended -- see affine_tables)."""
     lib = load()
     tab = host_tables(tables, dtype)
+    if op in (MASS_AFFINE, STIFFNESS_AFFINE):
+        if semantics != EXACT:
+            raise ValueError("affine forms: exact semantics only")
+        check(lib.femtc_affine_apply(op, dtype, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
+                                     ptr(geo), ncells, stream_ptr(stream)))
+        return
     fn = lib.femtc_mass_apply if op == MASS else lib.femtc_stiffness_apply
     check(fn(dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
              ptr(geo), ncells, stream_ptr(stream)))
+
+
+def affine_tables(tables, weights) -> np.ndarray:
+    """The affine forms' tables: Phi, Gamma (2*Q*N) then the Q 1D weights."""
+    return np.concatenate([np.asarray(tables, dtype=np.float64).reshape(-1),
+                           np.asarray(weights, dtype=np.float64).reshape(-1)])
+
+
+def affine_apply(op: int, dtype: int, degree: int, nquad: int, tables, weights, u, y, cgeo,
+                 ncells: int, stream=None) -> None:
+    """Operator action on affine cells (femtc_affine_apply): cgeo holds one
+    detJ (MASS_AFFINE) or one detJ J^-1 J^-T [zz,yz,xz,yy,xy,xx]
+    (STIFFNESS_AFFINE) per cell; the 1D quadrature weights enter through the
+    backward tables."""
+    apply(op, dtype, EXACT, degree, nquad, affine_tables(tables, weights), u, y, cgeo, ncells,
+          stream)
 
 
 def helmholtz_apply(dtype: int, degree: int, nquad: int, tables, u, y, geo8, ncells: int,
@@ -182,6 +209,12 @@ def apply_host(op: int, dtype: int, semantics: int, degree: int, nquad: int,
     """Host-buffer drop-in path (copies in, applies, copies out)."""
     lib = load()
     tab = host_tables(tables, dtype)
+    if op in (MASS_AFFINE, STIFFNESS_AFFINE):
+        if semantics != EXACT:
+            raise ValueError("affine forms: exact semantics only")
+        check(lib.femtc_affine_apply_host(op, dtype, degree, nquad, tab.ctypes.data, ptr(u),
+                                          ptr(y), ptr(geo), ncells))
+        return
     fn = lib.femtc_mass_apply_host if op == MASS else lib.femtc_stiffness_apply_host
     check(fn(dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
              ptr(geo), ncells))

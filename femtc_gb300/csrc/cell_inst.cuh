@@ -96,6 +96,26 @@ void add_helmholtz(std::vector<CellVariant>& v, int dtype)
   }
 }
 
+// Affine forms (exact semantics, one lane per slab), N = N0..8, Q = N..N+2:
+// the plain kernels, and the even-odd ones up to N = MAXEO.
+template <typename T, int OP, int N, int MAXEO>
+void add_affine(std::vector<CellVariant>& v, int dtype)
+{
+  if constexpr (N <= 8)
+  {
+    add_variant<T, N, N, OP, SEM_EXACT, 1>(v, dtype);
+    add_variant<T, N, N + 1, OP, SEM_EXACT, 1>(v, dtype);
+    add_variant<T, N, N + 2, OP, SEM_EXACT, 1>(v, dtype);
+    if constexpr (N <= MAXEO)
+    {
+      add_variant<T, N, N, OP, SEM_EXACT, 1, true>(v, dtype);
+      add_variant<T, N, N + 1, OP, SEM_EXACT, 1, true>(v, dtype);
+      add_variant<T, N, N + 2, OP, SEM_EXACT, 1, true>(v, dtype);
+    }
+    add_affine<T, OP, N + 1, MAXEO>(v, dtype);
+  }
+}
+
 inline unsigned read_clear_fault_word()
 {
   unsigned w = 0, z = 0;

@@ -41,15 +41,40 @@ enum Op : int
 {
   OP_MASS = 0,
   OP_STIFFNESS = 1,
-  OP_HELMHOLTZ = 2 // alpha M + beta K in one pass (exact semantics)
+  OP_HELMHOLTZ = 2, // alpha M + beta K in one pass (exact semantics)
+  // Affine cells (exact semantics): detJ and J^-1 J^-T are constant over a
+  // cell, so one set of factors per cell replaces the Q^3 per-point values.
+  // The tensor-product quadrature weight w(q0) w(q1) w(q2) is folded into
+  // the backward tables: every backward contraction along axis d scales
+  // its table rows by w(q_d), and each point's value passes one backward
+  // contraction per axis.
+  OP_MASS_AFFINE = 3,
+  OP_STIFFNESS_AFFINE = 4
 };
+
+__host__ __device__ constexpr bool op_affine(int op)
+{
+  return op == OP_MASS_AFFINE || op == OP_STIFFNESS_AFFINE;
+}
+// The operator an affine form computes (mass or stiffness).
+__host__ __device__ constexpr int op_base(int op)
+{
+  return op_affine(op) ? op - OP_MASS_AFFINE : op;
+}
 
 // Geometry values per quadrature point: mass detJ*w; stiffness the six
 // components of G; Helmholtz [zz,yz,xz,yy,xy,xx] of beta*G, then alpha*detJ*w
-// and one zero (eight values: four 8-byte pairs per point).
+// and one zero (eight values: four 8-byte pairs per point); none for the
+// affine forms.
 __host__ __device__ constexpr int geo_nc(int op)
 {
-  return op == OP_MASS ? 1 : (op == OP_STIFFNESS ? 6 : 8);
+  return op == OP_MASS ? 1 : (op == OP_STIFFNESS ? 6 : (op == OP_HELMHOLTZ ? 8 : 0));
+}
+// Geometry values per cell of the affine forms: detJ (mass); the six
+// components of detJ J^-1 J^-T as [zz,yz,xz,yy,xy,xx] (stiffness).
+__host__ __device__ constexpr int cell_nc(int op)
+{
+  return op == OP_MASS_AFFINE ? 1 : (op == OP_STIFFNESS_AFFINE ? 6 : 0);
 }
 enum Sem : int
 {
@@ -146,9 +171,9 @@ struct Shape
   static constexpr int BQ = Q | 1;
   static constexpr int QQP = (Q * BQ) | 1;
   static constexpr int SB = N * QQP;
-  static constexpr int nA = (OP == OP_STIFFNESS && SEM == SEM_EXACT) ? 2 : 1;
+  static constexpr int nA = (op_base(OP) == OP_STIFFNESS && SEM == SEM_EXACT) ? 2 : 1;
   static constexpr int nB =
-      (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
+      (op_base(OP) == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   static constexpr int work = nA * SA + nB * SB; // per cell, elements
 };
 
@@ -340,7 +365,7 @@ __host__ __device__ inline CellLayout tile_layout(const CellParams<T>& p)
   using ST = storage_t<T>;
   const unsigned bu = (unsigned)p.cb * N * Tile::US * sizeof(ST);
   const unsigned bg =
-      p.geo_staged ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(ST) : 0u;
+      (NC > 0 && p.geo_staged) ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(ST) : 0u;
   return CellLayout(bu, bg, Tile::work_bytes(p), Tile::kStages);
 }
 
@@ -352,7 +377,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   constexpr int US = Tile::US;
   extern __shared__ __align__(128) unsigned char smem[];
   const int cb = p.cb;
-  const bool staged = p.geo_staged != 0;
+  const bool staged = NC > 0 && p.geo_staged != 0; // affine forms: nothing to stage
   const long long ntiles = (p.ncells + cb - 1) / cb;
   static_assert(Tile::kStages == 2, "the CTA-wide loop keeps two stages");
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
@@ -569,8 +594,12 @@ struct SlabTile
   static constexpr int US = slab_stride<ST>(N);
   static constexpr int N2 = N * N, Q2 = Q * Q, Q3 = Q * Q * Q;
   // the gradient passes: stiffness and Helmholtz (the latter exact only)
-  static constexpr bool kGrad = (OP != OP_MASS);
+  static constexpr bool kGrad = (op_base(OP) != OP_MASS);
+  // affine forms: per-cell geometry, quadrature weights in the backward
+  // tables (PB, DB), which then differ from the forward ones in every form
+  static constexpr bool kAffine = op_affine(OP);
   static_assert(OP != OP_HELMHOLTZ || SEM == SEM_EXACT, "Helmholtz: exact semantics only");
+  static_assert(!kAffine || SEM == SEM_EXACT, "affine forms: exact semantics only");
   static_assert(!EVOD || (SEM == SEM_EXACT && LANES == 1), "even-odd: exact, one lane per slab");
   // Streaming loop: work split by warps (stream_tiles_warp) where its extra
   // live state costs no occupancy -- FP32 and N <= 4; the register-heavy
@@ -583,7 +612,7 @@ struct SlabTile
   // its shared memory costs more occupancy than the deeper prefetch gains.
   static constexpr int kStages = 2;
   static constexpr int NBUF =
-      (OP == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
+      (op_base(OP) == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
   // reference A(i,q) = tab[i + q*Q] (the forward table reused, Q == N)
   static constexpr int BSM = (SEM == SEM_EXACT) ? Q : 1;
@@ -894,9 +923,10 @@ struct SlabTile
   {
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
-    // backward tables: the even-odd ones, else the forward ones transposed
-    const T* __restrict__ PB = EVOD ? p.PB : p.P;
-    const T* __restrict__ DB = EVOD ? p.DB : p.D;
+    // backward tables: the even-odd or weighted ones, else the forward
+    // ones transposed
+    const T* __restrict__ PB = (EVOD || kAffine) ? p.PB : p.P;
+    const T* __restrict__ DB = (EVOD || kAffine) ? p.DB : p.D;
     const int bstride = w.ncb * p.sbc;
     for (int t = w.c0 * Q2 + w.tid; t < w.c1 * Q2; t += w.nthr)
     {
@@ -905,7 +935,21 @@ struct SlabTile
       T* b1 = b0 + bstride;
       T* b2 = b1 + bstride;
       const int sq = p.sq;
-      if constexpr (OP == OP_MASS)
+      if constexpr (OP == OP_MASS_AFFINE)
+      {
+        // detJ scales the pencil's N inputs (the weights are in PB)
+        const T dj = from_storage<T>(geo[geo_cell0 + c]);
+        T x[N], v[Q];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          x[k] = b0[k * sq] * dj;
+        fwd<1>(P, x, v);
+        bwd<1>(PB, v, x);
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          b0[k * sq] = x[k];
+      }
+      else if constexpr (OP == OP_MASS)
       {
         const ST* dw = geo + (geo_cell0 + c) * Q3 + r;
         T x[N], v[Q];
@@ -924,7 +968,7 @@ struct SlabTile
       else
       {
         constexpr int NCG = geo_nc(OP);
-        const ST* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG;
+        const ST* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG; // unused by affine forms
         T xa[N], xg[N], fx[Q], fy[Q], fz[Q];
         T fm[OP == OP_HELMHOLTZ ? Q : 1];
 #pragma unroll
@@ -951,13 +995,22 @@ struct SlabTile
         }
         // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx], read
         // as three 8/16-byte pairs (Helmholtz: a fourth pair holds the mass
-        // factor)
+        // factor; affine: the cell's one G for every point)
         using V2 = typename std::conditional<sizeof(ST) == 4, float2, double2>::type;
+        V2 a01{}, a23{}, a45{};
+        if constexpr (kAffine)
+        {
+          const V2* ga = reinterpret_cast<const V2*>(geo + (geo_cell0 + c) * cell_nc(OP));
+          a01 = ga[0];
+          a23 = ga[1];
+          a45 = ga[2];
+        }
 #pragma unroll
         for (int q = 0; q < Q; ++q)
         {
           const V2* g2 = reinterpret_cast<const V2*>(G + (long long)q * Q2 * NCG);
-          const V2 g01 = g2[0], g23 = g2[1], g45 = g2[2];
+          const V2 g01 = kAffine ? a01 : g2[0], g23 = kAffine ? a23 : g2[1],
+                   g45 = kAffine ? a45 : g2[2];
           if constexpr (OP == OP_HELMHOLTZ)
             fm[q] *= from_storage<T>(g2[3].x);
           const T zz = from_storage<T>(g01.x), yz = from_storage<T>(g01.y),
@@ -1141,8 +1194,8 @@ struct SlabTile
       backward_eo(p, sw, sy, w);
       return;
     }
-    const T* __restrict__ P = p.P;
-    const T* __restrict__ D = p.D;
+    const T* __restrict__ P = kAffine ? p.PB : p.P; // affine: weighted tables
+    const T* __restrict__ D = kAffine ? p.DB : p.D;
     // every lane of a warp takes part in the shuffle reduction, so all
     // threads of the part run the same number of rounds
     const int bstride = w.ncb * p.sbc;
@@ -1337,7 +1390,7 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   constexpr int US = Tile::US;
   extern __shared__ __align__(128) unsigned char smem[];
   const int cb = p.cb;
-  const bool staged = p.geo_staged != 0;
+  const bool staged = NC > 0 && p.geo_staged != 0; // affine forms: nothing to stage
   const long long ntiles = (p.ncells + cb - 1) / cb;
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
   constexpr int NS = Tile::kStages;

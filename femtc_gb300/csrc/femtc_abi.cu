@@ -68,6 +68,10 @@ Registry& registry()
     register_cell_f32eo_stiffness(r.cells, r.faults);
     register_cell_f64eeo_mass(r.cells, r.faults);
     register_cell_f64eeo_stiffness(r.cells, r.faults);
+    register_cell_affine_f64_mass(r.cells, r.faults);
+    register_cell_affine_f64_stiffness(r.cells, r.faults);
+    register_cell_affine_f32_mass(r.cells, r.faults);
+    register_cell_affine_f32_stiffness(r.cells, r.faults);
     register_cell_f64e_mass(r.cells, r.faults);
     register_cell_f64e_stiffness(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);
@@ -121,6 +125,19 @@ bool centro_symmetric(const S* tab, int n, int q, int ntab)
   return true;
 }
 
+template <typename S>
+bool symmetric_weights(const S* w, int q)
+{
+  const double tol = sizeof(S) == 8 ? 1e-12 : 5e-7;
+  double amax = 0.0, dev = 0.0;
+  for (int k = 0; k < q; ++k)
+  {
+    amax = std::max(amax, std::fabs((double)w[k]));
+    dev = std::max(dev, std::fabs((double)w[k] - (double)w[q - 1 - k]));
+  }
+  return dev <= tol * amax;
+}
+
 // The variant that runs a launch of v with these tables: v's even-odd twin
 // when there is one and the tables allow it.
 const CellVariant& launch_form(const CellVariant& v, const void* tables)
@@ -131,10 +148,16 @@ const CellVariant& launch_form(const CellVariant& v, const void* tables)
   const CellVariant* t = find_cell(v.op, v.dtype, v.sem, v.n, v.q, 1, 1);
   if (!t)
     return v;
-  const int ntab = v.op == FEMTC_OP_MASS ? 1 : 2;
-  const bool sym = v.dtype == FEMTC_F32
-                       ? centro_symmetric(static_cast<const float*>(tables), v.n, v.q, ntab)
-                       : centro_symmetric(static_cast<const double*>(tables), v.n, v.q, ntab);
+  const int ntab = op_base(v.op) == FEMTC_OP_MASS ? 1 : 2;
+  bool sym = v.dtype == FEMTC_F32
+                 ? centro_symmetric(static_cast<const float*>(tables), v.n, v.q, ntab)
+                 : centro_symmetric(static_cast<const double*>(tables), v.n, v.q, ntab);
+  // affine forms: the weights folded into the backward tables must be
+  // symmetric too, w(Q-1-q) = w(q)
+  if (sym && op_affine(v.op))
+    sym = v.dtype == FEMTC_F32
+              ? symmetric_weights(static_cast<const float*>(tables) + 2 * v.n * v.q, v.q)
+              : symmetric_weights(static_cast<const double*>(tables) + 2 * v.n * v.q, v.q);
   return sym ? *t : v;
 }
 
@@ -145,7 +168,7 @@ int default_lanes(int op, int dtype, int n)
 {
   if (dtype != FEMTC_F32)
     return 1;
-  return (op != FEMTC_OP_MASS && n <= 5) ? 2 : 1;
+  return ((op == FEMTC_OP_STIFFNESS || op == FEMTC_OP_HELMHOLTZ) && n <= 5) ? 2 : 1;
 }
 
 // ---------------------------------------------------------------- tiles --
@@ -469,13 +492,17 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
                 degree, nquad);
   if (!tables || !u || !y || !geo)
     return fail(FEMTC_ERR_INVALID, "null pointer argument");
+  static const char* const names[5] = {"mass", "stiffness", "Helmholtz", "affine mass",
+                                       "affine stiffness"};
+  if (op < 0 || op > 4)
+    return fail(FEMTC_ERR_INVALID, "unknown operator %d", op);
+  if (op_affine(op) && sem != FEMTC_EXACT)
+    return fail(FEMTC_ERR_INVALID, "affine forms: exact semantics only");
   const CellVariant* v = find_cell(op, dtype, sem, degree + 1, nquad);
   if (!v)
     return fail(FEMTC_ERR_UNSUPPORTED,
                 "no %s kernel for dtype %d, semantics %d, degree %d, nquad %d",
-                op == FEMTC_OP_MASS ? "mass" : (op == FEMTC_OP_STIFFNESS ? "stiffness" : "Helmholtz"),
-                dtype, sem, degree,
-                nquad);
+                names[op], dtype, sem, degree, nquad);
   *out = v;
   return FEMTC_OK;
 }
@@ -512,18 +539,23 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
   p.sq = cfg.sq;
   p.sbc = cfg.sbc;
   p.host_io = host_io;
-  const int ntab = (v.op != FEMTC_OP_MASS) ? 2 : 1;
+  const int ntab = (op_base(v.op) != FEMTC_OP_MASS) ? 2 : 1;
+  const bool affine = op_affine(v.op);
+  const ST* wq = tables + 2 * v.n * v.q; // affine forms: the Q weights
   if (v.eo)
   {
-    // even-odd tables: Phi, Gamma forward (Q x N), Phi^T, Gamma^T (N x Q),
+    // even-odd tables: Phi, Gamma forward (Q x N), Phi^T, Gamma^T (N x Q)
+    // (affine forms: of the weighted tables w(q) Phi(q,i), w(q) Gamma(q,i)),
     // formed in the storage precision, then in the launch's form
     for (int t = 0; t < ntab; ++t)
     {
       const ST* a = tables + t * v.n * v.q;
       const int sig = t == 0 ? 1 : -1;
-      ST f[kMaxQ * kMaxN], b[kMaxQ * kMaxN];
+      ST f[kMaxQ * kMaxN], b[kMaxQ * kMaxN], aw[kMaxQ * kMaxN];
+      for (int i = 0; i < v.n * v.q; ++i)
+        aw[i] = affine ? (ST)(a[i] * wq[i % v.q]) : a[i];
       host_eo_table<ST>(a, v.q, v.n, 1, v.q, sig, f);
-      host_eo_table<ST>(a, v.n, v.q, v.q, 1, sig, b);
+      host_eo_table<ST>(aw, v.n, v.q, v.q, 1, sig, b);
       for (int i = 0; i < v.n * v.q; ++i)
       {
         p.tab[t][i] = param_value<T>(f[i]);
@@ -534,7 +566,12 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
   else
     for (int t = 0; t < ntab; ++t)
       for (int i = 0; i < v.n * v.q; ++i)
+      {
         p.tab[t][i] = param_value<T>(tables[t * v.n * v.q + i]);
+        // affine forms: backward tables w(q) A(q,i) in the same layout
+        if (affine)
+          p.tab[2 + t][i] = param_value<T>((ST)(tables[t * v.n * v.q + i] * wq[i % v.q]));
+      }
   const unsigned smem = smem_of(v, cfg);
   int blocks = 0;
   int rc = prepare(v.fn, smem, cfg.nt, &blocks);
@@ -735,7 +772,8 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
   }
   const size_t es = elem_size(dtype);
   const size_t n3 = (size_t)v->n * v->n * v->n;
-  const size_t q3 = (size_t)v->q * v->q * v->q * geo_nc(op);
+  // geometry values per cell: per quadrature point, or one set (affine)
+  const size_t q3 = op_affine(op) ? (size_t)cell_nc(op) : (size_t)v->q * v->q * v->q * geo_nc(op);
   const size_t bu = ncells * n3 * es, bg = ncells * q3 * es;
   if ((rc = host_buffer(0, bu)) != FEMTC_OK ||
       (rc = host_buffer(1, bu)) != FEMTC_OK ||
@@ -960,6 +998,25 @@ int femtc_helmholtz_apply(int dtype, int degree, int nquad, const void* tables,
                ncells, stream);
 }
 
+int femtc_affine_apply(int op, int dtype, int degree, int nquad, const void* tables,
+                       const void* u, void* y, const void* cgeo, size_t ncells,
+                       void* stream)
+{
+  if (op != FEMTC_OP_MASS_AFFINE && op != FEMTC_OP_STIFFNESS_AFFINE)
+    return fail(FEMTC_ERR_INVALID, "affine apply: op must be FEMTC_OP_MASS_AFFINE or "
+                                   "FEMTC_OP_STIFFNESS_AFFINE (got %d)", op);
+  return apply(op, dtype, FEMTC_EXACT, degree, nquad, tables, u, y, cgeo, ncells, stream);
+}
+
+int femtc_affine_apply_host(int op, int dtype, int degree, int nquad, const void* tables,
+                            const void* u, void* y, const void* cgeo, size_t ncells)
+{
+  if (op != FEMTC_OP_MASS_AFFINE && op != FEMTC_OP_STIFFNESS_AFFINE)
+    return fail(FEMTC_ERR_INVALID, "affine apply: op must be FEMTC_OP_MASS_AFFINE or "
+                                   "FEMTC_OP_STIFFNESS_AFFINE (got %d)", op);
+  return apply_host(op, dtype, FEMTC_EXACT, degree, nquad, tables, u, y, cgeo, ncells);
+}
+
 int femtc_mass_apply_host(int dtype, int semantics, int degree, int nquad,
                           const void* tables, const void* u, void* y,
                           const void* dw, size_t ncells)
@@ -1124,7 +1181,7 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
     const CellVariant* lv = find_cell(op, dtype, semantics, degree + 1, nquad, lanes);
     if (!lv)
       continue;
-    for (int staged = 0; staged <= 1; ++staged)
+    for (int staged = 0; staged <= (geo_nc(op) > 0 ? 1 : 0); ++staged)
       for (int nt : {64, 128, 256})
       {
         std::vector<std::pair<double, TileCfg>> opts;

@@ -11,6 +11,10 @@ shapes and value distributions of the benchmark workloads:
   stiffness_p6 : P=6, Q=8, 131072 cells, same geometry, u ~ N(0,1) plus
                  sin(pi x) sin(pi y) sin(pi z) at the cell's GLL nodes
 
+make_affine(name) gives the same degree, Q and cell count on affine cells
+(J = I + 0.1 N(0,1) per cell, u ~ U(-1,1)) with one geometry set per cell:
+detJ (mass) or detJ J^-1 J^-T (stiffness), for the affine operator forms.
+
 Layouts follow include/femtc_gpu.h.  Seeds are fixed per workload.
 """
 from __future__ import annotations
@@ -31,8 +35,34 @@ class Workload:
     ncells: int
     tables: np.ndarray  # FP64, 2*Q*N
     u: np.ndarray       # FP64 [ncells, N^3]
-    geo: np.ndarray     # FP64 mass [ncells, Q^3]; stiffness [ncells, Q^3, 6]
+    geo: np.ndarray     # FP64 mass [ncells, Q^3]; stiffness [ncells, Q^3, 6];
+                        # affine forms: [ncells] or [ncells, 6]
     seed: int
+    weights: np.ndarray | None = None  # affine forms: the Q 1D quadrature weights
+
+    @property
+    def affine(self) -> bool:
+        return self.op in (_lib.MASS_AFFINE, _lib.STIFFNESS_AFFINE)
+
+    @property
+    def base_op(self) -> int:
+        """MASS or STIFFNESS: the operator the workload applies."""
+        return self.op - _lib.MASS_AFFINE if self.affine else self.op
+
+    def op_tables(self) -> np.ndarray:
+        """The tables the library's entry point for this workload takes."""
+        return _lib.affine_tables(self.tables, self.weights) if self.affine else self.tables
+
+    def point_geometry(self, k: int | None = None) -> np.ndarray:
+        """Per-point factors of the first k cells (all by default): the
+        geometry the per-point operator takes for the same action."""
+        g = self.geo[:k]
+        if not self.affine:
+            return g
+        w3 = tensor_weights(self.weights)
+        if self.base_op == _lib.MASS:
+            return np.ascontiguousarray(g[:, None] * w3[None])
+        return np.ascontiguousarray(g[:, None, :] * w3[None, :, None])
 
     @property
     def n(self) -> int:
@@ -68,17 +98,39 @@ def geometry_from_jacobians(J: np.ndarray, w3: np.ndarray) -> np.ndarray:
     return comps[:, None, :] * w3[None, :, None]
 
 
-def make(name: str, ncells: int | None = None, seed: int | None = None) -> Workload:
+def _spec(name: str):
+    """(degree, nquad, op, cells, seed) of a named workload."""
     if name == "mass_p3":
-        degree, nquad, op, nc, sd = 3, 5, _lib.MASS, 4096, 1001
-    elif name == "stiffness_p4":
-        degree, nquad, op, nc, sd = 4, 6, _lib.STIFFNESS, 32768, 1002
-    elif name == "stiffness_p6":
-        degree, nquad, op, nc, sd = 6, 8, _lib.STIFFNESS, 131072, 1003
-    else:
-        raise ValueError(f"unknown workload {name}")
+        return 3, 5, _lib.MASS, 4096, 1001
+    if name == "stiffness_p4":
+        return 4, 6, _lib.STIFFNESS, 32768, 1002
+    if name == "stiffness_p6":
+        return 6, 8, _lib.STIFFNESS, 131072, 1003
+    raise ValueError(f"unknown workload {name}")
+
+
+def make(name: str, ncells: int | None = None, seed: int | None = None) -> Workload:
+    degree, nquad, op, nc, sd = _spec(name)
     return make_custom(name, op, degree, nquad, ncells or nc, sd if seed is None else seed,
                        smooth=(name == "stiffness_p6"))
+
+
+def make_affine(name: str, ncells: int | None = None, seed: int | None = None) -> Workload:
+    """The named workload's degree, Q and cell count on affine cells, with
+    one geometry set per cell (the affine operator forms)."""
+    degree, nquad, op, nc, sd = _spec(name)
+    ncells = ncells or nc
+    rng = np.random.default_rng(sd if seed is None else seed)
+    tables, _, w, _ = _lib.tabulate(degree, nquad)
+    J = random_jacobians(rng, ncells)
+    if op == _lib.MASS:
+        geo, aop = np.linalg.det(J), _lib.MASS_AFFINE
+    else:
+        geo = geometry_from_jacobians(J, np.ones(1)).reshape(ncells, 6)
+        aop = _lib.STIFFNESS_AFFINE
+    u = rng.uniform(-1.0, 1.0, size=(ncells, (degree + 1) ** 3))
+    return Workload(name + "_affine", aop, degree, nquad, ncells, tables, np.ascontiguousarray(u),
+                    np.ascontiguousarray(geo), sd if seed is None else seed, weights=w)
 
 
 def make_custom(name: str, op: int, degree: int, nquad: int, ncells: int, seed: int,

@@ -62,7 +62,9 @@ typedef enum
 {
   FEMTC_OP_MASS = 0,
   FEMTC_OP_STIFFNESS = 1,
-  FEMTC_OP_HELMHOLTZ = 2 /* alpha M + beta K in one pass (femtc_helmholtz_apply) */
+  FEMTC_OP_HELMHOLTZ = 2, /* alpha M + beta K in one pass (femtc_helmholtz_apply) */
+  FEMTC_OP_MASS_AFFINE = 3,     /* mass, one detJ per cell (femtc_affine_apply) */
+  FEMTC_OP_STIFFNESS_AFFINE = 4 /* stiffness, one G per cell (femtc_affine_apply) */
 } femtc_op;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -124,6 +126,29 @@ int femtc_helmholtz_apply(int dtype, int degree, int nquad, const void* tables,
 int femtc_helmholtz_geometry(int nquad, double alpha, const void* dw,
                              double beta, const void* G, void* geo8,
                              size_t ncells, void* stream);
+
+/* Affine cells (parallelepipeds): J is constant over a cell, so the
+ * geometry is one set of factors per cell instead of Q^3 per point.
+ * op FEMTC_OP_MASS_AFFINE: cgeo [ncells] = detJ; FEMTC_OP_STIFFNESS_AFFINE:
+ * cgeo [ncells][6] = detJ J^-1 J^-T as [zz,yz,xz,yy,xy,xx].  tables (host):
+ * Phi (Q x N), Gamma (Q x N), then the Q 1D quadrature weights w, in the
+ * dtype's table type (FP64 or FP32).  The result equals femtc_mass_apply /
+ * femtc_stiffness_apply (exact semantics) with the per-point factors
+ * dw[c][q0][q1][q2] = w(q0) w(q1) w(q2) detJ[c] and
+ * G[c][q0][q1][q2][k] = w(q0) w(q1) w(q2) cgeo[c][k], up to rounding: the
+ * weights are folded into the backward contractions' tables.  The geometry
+ * stream shrinks from 8*6Q^3 to 48 bytes per cell (stiffness, FP64).
+ * femtc_geometry(dtype, 1, &one, J, 0, detJ, G, ncells, stream) with
+ * one = 1.0 computes cgeo from per-cell Jacobians.  FEMTC_F64 and
+ * FEMTC_F32, degree 1..7, nquad in degree+1..degree+3.  No reference
+ * counterpart: the reference takes per-point factors (src/mass.hpp:10-12,
+ * src/stiffness.hpp:34-36).  u, y, cgeo: device pointers, 16-byte aligned. */
+int femtc_affine_apply(int op, int dtype, int degree, int nquad, const void* tables,
+                       const void* u, void* y, const void* cgeo, size_t ncells,
+                       void* stream);
+/* The same with host buffers (as femtc_mass_apply_host). */
+int femtc_affine_apply_host(int op, int dtype, int degree, int nquad, const void* tables,
+                            const void* u, void* y, const void* cgeo, size_t ncells);
 
 /* Host-buffer forms of mass and stiffness: every pointer is host memory
  * (pinned memory copies fastest).  Copies u and dw/G to the device, applies

@@ -110,6 +110,44 @@ def test_helmholtz_supported_and_rejected(femtc):
     assert lib.femtc_helmholtz_geometry(4, 1.0, 16, 1.0, 16, 24, 1, None) == -1  # misaligned
 
 
+def test_affine_supported_and_rejected(femtc):
+    """Affine forms: FP64 and FP32, exact semantics, degree 1..7 with Q in
+    N..N+2; other forms and bad arguments rejected before any device work."""
+    lib = femtc.load()
+    for op in (femtc.MASS_AFFINE, femtc.STIFFNESS_AFFINE):
+        for P in range(1, 8):
+            for Q in (P + 1, P + 2, P + 3):
+                for dt in (femtc.F64, femtc.F32):
+                    assert femtc.supported(op, dt, femtc.EXACT, P, Q)
+            assert not femtc.supported(op, femtc.F64, femtc.REFERENCE, P, P + 1)
+            assert not femtc.supported(op, femtc.F16X2, femtc.EXACT, P, P + 1)
+    t = np.zeros(128)
+    # the per-point operators are not affine forms
+    assert lib.femtc_affine_apply(femtc.MASS, femtc.F64, 3, 4, t.ctypes.data, 16, 16, 16, 1,
+                                  None) == -1
+    assert lib.femtc_affine_apply_host(femtc.STIFFNESS, femtc.F64, 3, 4, t.ctypes.data, 16, 16,
+                                       16, 1) == -1
+    assert lib.femtc_affine_apply(femtc.MASS_AFFINE, femtc.F16X2, 3, 4, t.ctypes.data, 16, 16,
+                                  16, 1, None) == -2
+    assert lib.femtc_affine_apply(femtc.STIFFNESS_AFFINE, femtc.F64, 3, 4, t.ctypes.data, None,
+                                  16, 16, 1, None) == -1
+    with pytest.raises(ValueError):
+        femtc.apply(femtc.MASS_AFFINE, femtc.F64, femtc.REFERENCE, 3, 4, t, 16, 16, 16, 1)
+
+
+def test_affine_even_odd_selection(femtc):
+    """Affine forms run the even-odd kernels when the tables and the
+    weights are symmetric: tabulated tables with Gauss weights yes, with
+    asymmetric weights no."""
+    t, _, w, _ = femtc.tabulate(4, 6)
+    at = femtc.affine_tables(t, w)
+    for op in (femtc.MASS_AFFINE, femtc.STIFFNESS_AFFINE):
+        for dt in (femtc.F64, femtc.F32):
+            assert femtc.even_odd_used(op, dt, femtc.EXACT, 4, 6, at)
+            skew = femtc.affine_tables(t, w * np.linspace(0.9, 1.1, w.size))
+            assert not femtc.even_odd_used(op, dt, femtc.EXACT, 4, 6, skew)
+
+
 def test_even_odd_selection(femtc):
     """Host-side choice of the even-odd kernels: FP64 exact with the
     tabulated (symmetric) tables, not with random tables, not for FP32, not

@@ -200,15 +200,41 @@ struct CellLayout
   __host__ __device__ unsigned g(int s) const { return g0 + (unsigned)s * stage; }
 };
 
+// Worst bank conflict (ways) of one quarter-warp phase of 16-byte accesses
+// by 8 lanes to 8 consecutive packed slabs of n*n values: lanes whose slab
+// starts fall on the same 16-byte slot of a 128-byte bank row collide.
+template <typename T>
+__host__ __device__ constexpr int packed_slab_conflict(int n)
+{
+  const int s = n * n * (int)sizeof(T);
+  int worst = 0;
+  for (int a = 0; a < 8; ++a)
+  {
+    int c = 0;
+    for (int b = 0; b < 8; ++b)
+      c += ((a * s) % 128) == ((b * s) % 128) ? 1 : 0;
+    worst = c > worst ? c : worst;
+  }
+  return worst;
+}
+
+// Ways of conflict accepted on the slab loads and stores in exchange for
+// one bulk copy per tile: the slab accesses are a small part of a tile's
+// shared-memory traffic, while a padded layout needs one TMA copy per slab
+// (128 copies of 64 bytes per tile of 32 FP32 cells at N = 4).
+constexpr int kMaxSlabConflict = 4;
+
 // Shared-memory stride (elements) of one i0 slab (N*N values) of the DOF and
-// output stages.  Odd N: slabs are packed (the tile is one contiguous bulk
-// copy, and the odd slab stride is bank-conflict free).  Even N: every slab
-// is its own bulk copy into a slot whose byte size is an odd multiple of 16,
-// read and written with 16-byte vector accesses (conflict free per phase).
+// output stages.  Packed (N*N: the tile is one contiguous bulk copy) when N
+// is odd (odd strides are conflict free) or when the packed slabs' 16-byte
+// accesses conflict at most kMaxSlabConflict ways; else every slab is its
+// own bulk copy into a slot whose byte size is an odd multiple of 16
+// (conflict free per phase).
 template <typename T>
 __host__ __device__ constexpr int slab_stride(int n)
 {
-  if (n % 2 == 1)
+  if (n % 2 == 1 || (n * n * (int)sizeof(T)) % 16 != 0 ||
+      packed_slab_conflict<T>(n) <= kMaxSlabConflict)
     return n * n;
   int units = (n * n * (int)sizeof(T) + 15) / 16;
   if (units % 2 == 0)
@@ -590,8 +616,12 @@ struct SlabTile
 {
   using ST = storage_t<T>; // staged u, y and geometry; T is the arithmetic
   static constexpr int S = LANES;
-  static constexpr bool kSlabCopies = (N % 2 == 0);
   static constexpr int US = slab_stride<ST>(N);
+  // padded slots: one bulk copy per slab; packed slabs: one per tile
+  static constexpr bool kSlabCopies = (US != N * N);
+  // slabs of whole 16-byte vectors: vector loads and stores (16-byte
+  // aligned slots, packed or padded)
+  static constexpr bool kVecSlab = (N * N * sizeof(ST)) % 16 == 0;
   static constexpr int N2 = N * N, Q2 = Q * Q, Q3 = Q * Q * Q;
   // the gradient passes: stiffness and Helmholtz (the latter exact only)
   static constexpr bool kGrad = (op_base(OP) != OP_MASS);
@@ -631,7 +661,7 @@ struct SlabTile
   static __device__ __forceinline__ void load_slab(const ST* __restrict__ src,
                                                    T (&x)[N2])
   {
-    if constexpr (kSlabCopies)
+    if constexpr (kVecSlab)
     {
       using V = typename std::conditional<sizeof(ST) == 4, float4, double2>::type;
       constexpr int W = 16 / sizeof(ST);
@@ -656,7 +686,7 @@ struct SlabTile
   static __device__ __forceinline__ void store_slab(ST* __restrict__ dst,
                                                     const T (&x)[N2])
   {
-    if constexpr (kSlabCopies)
+    if constexpr (kVecSlab)
     {
       using V = typename std::conditional<sizeof(ST) == 4, float4, double2>::type;
       constexpr int W = 16 / sizeof(ST);

@@ -75,6 +75,7 @@ def _declare(lib: ctypes.CDLL) -> None:
                               ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_longlong)], c_int),
         "femtc_batch_layout": ([vp, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
         "femtc_batch_threads": ([vp], c_int),
+        "femtc_batch_plan": ([vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
         "femtc_batch_destroy": ([vp], None),
         "femtc_batch_apply_static": ([c_int, vp, c_int, vp], c_int),
         "femtc_solve_bytes": ([c_int, c_int, c_size], c_size),
@@ -336,6 +337,7 @@ class BatchItem(ctypes.Structure):
 
 
 BATCH_TUNE = 1
+BATCH_SPLIT = 2
 
 
 def batch_apply_static(dtype: int, meshes, stream=None) -> None:
@@ -355,9 +357,11 @@ class Batch:
 
     meshes: iterable of (op, degree, nquad, tables, u, y, geo, ncells) with
     device tensors; the tables are kept alive here until the batch is built.
+    tune: tile shapes measured on the meshes, and the split plan where it is
+    faster (femtc_batch_plan); split: the split plan in any case.
     """
 
-    def __init__(self, dtype: int, meshes, tune: bool = False):
+    def __init__(self, dtype: int, meshes, tune: bool = False, split: bool = False):
         lib = load()
         self._tabs = [host_tables(m[3], dtype) for m in meshes]
         arr = (BatchItem * len(self._tabs))()
@@ -367,7 +371,8 @@ class Batch:
                                ptr(geo), ncells)
         h = ctypes.c_void_p()
         check(lib.femtc_batch_create(dtype, ctypes.cast(arr, ctypes.c_void_p), len(self._tabs),
-                                     BATCH_TUNE if tune else 0, ctypes.byref(h)))
+                                     (BATCH_TUNE if tune else 0) | (BATCH_SPLIT if split else 0),
+                                     ctypes.byref(h)))
         self.handle = h
 
     def launch(self, stream=None) -> None:
@@ -382,8 +387,10 @@ class Batch:
                                       ctypes.byref(smem), ctypes.byref(nd)))
         threads = load().femtc_batch_threads(self.handle)
         check(min(threads, 0))
+        kern, solo = ctypes.c_int(), ctypes.c_int()
+        check(load().femtc_batch_plan(self.handle, ctypes.byref(kern), ctypes.byref(solo)))
         return {"tiles": nt.value, "ctas": ctas.value, "threads": threads, "smem": smem.value,
-                "dofs": nd.value}
+                "dofs": nd.value, "batch_kernels": kern.value, "single_launches": solo.value}
 
     def layout(self, op: int, degree: int):
         cb, st = ctypes.c_int(), ctypes.c_int()

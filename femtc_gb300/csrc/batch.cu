@@ -10,7 +10,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <queue>
 #include <vector>
 
@@ -321,10 +323,22 @@ int batch_plan(femtc_batch* b, const std::vector<BatchLayout>& lay,
   b->smem = 128 + 2 * (su + sg) + su + sw;
   if (b->smem > kBatchSmemCap)
     return aux_fail(FEMTC_ERR_INVALID, "batch: tile stages exceed shared memory");
-  cudaError_t e = cudaFuncSetAttribute(fam.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)b->smem);
-  if (e != cudaSuccess)
-    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  {
+    // the kernel's shared-memory limit only grows: batches (and the parts of
+    // a split batch) built earlier keep launching with their own sizes
+    static std::mutex m;
+    static std::map<const void*, unsigned> limit;
+    std::lock_guard<std::mutex> lk(m);
+    unsigned& cur = limit[fam.fn];
+    if (b->smem > cur)
+    {
+      cudaError_t e = cudaFuncSetAttribute(fam.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)b->smem);
+      if (e != cudaSuccess)
+        return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+      cur = b->smem;
+    }
+  }
   int per_sm = 0, dev = 0, sms = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fam.fn, b->threads, b->smem);
   cudaGetDevice(&dev);
@@ -432,8 +446,34 @@ int build(femtc_batch* b, const std::vector<BatchLayout>& lay)
   return FEMTC_OK;
 }
 
+int launch_solo(int dtype, const femtc_batch::Solo& s, cudaStream_t st)
+{
+  const femtc_batch_item& it = s.it;
+  return it.op == FEMTC_OP_MASS
+             ? femtc_mass_apply(dtype, FEMTC_EXACT, it.degree, it.nquad, s.tab.data(), it.u,
+                                it.y, it.geo, it.ncells, st)
+             : femtc_stiffness_apply(dtype, FEMTC_EXACT, it.degree, it.nquad, s.tab.data(),
+                                     it.u, it.y, it.geo, it.ncells, st);
+}
+
 int launch_eager(femtc_batch* b, cudaStream_t st)
 {
+  if (!b->parts.empty() || !b->solo.empty())
+  {
+    for (auto& p : b->parts)
+    {
+      const int rc = launch_eager(p.get(), st);
+      if (rc != FEMTC_OK)
+        return rc;
+    }
+    for (const auto& s : b->solo)
+    {
+      const int rc = launch_solo(b->dtype, s, st);
+      if (rc != FEMTC_OK)
+        return rc;
+    }
+    return FEMTC_OK;
+  }
   void* args[] = {&b->params};
   cudaError_t e = cudaLaunchKernel(b->fam->fn, dim3((unsigned)b->grid), dim3((unsigned)b->threads),
                                    args, b->smem, st);
@@ -564,6 +604,118 @@ void tune(femtc_batch* b, std::vector<BatchLayout>& lay)
   cudaStreamSynchronize(st);
   cudaStreamDestroy(st);
 }
+
+// Mean time (ms) of `reps` runs of `run` on st, after one untimed run.
+template <typename F>
+float time_runs(F run, cudaStream_t st, int reps)
+{
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  run();
+  cudaEventRecord(e0, st);
+  for (int r = 0; r < reps; ++r)
+    run();
+  cudaEventRecord(e1, st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms / reps;
+}
+
+// Split plan: one kernel over the whole mix sizes its shared memory and
+// registers for the largest variant present, so small variants run at the
+// occupancy of the largest; and the largest meshes run as fast alone, where
+// a launch's overhead is negligible.  For every variant present, time (a)
+// a batch of its meshes alone, tuned, and (b) its meshes as single-mesh
+// launches with tiles autotuned on the largest; keep the faster of each.
+// The split plan replaces the one-kernel plan when the whole of it is
+// faster.  The y buffers are overwritten.
+void plan_split(femtc_batch* b, bool force)
+{
+  cudaStream_t st;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+    return;
+  const float t_full = time_launches(b, st, 3);
+  std::vector<std::unique_ptr<femtc_batch>> parts;
+  std::vector<femtc_batch::Solo> solo;
+  bool ok = true;
+  for (int v = 0; v < kBatchVariants && ok; ++v)
+  {
+    std::vector<femtc_batch_item> mine;
+    for (const auto& it : b->items)
+      if (batch_variant(it.op, it.degree + 1) == v)
+        mine.push_back(it);
+    if (mine.empty())
+      continue;
+    auto s = std::make_unique<femtc_batch>();
+    if (batch_setup(s.get(), b->dtype, mine.data(), (int)mine.size(), "batch") != FEMTC_OK)
+    {
+      ok = false;
+      break;
+    }
+    s->threads = default_threads(*s->fam);
+    std::vector<BatchLayout> lay = batch_default_layouts(*s->fam, s->threads, s->items);
+    tune(s.get(), lay);
+    if (build(s.get(), lay) != FEMTC_OK)
+    {
+      ok = false;
+      break;
+    }
+    const float tb = time_launches(s.get(), st, 3);
+    std::vector<femtc_batch::Solo> ms;
+    size_t big = 0;
+    for (size_t i = 0; i < mine.size(); ++i)
+    {
+      const femtc_batch_item& it = mine[i];
+      const size_t ntab = 2 * (size_t)it.nquad * (it.degree + 1);
+      const float* t = static_cast<const float*>(it.tables);
+      ms.push_back({it, std::vector<float>(t, t + ntab)});
+      if (it.ncells > mine[big].ncells)
+        big = i;
+    }
+    float ts = 1e30f;
+    int cb = 0, staged = 0, nt = 0;
+    float tune_ms = 0.f;
+    const femtc_batch_item& bi = mine[big];
+    if (femtc_autotune(bi.op, b->dtype, FEMTC_EXACT, bi.degree, bi.nquad, ms[big].tab.data(),
+                       bi.u, bi.y, bi.geo, bi.ncells, st, &cb, &staged, &nt, &tune_ms) ==
+        FEMTC_OK)
+    {
+      bool run_ok = true;
+      ts = time_runs(
+          [&] {
+            for (const auto& m : ms)
+              run_ok = launch_solo(b->dtype, m, st) == FEMTC_OK && run_ok;
+          },
+          st, 3);
+      if (!run_ok)
+        ts = 1e30f;
+    }
+    if (ts < tb)
+      solo.insert(solo.end(), ms.begin(), ms.end());
+    else
+      parts.push_back(std::move(s));
+  }
+  if (ok)
+  {
+    femtc_batch trial;
+    trial.dtype = b->dtype;
+    trial.parts = std::move(parts);
+    trial.solo = std::move(solo);
+    const float t_split = time_runs([&] { launch_eager(&trial, st); }, st, 3);
+    if (force || t_split < t_full)
+    {
+      b->parts = std::move(trial.parts);
+      b->solo = std::move(trial.solo);
+    }
+  }
+  cudaGetLastError();
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+}
 } // namespace
 } // namespace femtc
 
@@ -587,6 +739,8 @@ int femtc_batch_create(int dtype, const femtc_batch_item* items, int nitems,
   rc = build(b.get(), lay);
   if (rc != FEMTC_OK)
     return rc;
+  if (flags & (FEMTC_BATCH_TUNE | FEMTC_BATCH_SPLIT))
+    plan_split(b.get(), (flags & FEMTC_BATCH_SPLIT) != 0);
   rc = capture(b.get());
   if (rc != FEMTC_OK)
     return rc;
@@ -614,14 +768,42 @@ int femtc_batch_info(const femtc_batch* b, long long* ntiles, int* ctas,
 {
   if (!b)
     return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
+  long long nt = b->ntiles;
+  int grid = b->grid;
+  unsigned smem = b->smem;
+  if (!b->parts.empty() || !b->solo.empty())
+  {
+    // split plan: tiles of the batch kernels plus one per single-mesh launch
+    nt = (long long)b->solo.size();
+    grid = 0;
+    smem = 0;
+    for (const auto& p : b->parts)
+    {
+      nt += p->ntiles;
+      grid = std::max(grid, p->grid);
+      smem = std::max(smem, p->smem);
+    }
+  }
   if (ntiles)
-    *ntiles = b->ntiles;
+    *ntiles = nt;
   if (ctas)
-    *ctas = b->grid;
+    *ctas = grid;
   if (smem_bytes)
-    *smem_bytes = (int)b->smem;
+    *smem_bytes = (int)smem;
   if (ndofs)
     *ndofs = b->ndofs;
+  return FEMTC_OK;
+}
+
+int femtc_batch_plan(const femtc_batch* b, int* kernels, int* single_launches)
+{
+  if (!b)
+    return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
+  const bool split = !b->parts.empty() || !b->solo.empty();
+  if (kernels)
+    *kernels = split ? (int)b->parts.size() : 1;
+  if (single_launches)
+    *single_launches = (int)b->solo.size();
   return FEMTC_OK;
 }
 
@@ -630,11 +812,22 @@ int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
 {
   if (!b || degree < 1 || degree > kBatchDegrees || (op != 0 && op != 1))
     return aux_fail(FEMTC_ERR_INVALID, "batch: bad layout query");
-  const BatchLayout& l = b->params.lay[batch_variant(op, degree + 1)];
+  const int v = batch_variant(op, degree + 1);
+  const femtc_batch* owner = b;
+  if (!b->parts.empty() || !b->solo.empty())
+  {
+    // split plan: the batch kernel that holds the variant; 0 cells for a
+    // variant run by single-mesh launches
+    owner = nullptr;
+    for (const auto& p : b->parts)
+      for (const auto& it : p->items)
+        if (batch_variant(it.op, it.degree + 1) == v)
+          owner = p.get();
+  }
   if (cb)
-    *cb = l.cb;
+    *cb = owner ? owner->params.lay[v].cb : 0;
   if (geo_staged)
-    *geo_staged = l.staged;
+    *geo_staged = owner ? owner->params.lay[v].staged : 0;
   return FEMTC_OK;
 }
 
@@ -642,7 +835,16 @@ int femtc_batch_threads(const femtc_batch* b)
 {
   if (!b)
     return aux_fail(FEMTC_ERR_INVALID, "batch: not created");
-  return b->threads;
+  if (!b->parts.empty())
+  {
+    // split plan: the CTA size of the batch kernel with the most tiles
+    const femtc_batch* top = b->parts[0].get();
+    for (const auto& p : b->parts)
+      if (p->ntiles > top->ntiles)
+        top = p.get();
+    return top->threads;
+  }
+  return b->solo.empty() ? b->threads : 0;
 }
 
 void femtc_batch_destroy(femtc_batch* b) { delete b; }

@@ -6,10 +6,19 @@
 
 #include "batch_kernel.cuh"
 
+#include <memory>
 #include <vector>
 
 struct femtc_batch
 {
+  // A mesh run by the library's single-mesh operator kernels inside the
+  // batch's graph (split plan), with its own copy of the tables.
+  struct Solo
+  {
+    femtc_batch_item it;
+    std::vector<float> tab;
+  };
+
   int dtype = 0;
   const femtc::BatchKernelInfo* fam = nullptr;
   std::vector<femtc_batch_item> items;
@@ -25,6 +34,12 @@ struct femtc_batch
   cudaStream_t cap_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // Split plan (chosen by the tuner when faster than one kernel over the
+  // whole mix): one batch kernel per variant whose meshes run best
+  // persistent, and single-mesh launches for the variants whose meshes are
+  // large enough to run best alone.  Empty: the one-kernel plan above.
+  std::vector<std::unique_ptr<femtc_batch>> parts;
+  std::vector<Solo> solo;
 
   ~femtc_batch()
   {

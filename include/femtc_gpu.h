@@ -273,6 +273,9 @@ int femtc_geometry(int out_dtype, int nquad, const double* weights,
  * batch's own buffers at creation (the y buffers are overwritten).
  * ---------------------------------------------------------------------- */
 #define FEMTC_BATCH_TUNE 1
+/* Take the tuner's split plan (see femtc_batch_plan) even when the one-kernel
+ * plan measured faster. */
+#define FEMTC_BATCH_SPLIT 2
 
 typedef struct
 {
@@ -298,8 +301,18 @@ int femtc_batch_info(const femtc_batch* b, long long* ntiles, int* ctas,
                      int* smem_bytes, long long* ndofs);
 int femtc_batch_layout(const femtc_batch* b, int op, int degree, int* cb,
                        int* geo_staged);
-/* Threads per CTA of the batch's launch (built-in or chosen by the tuner). */
+/* Threads per CTA of the batch's launch (built-in or chosen by the tuner;
+ * split plan: of its batch kernel with the most tiles, 0 when it has none). */
 int femtc_batch_threads(const femtc_batch* b);
+/* The batch's plan.  Without FEMTC_BATCH_TUNE: one persistent kernel over
+ * every mesh (kernels = 1, single_launches = 0).  With it the tuner may
+ * split the graph: one persistent kernel per (degree, operator) whose
+ * meshes run faster batched, and single-mesh operator launches for the
+ * variants whose meshes run faster alone (large meshes, where a launch's
+ * overhead is negligible) -- whichever whole plan measured faster.  The
+ * graph is still one femtc_batch_launch.  femtc_batch_layout reports 0
+ * cells for variants run by single-mesh launches. */
+int femtc_batch_plan(const femtc_batch* b, int* kernels, int* single_launches);
 void femtc_batch_destroy(femtc_batch* b);
 
 /* The batched launch for callers that cannot allocate device memory (code

@@ -17,7 +17,7 @@ unsigned cell_smem_bytes(int cb, int staged, int sq, int sbc)
   p.geo_staged = staged;
   p.sq = sq;
   p.sbc = sbc;
-  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L, EVOD>, N, Q, geo_nc(OP)>(p)
+  return tile_layout<T, SlabTile<T, N, Q, OP, SEM, L, EVOD, true>, N, Q, geo_nc(OP)>(p)
       .total;
 }
 

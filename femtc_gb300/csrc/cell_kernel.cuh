@@ -32,6 +32,8 @@
 #include "common.cuh"
 #include "df64.cuh"
 
+#include <cuda.h> // CUtensorMap (the type only)
+
 #include <type_traits>
 
 namespace femtc
@@ -129,6 +131,13 @@ template <typename T>
 struct CellParams
 {
   using ST = storage_t<T>;
+  // Padded DOF/output slab slots (see slot_stride) move by 2D tensor copies
+  // when tma_rows > 0: u and y as [ncells*N rows][N*N] with boxes of
+  // [tma_rows rows][slot] (the slot's padding columns lie outside the
+  // tensor: zeros in, not written out).  tma_rows == 0: one bulk copy per
+  // slab.
+  CUtensorMap tmu, tmy;
+  int tma_rows;
   const ST* u;       // [ncells][N^3]
   ST* y;             // [ncells][N^3]
   const ST* geo;     // [ncells][Q^3][geo_nc(op)] (mass: [ncells][Q^3])
@@ -179,7 +188,8 @@ struct Shape
 
 // Byte offsets of the shared-memory regions (identical on host and device):
 // two mbarriers, two (DOF slab, geometry slab) stages, the output slab, and
-// the kernel family's work buffers.  Every region starts 16-byte aligned.
+// the kernel family's work buffers.  The DOF, geometry and output regions
+// start 128-byte aligned (tensor copies), the work buffers 16-byte aligned.
 struct CellLayout
 {
   unsigned u0, g0, u1, g1, y, w, total;
@@ -187,18 +197,34 @@ struct CellLayout
   // ns stages (2 for the CTA-wide loop, more for the warp-split one)
   __host__ __device__ CellLayout(unsigned bu, unsigned bg, unsigned bw, int ns = 2)
   {
-    stage = bu + bg;
+    const unsigned au = (bu + 127u) & ~127u, ag = (bg + 127u) & ~127u;
+    stage = au + ag;
     u0 = 128; // the mbarriers live in the first 128 bytes
-    g0 = u0 + bu;
+    g0 = u0 + au;
     u1 = u0 + stage;
-    g1 = u1 + bu;
+    g1 = u1 + au;
     y = u0 + (unsigned)ns * stage;
-    w = y + bu;
+    w = y + au;
     total = w + ((bw + 15u) & ~15u);
   }
   __host__ __device__ unsigned u(int s) const { return u0 + (unsigned)s * stage; }
   __host__ __device__ unsigned g(int s) const { return g0 + (unsigned)s * stage; }
 };
+
+// Slot stride (elements) of one i0 slab in conflict-free form: packed for
+// odd N (odd strides are conflict free), else the smallest slot whose byte
+// size is an odd multiple of 16, read and written with 16-byte vector
+// accesses (conflict free per quarter-warp phase).
+template <typename T>
+__host__ __device__ constexpr int slot_stride(int n)
+{
+  if (n % 2 == 1)
+    return n * n;
+  int units = (n * n * (int)sizeof(T) + 15) / 16;
+  if (units % 2 == 0)
+    ++units;
+  return units * 16 / (int)sizeof(T);
+}
 
 // Worst bank conflict (ways) of one quarter-warp phase of 16-byte accesses
 // by 8 lanes to 8 consecutive packed slabs of n*n values: lanes whose slab
@@ -225,21 +251,18 @@ __host__ __device__ constexpr int packed_slab_conflict(int n)
 constexpr int kMaxSlabConflict = 4;
 
 // Shared-memory stride (elements) of one i0 slab (N*N values) of the DOF and
-// output stages.  Packed (N*N: the tile is one contiguous bulk copy) when N
-// is odd (odd strides are conflict free) or when the packed slabs' 16-byte
-// accesses conflict at most kMaxSlabConflict ways; else every slab is its
-// own bulk copy into a slot whose byte size is an odd multiple of 16
-// (conflict free per phase).
+// output stages for tiles whose slabs move by 1D bulk copies.  Packed (N*N:
+// the tile is one contiguous bulk copy) when N is odd or when the packed
+// slabs' 16-byte accesses conflict at most kMaxSlabConflict ways; else
+// every slab is its own bulk copy into its slot (slot_stride).  Tiles whose
+// padded slots move by 2D tensor copies use slot_stride throughout.
 template <typename T>
 __host__ __device__ constexpr int slab_stride(int n)
 {
   if (n % 2 == 1 || (n * n * (int)sizeof(T)) % 16 != 0 ||
       packed_slab_conflict<T>(n) <= kMaxSlabConflict)
     return n * n;
-  int units = (n * n * (int)sizeof(T) + 15) / 16;
-  if (units % 2 == 0)
-    ++units;
-  return units * 16 / (int)sizeof(T);
+  return slot_stride<T>(n);
 }
 
 // y[m] = sum_k A(m,k) x[k] with A(m,k) = A[m*SM + k*SK] (compile-time
@@ -416,6 +439,9 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   const unsigned bslab = N2 * sizeof(ST);
   const unsigned bu = (unsigned)cb * N3 * sizeof(ST);
   const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(ST) : 0u;
+  // padded slots by tensor copies (whole boxes, padding included, land)
+  const bool tma = Tile::kSlabCopies && p.tma_rows > 0 && (cb * N) % p.tma_rows == 0;
+  const unsigned bx = tma ? (unsigned)cb * N * US * sizeof(ST) : bu;
   const int lane = threadIdx.x & 31;
   const bool warp0 = threadIdx.x < 32;
   const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3]};
@@ -436,18 +462,24 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     if (lane == 0)
     {
       fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&bar[s], bu + bg);
+      mbar_arrive_expect_tx(&bar[s], bx + bg);
       if (staged)
         bulk_g2s(sg(s), p.geo + t * cb * Q3NC, bg, &bar[s]);
       if constexpr (!Tile::kSlabCopies)
         bulk_g2s(su(s), p.u + t * cb * N3, bu, &bar[s]);
+      else if (tma)
+        for (int r = 0; r < cb * N; r += p.tma_rows)
+          tma_load_2d(su(s) + r * US, &p.tmu, 0, (int)(t * cb * N) + r, &bar[s]);
     }
     if constexpr (Tile::kSlabCopies)
     {
-      __syncwarp();
-      const long long slab0 = t * cb * N;
-      for (int k = lane; k < cb * N; k += 32)
-        bulk_g2s(su(s) + k * US, p.u + (slab0 + k) * N2, bslab, &bar[s]);
+      if (!tma)
+      {
+        __syncwarp();
+        const long long slab0 = t * cb * N;
+        for (int k = lane; k < cb * N; k += 32)
+          bulk_g2s(su(s) + k * US, p.u + (slab0 + k) * N2, bslab, &bar[s]);
+      }
     }
   };
 
@@ -534,6 +566,15 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
           bulk_commit();
         }
       }
+      else if (tma)
+      {
+        if (threadIdx.x == 0)
+        {
+          for (int r = 0; r < cb * N; r += p.tma_rows)
+            tma_store_2d(&p.tmy, 0, (int)(tile * cb * N) + r, sy + r * US);
+          bulk_commit();
+        }
+      }
       else if (warp0)
       {
         const long long slab0 = tile * cb * N;
@@ -610,14 +651,18 @@ __device__ __forceinline__ Part cta_part(int ncb)
 
 // EVOD: even-odd contractions (mv_eo) for tables with the GLL-to-Gauss
 // symmetry; one lane per slab, exact semantics.
+// SLOTS: the DOF/output slabs always sit in conflict-free slots
+// (slot_stride), moved by 2D tensor copies when the launch has tensor maps
+// (the single-mesh kernels); else slab_stride's rule (the batch kernels).
 template <typename T, int N, int Q, int OP, int SEM, int LANES = slab_lanes<T>(),
-          bool EVOD = false>
+          bool EVOD = false, bool SLOTS = false>
 struct SlabTile
 {
   using ST = storage_t<T>; // staged u, y and geometry; T is the arithmetic
   static constexpr int S = LANES;
-  static constexpr int US = slab_stride<ST>(N);
-  // padded slots: one bulk copy per slab; packed slabs: one per tile
+  static constexpr int US = SLOTS ? slot_stride<ST>(N) : slab_stride<ST>(N);
+  // padded slots: one tensor copy per tile (or one bulk copy per slab);
+  // packed slabs: one bulk copy per tile
   static constexpr bool kSlabCopies = (US != N * N);
   // slabs of whole 16-byte vectors: vector loads and stores (16-byte
   // aligned slots, packed or padded)
@@ -1433,6 +1478,9 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   const unsigned bslab = N2 * sizeof(ST);
   const unsigned bu = (unsigned)cb * N3 * sizeof(ST);
   const unsigned bg = staged ? (unsigned)cb * Q3NC * sizeof(ST) : 0u;
+  // padded slots by tensor copies (whole boxes, padding included, land)
+  const bool tma = Tile::kSlabCopies && p.tma_rows > 0 && (cb * N) % p.tma_rows == 0;
+  const unsigned bx = tma ? (unsigned)cb * N * US * sizeof(ST) : bu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   const int cw = (cb + nwarps - 1) / nwarps; // cells per warp
@@ -1456,18 +1504,24 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
     if (lane == 0)
     {
       fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&full[s], bu + bg);
+      mbar_arrive_expect_tx(&full[s], bx + bg);
       if (staged)
         bulk_g2s(sg(s), p.geo + t * cb * Q3NC, bg, &full[s]);
       if constexpr (!Tile::kSlabCopies)
         bulk_g2s(su(s), p.u + t * cb * N3, bu, &full[s]);
+      else if (tma)
+        for (int r = 0; r < cb * N; r += p.tma_rows)
+          tma_load_2d(su(s) + r * US, &p.tmu, 0, (int)(t * cb * N) + r, &full[s]);
     }
     if constexpr (Tile::kSlabCopies)
     {
-      __syncwarp();
-      const long long slab0 = t * cb * N;
-      for (int k = lane; k < cb * N; k += 32)
-        bulk_g2s(su(s) + k * US, p.u + (slab0 + k) * N2, bslab, &full[s]);
+      if (!tma)
+      {
+        __syncwarp();
+        const long long slab0 = t * cb * N;
+        for (int k = lane; k < cb * N; k += 32)
+          bulk_g2s(su(s) + k * US, p.u + (slab0 + k) * N2, bslab, &full[s]);
+      }
     }
   };
 
@@ -1551,7 +1605,7 @@ template <typename T, int N, int Q, int OP, int SEM, int LANES, bool EVOD = fals
 __global__ void __launch_bounds__(kCellThreads)
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  using Tile = SlabTile<T, N, Q, OP, SEM, LANES, EVOD>;
+  using Tile = SlabTile<T, N, Q, OP, SEM, LANES, EVOD, true>;
   if constexpr (Tile::kWarpSplit)
     stream_tiles_warp<T, Tile, N, Q, geo_nc(OP)>(p);
   else

@@ -103,6 +103,28 @@ __device__ __forceinline__ void bulk_s2g(void* dst, const void* src,
       : "memory");
 }
 
+// 2D tiled tensor copy global -> shared of the box at (x, y) of the tensor
+// map `map` (a __grid_constant__ parameter), completion on `bar`; dst
+// 128-byte aligned, x * element size a multiple of 16 bytes.  Box elements
+// outside the tensor are written as zeros.
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* map, int x, int y,
+                                            uint64_t* bar)
+{
+  asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+               " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+               "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// 2D tiled tensor copy shared -> global of the box at (x, y), tracked by
+// bulk groups; box elements outside the tensor are not written.
+__device__ __forceinline__ void tma_store_2d(const void* map, int x, int y, const void* src)
+{
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::
+                   "l"(map), "r"(x), "r"(y), "r"(smem_addr(src))
+               : "memory");
+}
+
 __device__ __forceinline__ void bulk_commit()
 {
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");

@@ -507,6 +507,69 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
   return FEMTC_OK;
 }
 
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on it);
+// null when the driver does not provide it.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled()
+{
+  static EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+    {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+
+// Tensor maps of the padded DOF/output slots of a slab kernel's tile: u and
+// y viewed as [ncells*N rows][N*N], boxes of `rows` rows by `slot` columns
+// (columns N*N.. are outside the tensor).  Box rows: the largest divisor of
+// cb*N that is at most 256 and keeps every box's shared-memory start
+// 128-byte aligned.  Returns the box rows, or 0 (then the kernel copies
+// slab by slab).
+int slot_tensor_maps(CUtensorMap* tu, CUtensorMap* ty, const void* u, void* y, int n, int esize,
+                     int cb, size_t ncells)
+{
+  EncodeTiledFn enc = encode_tiled();
+  const int slot = esize == 8 ? slot_stride<double>(n) : slot_stride<float>(n);
+  const long long rows_total = (long long)ncells * n;
+  if (!enc || slot == n * n || rows_total >= (1LL << 31))
+    return 0;
+  const int rows = cb * n;
+  int box = 0;
+  for (int k = 1; k <= rows; ++k)
+    if (rows % k == 0 && rows / k <= 256 && ((long long)(rows / k) * slot * esize) % 128 == 0)
+    {
+      box = rows / k;
+      break;
+    }
+  if (box == 0)
+    return 0;
+  const CUtensorMapDataType dt =
+      esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const cuuint64_t dims[2] = {(cuuint64_t)n * n, (cuuint64_t)rows_total};
+  const cuuint64_t strides[1] = {(cuuint64_t)n * n * esize};
+  const cuuint32_t boxd[2] = {(cuuint32_t)slot, (cuuint32_t)box};
+  const cuuint32_t estr[2] = {1, 1};
+  if (enc(tu, dt, 2, const_cast<void*>(u), dims, strides, boxd, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+      enc(ty, dt, 2, y, dims, strides, boxd, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return 0;
+  return box;
+}
+
 // Launch-parameter form of a table entry (double-float splits FP64).
 template <typename T>
 T param_value(storage_t<T> x)
@@ -539,6 +602,9 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
   p.sq = cfg.sq;
   p.sbc = cfg.sbc;
   p.host_io = host_io;
+  if (v.slab && !host_io)
+    p.tma_rows = slot_tensor_maps(&p.tmu, &p.tmy, u, y, v.n, (int)sizeof(storage_t<T>), cfg.cb,
+                                  ncells);
   const int ntab = (op_base(v.op) != FEMTC_OP_MASS) ? 2 : 1;
   const bool affine = op_affine(v.op);
   const ST* wq = tables + 2 * v.n * v.q; // affine forms: the Q weights

@@ -169,4 +169,36 @@ void stiffness_operator(std::span<T> phi, std::span<T> U, std::span<T> W,
       nquad > 0 ? nquad : degree + 1, phi.data(), U.data(), W.data(),
       G.data(), (std::size_t)num_cells));
 }
+
+// ------------------------------------------------------- affine cells --
+// No reference counterpart (the reference takes per-point detJ and G,
+// src/mass.hpp:10-12, src/stiffness.hpp:34-36).  On affine cells the
+// geometry is one set per cell: detJ (mass) or detJ J^-1 J^-T as
+// [zz,yz,xz,yy,xy,xx] (stiffness).  tables: Phi (Q x N), Gamma (Q x N),
+// then the Q 1D quadrature weights.  Host buffers, as the operators above.
+template <typename T, int P, int Q = P + 2>
+void affine_mass_operator(std::span<const T> tables, std::span<const T> U, std::span<T> W,
+                          std::span<const T> detJ, std::size_t num_cells)
+{
+  static_assert(P >= 1, "degree must be at least 1");
+  if (tables.size() < std::size_t(2 * Q * (P + 1) + Q) || detJ.size() < num_cells)
+    throw std::runtime_error("femtc_gpu: affine tables hold Phi, Gamma and the weights; "
+                             "one detJ per cell");
+  detail::check(femtc_affine_apply_host(FEMTC_OP_MASS_AFFINE, detail::dtype<T>(), P, Q,
+                                        tables.data(), U.data(), W.data(), detJ.data(),
+                                        num_cells));
+}
+
+template <typename T, int P, int Q = P + 2>
+void affine_stiffness_operator(std::span<const T> tables, std::span<const T> U,
+                               std::span<T> W, std::span<const T> G, std::size_t num_cells)
+{
+  static_assert(P >= 1, "degree must be at least 1");
+  if (tables.size() < std::size_t(2 * Q * (P + 1) + Q) || G.size() < 6 * num_cells)
+    throw std::runtime_error("femtc_gpu: affine tables hold Phi, Gamma and the weights; "
+                             "six G values per cell");
+  detail::check(femtc_affine_apply_host(FEMTC_OP_STIFFNESS_AFFINE, detail::dtype<T>(), P, Q,
+                                        tables.data(), U.data(), W.data(), G.data(),
+                                        num_cells));
+}
 } // namespace operators

@@ -47,3 +47,32 @@ def test_drop_in_matches_oracle(femtc, orc, dev, tmp_path, op, dtype, degree):
     for f in ("W_dispatch.bin", "W_template.bin"):
         W = rd(f).reshape(ncells, -1)
         assert np.abs(W - ref).max() / np.abs(ref).max() <= tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op", ["affine_mass", "affine_stiffness"])
+@pytest.mark.parametrize("dtype", ["double", "float"])
+@pytest.mark.parametrize("degree", [1, 4, 7])
+def test_drop_in_affine_matches_oracle(femtc, orc, dev, tmp_path, op, dtype, degree):
+    """The header's affine operators against the oracle on the expanded
+    per-point factors (Q = P+2, tabulated tables)."""
+    from femtc_gb300 import workloads as W
+    exe = compile_driver(femtc, str(tmp_path))
+    ncells = 133
+    r = subprocess.run([exe, op, str(degree), str(ncells), dtype, str(tmp_path)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    npdt = np.float64 if dtype == "double" else np.float32
+    rd = lambda f: np.fromfile(os.path.join(tmp_path, f), dtype=npdt).astype(np.float64)
+    n, q = degree + 1, degree + 2
+    tab, U, geo = rd("tables.bin"), rd("U.bin").reshape(ncells, -1), rd("geo.bin")
+    w3 = W.tensor_weights(tab[2 * q * n:])
+    if op == "affine_mass":
+        ref = orc.mass(orc.EXACT, degree, q, tab[:2 * q * n], U, geo[:, None] * w3[None])
+    else:
+        g = geo.reshape(ncells, 6)
+        ref = orc.stiffness(orc.EXACT, degree, q, tab[:2 * q * n], U,
+                            g[:, None, :] * w3[None, :, None])
+    tol = 1e-12 if dtype == "double" else 2e-6
+    Wt = rd("W_template.bin").reshape(ncells, -1)
+    assert np.abs(Wt - ref).max() / np.abs(ref).max() <= tol

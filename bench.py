@@ -443,7 +443,8 @@ def run_serve(args, rank, world, dev, pg):
         wp = F.Problem(P, P + 2, np.tile(np.eye(3).reshape(1, 9), (8, 1)), np.ones((8, (P + 1) ** 3)),
                        inner_dtype=inner)
         F.solve(wp)
-    srv = F.Server(budget, max_active=8)
+    policy = F.SERVE_FIFO if args.serve_policy == "fifo" else F.SERVE_SHORTEST_FIRST
+    srv = F.Server(budget, max_active=8, policy=policy)
     tickets = [None] * nreq
     t0 = time.perf_counter()
 
@@ -475,7 +476,8 @@ def run_serve(args, rank, world, dev, pg):
             "data": "synthetic",
             "config": {"workload": "serve", "requests": nreq, "arrival_rate_per_s": 2000,
                        "degrees": "2..7", "cells": "log-uniform [1e3, 2e5]", "rtol": 1e-8,
-                       "hbm_budget_bytes": budget, "max_active": 8},
+                       "hbm_budget_bytes": budget, "max_active": 8,
+                       "admission": args.serve_policy},
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "service_p50_ms": float(np.percentile(svc, 50)),
             "service_p99_ms": float(np.percentile(svc, 99)),
@@ -503,6 +505,9 @@ def main():
     ap.add_argument("--workload", default="stiffness_p4",
                     choices=["stiffness_p4", "mass_p3", "stiffness_p6", "batch64", "serve"])
     ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
+    ap.add_argument("--serve-policy", default="shortest", choices=["shortest", "fifo"],
+                    help="serve: admission order (shortest estimated work first, with aging; "
+                         "or arrival order)")
     ap.add_argument("--inner-dtype", default="f32", choices=["f32", "f16x2", "bf16x3"],
                     help="serve: operator form of the inner CG (FP64 refinement outside)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

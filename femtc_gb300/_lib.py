@@ -84,6 +84,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_server_submit": ([vp, vp, ctypes.POINTER(ctypes.c_longlong)], c_int),
         "femtc_server_wait": ([vp, ctypes.c_longlong, ctypes.c_double, vp], c_int),
         "femtc_server_get_stats": ([vp, vp], c_int),
+        "femtc_server_set_policy": ([vp, c_int], c_int),
         "femtc_server_destroy": ([vp], None),
     }
     for name, (args, res) in sigs.items():
@@ -468,14 +469,20 @@ def solve(problem: "Problem", stream=None, raise_on_error: bool = True) -> dict:
     return out
 
 
-class Server:
-    """Continuous-batching solve server (femtc_server_*)."""
+SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
 
-    def __init__(self, hbm_budget_bytes: int, max_active: int):
+
+class Server:
+    """Continuous-batching solve server (femtc_server_*); policy: admission
+    order, SERVE_SHORTEST_FIRST (default, with aging) or SERVE_FIFO."""
+
+    def __init__(self, hbm_budget_bytes: int, max_active: int,
+                 policy: int = SERVE_SHORTEST_FIRST):
         h = ctypes.c_void_p()
         check(load().femtc_server_create(hbm_budget_bytes, max_active, ctypes.byref(h)))
         self.handle = h
         self._live = {}
+        check(load().femtc_server_set_policy(h, policy))
 
     def submit(self, problem: "Problem") -> int:
         t = ctypes.c_longlong()

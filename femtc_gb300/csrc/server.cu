@@ -1,9 +1,13 @@
 // Serving loop (femtc_server_* in femtc_gpu.h): continuous batching of
 // matrix-free solves.  A fixed pool of host workers, each with its own CUDA
-// stream, takes requests from one FIFO queue as soon as a worker is free and
-// the request fits in the HBM budget next to the solves already running;
-// running solves overlap on the device.  Timestamps (submit, admit, done)
-// are taken on one steady clock so callers get queueing and service latency.
+// stream, takes requests from one queue as soon as a worker is free and the
+// request fits in the HBM budget next to the solves already running;
+// running solves overlap on the device.  The next request is the oldest
+// (FIFO) or, by default, the one with the least estimated work less the
+// time it has waited (shortest first with aging: no request waits longer
+// than the estimate of the work admitted ahead of it).  Timestamps (submit,
+// admit, done) are taken on one steady clock so callers get queueing and
+// service latency.
 #include "femtc_gpu.h"
 
 #include <chrono>
@@ -33,7 +37,17 @@ struct femtc_server
     femtc_solve_request rq;
     size_t bytes;
     double t_submit;
+    double est_ms; // estimated work, in the units of the aging clock
   };
+  // Estimated work of a solve: DOFs times the operator's work per DOF
+  // (sum factorisation: about N flops per DOF per contraction), scaled to
+  // milliseconds of a solve sharing the GPU with others.
+  static double estimate_ms(const femtc_solve_request& rq)
+  {
+    const double n = rq.degree + 1;
+    return 1e-5 * (double)rq.ncells * n * n * n * n;
+  }
+  int policy = FEMTC_SERVE_SHORTEST_FIRST;
   size_t budget = 0;
   int device = 0;
   clk::time_point t0 = clk::now();
@@ -52,6 +66,31 @@ struct femtc_server
     return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
   }
 
+  // Queue index of the request to admit now, or -1 (caller holds m).  The
+  // chosen request waits for memory rather than being passed by smaller
+  // ones, so a large request is not starved.
+  long pick() const
+  {
+    if (queue.empty())
+      return -1;
+    size_t best = 0;
+    if (policy == FEMTC_SERVE_SHORTEST_FIRST)
+    {
+      const double t = now_ms();
+      double key = 1e300;
+      for (size_t i = 0; i < queue.size(); ++i)
+      {
+        const double k = queue[i].est_ms - (t - queue[i].t_submit);
+        if (k < key)
+        {
+          key = k;
+          best = i;
+        }
+      }
+    }
+    return in_use + queue[best].bytes <= budget ? (long)best : -1;
+  }
+
   void worker()
   {
     cudaSetDevice(device);
@@ -63,13 +102,12 @@ struct femtc_server
       Job job;
       {
         std::unique_lock<std::mutex> lk(m);
-        cv_work.wait(lk, [&] {
-          return stop || (!queue.empty() && in_use + queue.front().bytes <= budget);
-        });
+        long idx = -1;
+        cv_work.wait(lk, [&] { return stop || (idx = pick()) >= 0; });
         if (stop)
           break;
-        job = queue.front();
-        queue.pop_front();
+        job = queue[(size_t)idx];
+        queue.erase(queue.begin() + idx);
         in_use += job.bytes;
         peak = std::max(peak, in_use);
         ++active;
@@ -129,7 +167,8 @@ int femtc_server_submit(femtc_server* s, const femtc_solve_request* rq, long lon
     return aux_fail(FEMTC_ERR_NOMEM, "server: request exceeds the HBM budget");
   }
   *ticket = s->next_ticket++;
-  s->queue.push_back(femtc_server::Job{*ticket, *rq, bytes, s->now_ms()});
+  s->queue.push_back(
+      femtc_server::Job{*ticket, *rq, bytes, s->now_ms(), femtc_server::estimate_ms(*rq)});
   ++s->submitted;
   s->cv_work.notify_one();
   return FEMTC_OK;
@@ -149,6 +188,19 @@ int femtc_server_wait(femtc_server* s, long long ticket, double timeout_s,
   *res = s->results[ticket];
   s->results.erase(ticket);
   return res->status;
+}
+
+int femtc_server_set_policy(femtc_server* s, int policy)
+{
+  if (!s || (policy != FEMTC_SERVE_FIFO && policy != FEMTC_SERVE_SHORTEST_FIRST))
+    return aux_fail(FEMTC_ERR_INVALID, "server: policy is FEMTC_SERVE_FIFO or "
+                                       "FEMTC_SERVE_SHORTEST_FIRST");
+  {
+    std::lock_guard<std::mutex> lk(s->m);
+    s->policy = policy;
+  }
+  s->cv_work.notify_all();
+  return FEMTC_OK;
 }
 
 int femtc_server_get_stats(femtc_server* s, femtc_server_stats* st)

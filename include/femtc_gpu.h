@@ -372,11 +372,19 @@ int femtc_solve(const femtc_solve_request* rq, femtc_solve_result* res,
 
 /* Serving loop with continuous batching: up to max_active solves run at
  * once, each on its own stream and host worker, so their kernels overlap on
- * the device; queued requests are admitted in arrival order as slots and
- * HBM budget free up (a request larger than the whole budget is rejected
- * at submit with FEMTC_ERR_NOMEM).  Request memory (J, b, x) must stay
- * valid until the request's result has been collected. */
+ * the device; queued requests are admitted as slots and HBM budget free up
+ * (a request larger than the whole budget is rejected at submit with
+ * FEMTC_ERR_NOMEM).  Request memory (J, b, x) must stay valid until the
+ * request's result has been collected. */
 typedef struct femtc_server femtc_server;
+
+/* Admission order (femtc_server_set_policy).  SHORTEST_FIRST (default): the
+ * queued request with the least estimated work (cells x N^4) less the time
+ * it has waited, so small requests pass large ones but a request's wait is
+ * bounded by the work admitted ahead of it; the chosen request waits for
+ * HBM rather than being passed.  FIFO: arrival order. */
+#define FEMTC_SERVE_FIFO 0
+#define FEMTC_SERVE_SHORTEST_FIRST 1
 
 typedef struct
 {
@@ -394,6 +402,7 @@ int femtc_server_submit(femtc_server* s, const femtc_solve_request* rq,
 int femtc_server_wait(femtc_server* s, long long ticket, double timeout_s,
                       femtc_solve_result* res);
 int femtc_server_get_stats(femtc_server* s, femtc_server_stats* st);
+int femtc_server_set_policy(femtc_server* s, int policy);
 /* Stops admitting, lets running solves finish, drops queued ones. */
 void femtc_server_destroy(femtc_server* s);
 

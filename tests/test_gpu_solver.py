@@ -89,3 +89,25 @@ def test_server_budget_serialises(femtc, dev):
     assert r1["rc"] == 0 and r2["rc"] == 0
     assert st["max_concurrent"] == 1 and st["peak_in_use_bytes"] <= need * 1.5
     assert r2["t_admit_ms"] >= r1["t_done_ms"] - 1.0
+
+
+@pytest.mark.parametrize("policy", ["fifo", "shortest"])
+def test_server_admission_order(femtc, dev, policy):
+    """One worker: FIFO admits in arrival order; shortest-first admits the
+    queued requests smallest first (equal waits, so the estimates decide)."""
+    big = problem(femtc, 5, 7, 3000, 1.0, seed=11)[0]
+    others = [problem(femtc, P, P + 2, n, 1.0, seed=20 + i)[0]
+              for i, (P, n) in enumerate([(4, 800), (3, 300), (2, 50)])]
+    pol = femtc.SERVE_FIFO if policy == "fifo" else femtc.SERVE_SHORTEST_FIRST
+    srv = femtc.Server(hbm_budget_bytes=8 << 30, max_active=1, policy=pol)
+    try:
+        tickets = [srv.submit(big)] + [srv.submit(p) for p in others]
+        res = [srv.wait(t, 300.0) for t in tickets]
+    finally:
+        srv.close()
+    assert all(r["rc"] == 0 for r in res)
+    admits = [r["t_admit_ms"] for r in res[1:]]
+    if policy == "fifo":
+        assert admits == sorted(admits)
+    else:
+        assert admits == sorted(admits, reverse=True)

@@ -34,6 +34,17 @@ def test_server_rejects_over_budget_and_malformed(femtc):
         s.close()
 
 
+def test_server_policy_validation(femtc):
+    s = femtc.Server(hbm_budget_bytes=1 << 20, max_active=1, policy=femtc.SERVE_FIFO)
+    try:
+        lib = femtc.load()
+        assert lib.femtc_server_set_policy(s.handle, femtc.SERVE_SHORTEST_FIRST) == 0
+        assert lib.femtc_server_set_policy(s.handle, 7) == -1
+        assert lib.femtc_server_set_policy(None, 0) == -1
+    finally:
+        s.close()
+
+
 def test_solve_argument_errors(femtc):
     p = femtc.Problem(3, 5, np.eye(3).reshape(1, 9), np.ones((1, 64)), alpha=0.0)
     with pytest.raises(femtc.FemtcError):

@@ -1262,12 +1262,28 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
                   [](const auto& a, const auto& b) { return a.first > b.first; });
         for (size_t i = 0; i < opts.size() && i < 4; ++i)
           cands.push_back({lv, opts[i].second});
-        for (int c : wave_cb)
+        // and the largest tiles that let 2 or 3 CTAs share an SM's shared
+        // memory (228 KB, 1 KB reserved per CTA): lane efficiency does not
+        // see the CTAs that overlap one another's barriers and copies
+        std::vector<int> extra = wave_cb;
+        for (int k = 2; k <= 3; ++k)
+        {
+          int best_c = 0;
+          for (int c = 4; c <= 128; c += 4)
+            if (smem_of(*lv, with_layout(*lv, c, staged, nt)) <= 228u * 1024u / k - 1024u)
+              best_c = c;
+          if (best_c > 0)
+            extra.push_back(best_c);
+        }
+        for (int c : extra)
         {
           const TileCfg t = with_layout(*lv, c, staged, nt);
           bool dup = false;
           for (size_t i = 0; i < opts.size() && i < 4; ++i)
             dup = dup || opts[i].second.cb == c;
+          for (const auto& cd : cands)
+            dup = dup || (cd.first == lv && cd.second.cb == c && cd.second.staged == staged &&
+                          cd.second.nt == nt);
           if (!dup && smem_of(*lv, t) <= 227u * 1024u)
             cands.push_back({lv, t});
         }
@@ -1288,20 +1304,28 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
     rc = launch_variant(*cv, c, tables, u, y, geo, ncells, st, host_io);
     if (rc != FEMTC_OK)
       continue; // e.g. does not fit on an SM with these registers
-    cudaEventRecord(e0, st);
-    for (int r = 0; r < 3; ++r)
-      launch_variant(*cv, c, tables, u, y, geo, ncells, st, host_io);
-    cudaEventRecord(e1, st);
-    cudaError_t e = cudaEventSynchronize(e1);
-    if (e != cudaSuccess)
-    {
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      return cuda_fail(e, "autotune");
-    }
+    // 3 launches, or about 2 ms of them for short calls (whose times
+    // scatter by more than the differences between tile shapes)
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    ms /= 3.f;
+    for (int reps = 3;;)
+    {
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < reps; ++r)
+        launch_variant(*cv, c, tables, u, y, geo, ncells, st, host_io);
+      cudaEventRecord(e1, st);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess)
+      {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(e, "autotune");
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= (float)reps;
+      if (reps > 3 || ms * reps >= 2.f)
+        break;
+      reps = std::min(200, (int)(2.f / std::max(ms, 1e-3f)) + 1);
+    }
     if (ms < best)
     {
       best = ms;

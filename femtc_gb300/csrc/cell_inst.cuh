@@ -96,12 +96,12 @@ void add_helmholtz(std::vector<CellVariant>& v, int dtype)
   }
 }
 
-// Affine forms (exact semantics, one lane per slab), N = N0..8, Q = N..N+2:
-// the plain kernels, and the even-odd ones up to N = MAXEO.
-template <typename T, int OP, int N, int MAXEO>
+// Affine forms (exact semantics, one lane per slab), N = N0..MAXN, Q =
+// N..N+2: the plain kernels, and the even-odd ones up to N = MAXEO.
+template <typename T, int OP, int N, int MAXEO, int MAXN = 8>
 void add_affine(std::vector<CellVariant>& v, int dtype)
 {
-  if constexpr (N <= 8)
+  if constexpr (N <= MAXN)
   {
     add_variant<T, N, N, OP, SEM_EXACT, 1>(v, dtype);
     add_variant<T, N, N + 1, OP, SEM_EXACT, 1>(v, dtype);
@@ -112,7 +112,7 @@ void add_affine(std::vector<CellVariant>& v, int dtype)
       add_variant<T, N, N + 1, OP, SEM_EXACT, 1, true>(v, dtype);
       add_variant<T, N, N + 2, OP, SEM_EXACT, 1, true>(v, dtype);
     }
-    add_affine<T, OP, N + 1, MAXEO>(v, dtype);
+    add_affine<T, OP, N + 1, MAXEO, MAXN>(v, dtype);
   }
 }
 

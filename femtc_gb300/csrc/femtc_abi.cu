@@ -72,6 +72,8 @@ Registry& registry()
     register_cell_affine_f64_stiffness(r.cells, r.faults);
     register_cell_affine_f32_mass(r.cells, r.faults);
     register_cell_affine_f32_stiffness(r.cells, r.faults);
+    register_cell_affine_f64e_mass(r.cells, r.faults);
+    register_cell_affine_f64e_stiffness(r.cells, r.faults);
     register_cell_f64e_mass(r.cells, r.faults);
     register_cell_f64e_stiffness(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);

@@ -45,6 +45,8 @@ void register_cell_affine_f64_mass(std::vector<CellVariant>&, std::vector<FaultR
 void register_cell_affine_f64_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_affine_f32_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_affine_f32_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_affine_f64e_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_affine_f64e_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_f16x2_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_f16x2_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_bf16x3_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);

@@ -140,7 +140,8 @@ int femtc_helmholtz_geometry(int nquad, double alpha, const void* dw,
  * stream shrinks from 8*6Q^3 to 48 bytes per cell (stiffness, FP64).
  * femtc_geometry(dtype, 1, &one, J, 0, detJ, G, ncells, stream) with
  * one = 1.0 computes cgeo from per-cell Jacobians.  FEMTC_F64 and
- * FEMTC_F32, degree 1..7, nquad in degree+1..degree+3.  No reference
+ * FEMTC_F32, degree 1..7, and FEMTC_F64E (FP64-accurate double-float),
+ * degree 1..4; nquad in degree+1..degree+3.  No reference
  * counterpart: the reference takes per-point factors (src/mass.hpp:10-12,
  * src/stiffness.hpp:34-36).  u, y, cgeo: device pointers, 16-byte aligned. */
 int femtc_affine_apply(int op, int dtype, int degree, int nquad, const void* tables,

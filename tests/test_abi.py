@@ -119,6 +119,7 @@ def test_affine_supported_and_rejected(femtc):
             for Q in (P + 1, P + 2, P + 3):
                 for dt in (femtc.F64, femtc.F32):
                     assert femtc.supported(op, dt, femtc.EXACT, P, Q)
+                assert femtc.supported(op, femtc.F64E, femtc.EXACT, P, Q) == (P <= 4)
             assert not femtc.supported(op, femtc.F64, femtc.REFERENCE, P, P + 1)
             assert not femtc.supported(op, femtc.F16X2, femtc.EXACT, P, P + 1)
     t = np.zeros(128)

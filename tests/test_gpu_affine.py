@@ -4,15 +4,15 @@ tables) against the FP64 oracle run on the equivalent per-point factors
 dw[c][q0][q1][q2] = w(q0) w(q1) w(q2) detJ[c] and
 G[c][q0][q1][q2][k] = w(q0) w(q1) w(q2) Gc[c][k].
 
-Tolerances (normwise, max|y - y_ref| / max|y_ref|): FP64 1e-12 and FP32
-2e-6, the per-point operators' own.
+Tolerances (normwise, max|y - y_ref| / max|y_ref|): FP64 1e-12, FP32
+2e-6 and double-float (F64E) 1e-13, the per-point operators' own.
 """
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {0: 1e-12, 1: 2e-6}
+TOL = {0: 1e-12, 1: 2e-6, 4: 1e-13}
 
 
 def relerr(a, b):
@@ -45,7 +45,7 @@ def oracle_ref(orc, femtc, op, P, Q, t, u, pg):
 
 def run_affine(femtc, dev, op, dtype, P, Q, t, w, u, cg):
     import torch
-    tdt = torch.float64 if dtype == femtc.F64 else torch.float32
+    tdt = torch.float64 if dtype in femtc.FP64_STORAGE else torch.float32
     ud = torch.from_numpy(u).to(dev, tdt)
     gd = torch.from_numpy(cg).to(dev, tdt)
     yd = torch.full_like(ud, float("nan"))
@@ -55,12 +55,15 @@ def run_affine(femtc, dev, op, dtype, P, Q, t, w, u, cg):
     return yd.cpu().double().numpy()
 
 
-@pytest.mark.parametrize("dtype", [0, 1])
+@pytest.mark.parametrize("dtype", [0, 1, 4])
 @pytest.mark.parametrize("op", [3, 4])
 @pytest.mark.parametrize("P", range(1, 8))
 @pytest.mark.parametrize("dq", [0, 1, 2])
 def test_affine_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
     Q = P + 1 + dq
+    if dtype == 4 and P > 4:
+        assert not femtc.supported(op, dtype, femtc.EXACT, P, Q)
+        pytest.skip("double-float forms up to degree 4")
     assert femtc.supported(op, dtype, femtc.EXACT, P, Q)
     for ncells in (37, 1001):  # ragged tails, many tiles and CTAs
         t, w, u, cg, pg = affine_mesh(femtc, op, P, Q, ncells, seed=10 * P + dq + 100 * op)
@@ -69,13 +72,15 @@ def test_affine_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
         assert relerr(y, ref) <= TOL[dtype], (ncells, relerr(y, ref))
 
 
-@pytest.mark.parametrize("dtype", [0, 1])
+@pytest.mark.parametrize("dtype", [0, 1, 4])
 @pytest.mark.parametrize("op", [3, 4])
 @pytest.mark.parametrize("P,Q", [(1, 3), (3, 5), (4, 6), (6, 8)])
 def test_affine_plain_and_even_odd(femtc, orc, dev, dtype, op, P, Q):
     """Both kernel forms against the oracle: even-odd (symmetric tables and
     weights), plain (switched off), and plain with asymmetric weights (the
     even-odd split does not apply to them)."""
+    if not femtc.supported(op, dtype, femtc.EXACT, P, Q):
+        pytest.skip("variant not built")
     t, w, u, cg, pg = affine_mesh(femtc, op, P, Q, 555, seed=P + 7 * op)
     at = femtc.affine_tables(t, w)
     assert femtc.even_odd_used(op, dtype, femtc.EXACT, P, Q, at)

@@ -15,6 +15,11 @@
 // Jacobi diagonal comes from sum factorization (squared and product 1D tables
 // applied to the per-point factors).  Inner iterations run as CUDA graphs of
 // kItersPerGraph iterations; the host reads one residual scalar per graph.
+// An inner iteration is four launches: the operator, <p,Ap> partial sums,
+// the update (every block first sums the <p,Ap> partials itself for alpha)
+// and the direction (every block sums the <r,z> partials for beta).  The CG
+// scalars live in two slots used in turn, so that the block that writes the
+// next iteration's <r,z> never overwrites the value the others still read.
 // All device memory of a request is one stream-ordered allocation whose size
 // femtc_solve_bytes() reports up front, so a server can admit by HBM budget.
 // Reductions use a fixed grid and a fixed summation order, so a solve gives
@@ -152,7 +157,11 @@ __device__ __forceinline__ double block_sum(double v)
   return s; // valid in thread 0
 }
 
-// Ap = a t1 + b t2 ; partial <p, Ap>
+// Partial sums: part[0..kRedBlocks) <r,z>, part[kRedBlocks..) <r,r>,
+// part[2 kRedBlocks..) <p,Ap>.
+constexpr int kPartRZ = 0, kPartRR = kRedBlocks, kPartPAP = 2 * kRedBlocks;
+
+// Ap = a t1 + b t2 ; partial <p, Ap> (part: the <p,Ap> region)
 __global__ void __launch_bounds__(kRedThreads)
     ap_dot_kernel(const float* t1, const float* t2, float a, float b,
                   const float* pv, float* Ap, long long n, double* part)
@@ -178,24 +187,28 @@ __device__ __forceinline__ double sum_parts(const double* part, int nb)
   return block_sum(s);
 }
 
+// alpha = <r,z> / <p,Ap> (every block sums the <p,Ap> partials in the same
+// order, so all get the same bits); d += alpha p ; r -= alpha Ap ;
+// z = r / diag ; partial <r,z>, <r,r>.  sc: this iteration's slot.
 __global__ void __launch_bounds__(kRedThreads)
-    reduce_alpha_kernel(const double* part, int nb, Scalars* sc)
+    update_kernel(Scalars* sc, const float* pv, const float* Ap, float* d,
+                  float* r, float* z, const float* invdiag, long long n,
+                  double* part, int nb)
 {
-  const double pap = sum_parts(part, nb);
+  __shared__ double s_alpha;
+  const double pap = sum_parts(part + kPartPAP, nb);
   if (threadIdx.x == 0)
   {
-    sc->pap = pap;
-    sc->alpha = (pap > 0.0 && sc->rz > 0.0) ? sc->rz / pap : 0.0;
+    const double rz0 = sc->rz;
+    s_alpha = (pap > 0.0 && rz0 > 0.0) ? rz0 / pap : 0.0;
+    if (blockIdx.x == 0)
+    {
+      sc->pap = pap;
+      sc->alpha = s_alpha;
+    }
   }
-}
-
-// d += alpha p ; r -= alpha Ap ; z = r / diag ; partial <r,z>, <r,r>
-__global__ void __launch_bounds__(kRedThreads)
-    update_kernel(const Scalars* sc, const float* pv, const float* Ap, float* d,
-                  float* r, float* z, const float* invdiag, long long n,
-                  double* part)
-{
-  const float alpha = (float)sc->alpha;
+  __syncthreads();
+  const float alpha = (float)s_alpha;
   double rz = 0.0, rr = 0.0;
   for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n;
        i += (long long)gridDim.x * kRedThreads)
@@ -212,30 +225,48 @@ __global__ void __launch_bounds__(kRedThreads)
   rr = block_sum(rr);
   if (threadIdx.x == 0)
   {
-    part[blockIdx.x] = rz;
-    part[kRedBlocks + blockIdx.x] = rr;
+    part[kPartRZ + blockIdx.x] = rz;
+    part[kPartRR + blockIdx.x] = rr;
   }
 }
 
-// rz_new, rr -> beta = rz_new / rz ; rz = rz_new
+// <r,z>, <r,r> of a start (no previous direction): into slot sc
 __global__ void __launch_bounds__(kRedThreads)
-    reduce_beta_kernel(const double* part, int nb, Scalars* sc, int init)
+    reduce_start_kernel(const double* part, int nb, Scalars* sc)
 {
-  const double rz = sum_parts(part, nb);
-  const double rr = sum_parts(part + kRedBlocks, nb);
+  const double rz = sum_parts(part + kPartRZ, nb);
+  const double rr = sum_parts(part + kPartRR, nb);
   if (threadIdx.x == 0)
   {
-    sc->beta = (!init && sc->rz > 0.0) ? rz / sc->rz : 0.0;
+    sc->beta = 0.0;
     sc->rz = rz;
     sc->rr = rr;
   }
 }
 
-// p = z + beta p
+// beta = <r,z>_new / <r,z> (every block sums the partials in the same
+// order); p = z + beta p.  sc: this iteration's slot (read), next: the other
+// slot, where block 0 leaves <r,z>_new, <r,r> and beta.
 __global__ void __launch_bounds__(kRedThreads)
-    dir_kernel(const Scalars* sc, const float* z, float* p, long long n)
+    dir_kernel(const Scalars* sc, Scalars* next, const double* part, int nb, const float* z,
+               float* p, long long n)
 {
-  const float beta = (float)sc->beta;
+  __shared__ double s_beta;
+  const double rz = sum_parts(part + kPartRZ, nb);
+  const double rr = sum_parts(part + kPartRR, nb);
+  if (threadIdx.x == 0)
+  {
+    const double rz0 = sc->rz;
+    s_beta = rz0 > 0.0 ? rz / rz0 : 0.0;
+    if (blockIdx.x == 0)
+    {
+      next->beta = s_beta;
+      next->rz = rz;
+      next->rr = rr;
+    }
+  }
+  __syncthreads();
+  const float beta = (float)s_beta;
   for (long long i = blockIdx.x * (long long)kRedThreads + threadIdx.x; i < n;
        i += (long long)gridDim.x * kRedThreads)
     p[i] = fmaf(beta, p[i], z[i]);
@@ -264,8 +295,8 @@ __global__ void __launch_bounds__(kRedThreads)
   rr = block_sum(rr);
   if (threadIdx.x == 0)
   {
-    part[blockIdx.x] = rz;
-    part[kRedBlocks + blockIdx.x] = rr;
+    part[kPartRZ + blockIdx.x] = rz;
+    part[kPartRR + blockIdx.x] = rr;
   }
 }
 
@@ -294,8 +325,8 @@ __global__ void __launch_bounds__(kRedThreads)
   rr = block_sum(rr);
   if (threadIdx.x == 0)
   {
-    part[blockIdx.x] = 0.0;
-    part[kRedBlocks + blockIdx.x] = rr;
+    part[kPartRZ + blockIdx.x] = 0.0;
+    part[kPartRR + blockIdx.x] = rr;
   }
 }
 
@@ -324,7 +355,8 @@ __global__ void __launch_bounds__(kRedThreads)
   }
 }
 
-// s = <p, Ap> partial sums (the fused operator already wrote Ap)
+// s = <p, Ap> partial sums (the fused operator already wrote Ap); part:
+// the <p,Ap> region
 __global__ void __launch_bounds__(kRedThreads)
     dot_kernel(const float* pv, const float* Ap, long long n, double* part)
 {
@@ -365,7 +397,7 @@ size_t carve(void* base, int n, int q, size_t nc, Bufs* B)
   b.r = (double*)take(n3 * 8);
   b.t1d = (double*)take(n3 * 8);
   b.t2d = (double*)take(n3 * 8);
-  b.part = (double*)take(2 * kRedBlocks * 8);
+  b.part = (double*)take(3 * kRedBlocks * 8);
   // FP32 geometry: separate dw and G (mass and stiffness launches), or the
   // interleaved geo8 of the fused Helmholtz launch, in one region sized for
   // the larger (8 values per point)
@@ -383,7 +415,7 @@ size_t carve(void* base, int n, int q, size_t nc, Bufs* B)
   b.t2 = (float*)take(n3 * 4);
   b.d = (float*)take(n3 * 4);
   b.invdiag = (float*)take(n3 * 4);
-  b.sc = (Scalars*)take(sizeof(Scalars));
+  b.sc = (Scalars*)take(2 * sizeof(Scalars)); // two slots, used in turn
   if (B)
     *B = b;
   return off;
@@ -407,9 +439,10 @@ bool fused_operator(const femtc_solve_request& rq)
   return rq.inner_dtype == FEMTC_F32 && rq.beta != 0.0;
 }
 
-// One inner CG iteration (6 or 7 launches) on stream st.
+// One inner CG iteration (4 or 5 launches) on stream st; it reads <r,z> from
+// slot `slot` and leaves the next one in the other slot.
 int inner_iteration(const femtc_solve_request& rq, const Bufs& B, const float* tab32,
-                    size_t nd, cudaStream_t st)
+                    size_t nd, cudaStream_t st, int slot)
 {
   const int g = grid_of((long long)nd);
   if (fused_operator(rq))
@@ -418,7 +451,7 @@ int inner_iteration(const femtc_solve_request& rq, const Bufs& B, const float* t
                                    rq.ncells, st);
     if (rc != FEMTC_OK)
       return rc;
-    dot_kernel<<<g, kRedThreads, 0, st>>>(B.p, B.Ap, (long long)nd, B.part);
+    dot_kernel<<<g, kRedThreads, 0, st>>>(B.p, B.Ap, (long long)nd, B.part + kPartPAP);
   }
   else
   {
@@ -432,13 +465,12 @@ int inner_iteration(const femtc_solve_request& rq, const Bufs& B, const float* t
     ap_dot_kernel<<<g, kRedThreads, 0, st>>>(B.t1, rq.beta != 0.0 ? B.t2 : B.t1,
                                              (float)rq.alpha,
                                              rq.beta != 0.0 ? (float)rq.beta : 0.f, B.p, B.Ap,
-                                             (long long)nd, B.part);
+                                             (long long)nd, B.part + kPartPAP);
   }
-  reduce_alpha_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc);
-  update_kernel<<<g, kRedThreads, 0, st>>>(B.sc, B.p, B.Ap, B.d, B.r32, B.z, B.invdiag,
-                                           (long long)nd, B.part);
-  reduce_beta_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc, 0);
-  dir_kernel<<<g, kRedThreads, 0, st>>>(B.sc, B.z, B.p, (long long)nd);
+  update_kernel<<<g, kRedThreads, 0, st>>>(B.sc + slot, B.p, B.Ap, B.d, B.r32, B.z, B.invdiag,
+                                           (long long)nd, B.part, g);
+  dir_kernel<<<g, kRedThreads, 0, st>>>(B.sc + slot, B.sc + (slot ^ 1), B.part, g, B.z, B.p,
+                                        (long long)nd);
   return cuda_err(cudaGetLastError());
 }
 
@@ -457,7 +489,7 @@ int residual64(const femtc_solve_request& rq, const Bufs& B, const double* tab64
   resid_kernel<<<g, kRedThreads, 0, st>>>(B.b, B.t1d, rq.beta != 0.0 ? B.t2d : B.t1d, rq.alpha,
                                           rq.beta != 0.0 ? rq.beta : 0.0, B.r, (long long)nd,
                                           B.part);
-  reduce_beta_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc, 1);
+  reduce_start_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc);
   Scalars s;
   cudaMemcpyAsync(&s, B.sc, sizeof(s), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
@@ -571,22 +603,26 @@ int solve_on_stream(const femtc_solve_request* rq, femtc_solve_result* res, cuda
     const int g = grid_of((long long)nd);
     inner_init_kernel<<<g, kRedThreads, 0, st>>>(B.r, 1.0 / std::sqrt(rr), B.r32, B.d, B.z,
                                                  B.p, B.invdiag, (long long)nd, B.part);
-    reduce_beta_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc, 1);
+    // slots: the first (eager) iteration of a solve reads slot 0 and leaves
+    // its result in slot 1; the graph's iterations read slots 1, 0, 1, ...
+    // (an even count), so every graph starts and ends on slot 1
+    reduce_start_kernel<<<1, kRedThreads, 0, st>>>(B.part, g, B.sc + (exec ? 1 : 0));
     int it = 0;
     while (it < max_inner)
     {
       if (!exec)
       {
         // first use: one eager iteration, then capture a graph of k of them
-        rc = inner_iteration(*rq, B, tab32.data(), nd, st);
+        rc = inner_iteration(*rq, B, tab32.data(), nd, st, 0);
         if (rc != FEMTC_OK)
           return finish(rc);
         ++it;
         e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess)
           return finish(cuda_err(e));
+        static_assert(kItersPerGraph % 2 == 0, "graphs start and end on slot 1");
         for (int k = 0; k < kItersPerGraph && rc == FEMTC_OK; ++k)
-          rc = inner_iteration(*rq, B, tab32.data(), nd, st);
+          rc = inner_iteration(*rq, B, tab32.data(), nd, st, (k & 1) ^ 1);
         e = cudaStreamEndCapture(st, &graph);
         if (rc != FEMTC_OK)
           return finish(rc);
@@ -600,8 +636,8 @@ int solve_on_stream(const femtc_solve_request* rq, femtc_solve_result* res, cuda
           return finish(cuda_err(e));
         it += kItersPerGraph;
       }
-      Scalars s;
-      cudaMemcpyAsync(&s, B.sc, sizeof(s), cudaMemcpyDeviceToHost, st);
+      Scalars s; // the latest <r,z>, <r,r>: slot 1 after the eager iteration or a graph
+      cudaMemcpyAsync(&s, B.sc + 1, sizeof(s), cudaMemcpyDeviceToHost, st);
       e = cudaStreamSynchronize(st);
       if (e != cudaSuccess)
         return finish(cuda_err(e));

@@ -271,7 +271,9 @@ int femtc_geometry(int out_dtype, int nquad, const double* weights,
  * dtype: FEMTC_F32 (CUDA cores), FEMTC_F16X2 or FEMTC_BF16X3 (tensor
  * cores); FP32 storage and tables.
  * flags: FEMTC_BATCH_TUNE measures tile shapes per (degree, op) on the
- * batch's own buffers at creation (the y buffers are overwritten).
+ * batch's own buffers at creation (the y buffers are overwritten), and
+ * the split plan (femtc_batch_plan); the single-mesh tile shapes it tunes
+ * stay in the process's tile table, as femtc_autotune's do.
  * ---------------------------------------------------------------------- */
 #define FEMTC_BATCH_TUNE 1
 /* Take the tuner's split plan (see femtc_batch_plan) even when the one-kernel

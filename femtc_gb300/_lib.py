@@ -52,6 +52,10 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_helmholtz_geometry": ([c_int, ctypes.c_double, vp, ctypes.c_double, vp, vp, c_size, vp],
                                      c_int),
         "femtc_affine_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
+        "femtc_assembled_apply": ([c_int] * 5 + [vp] * 4 + [c_size] + [vp] * 3 + [c_size, vp, vp],
+                                  c_int),
+        "femtc_assembled_work_bytes": ([c_int, c_int, c_size], c_size),
+        "femtc_dofmap_transpose": ([vp, c_size, c_int, c_size, vp, vp], c_int),
         "femtc_affine_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_mass_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
         "femtc_stiffness_apply_host": ([c_int] * 4 + [vp] * 4 + [c_size], c_int),
@@ -172,6 +176,33 @@ def apply(op: int, dtype: int, semantics: int, degree: int, nquad: int,
     fn = lib.femtc_mass_apply if op == MASS else lib.femtc_stiffness_apply
     check(fn(dtype, semantics, degree, nquad, tab.ctypes.data, ptr(u), ptr(y),
              ptr(geo), ncells, stream_ptr(stream)))
+
+
+def dofmap_transpose(dofmap, ndofs: int):
+    """CSR transpose (offsets[ndofs+1], entries) of a [ncells, N^3] int32 DOF
+    map, on the host (femtc_dofmap_transpose)."""
+    dm = np.ascontiguousarray(dofmap, dtype=np.int32)
+    ncells, n3 = dm.shape
+    offsets = np.empty(ndofs + 1, dtype=np.int32)
+    entries = np.empty(dm.size, dtype=np.int32)
+    check(load().femtc_dofmap_transpose(dm.ctypes.data, ncells, n3, ndofs, offsets.ctypes.data,
+                                        entries.ctypes.data))
+    return offsets, entries
+
+
+def assembled_work_bytes(dtype: int, degree: int, ncells: int) -> int:
+    return int(load().femtc_assembled_work_bytes(dtype, degree, ncells))
+
+
+def assembled_apply(op: int, dtype: int, semantics: int, degree: int, nquad: int, tables,
+                    dofmap, offsets, entries, ndofs: int, x, y, geo, ncells: int, work,
+                    stream=None) -> None:
+    """Global-DOF action y = sum_c P_c^T A_c P_c x (femtc_assembled_apply);
+    dofmap, offsets, entries, x, y, geo and work are device buffers."""
+    tab = host_tables(tables, dtype)
+    check(load().femtc_assembled_apply(op, dtype, semantics, degree, nquad, tab.ctypes.data,
+                                       ptr(dofmap), ptr(offsets), ptr(entries), ndofs, ptr(x),
+                                       ptr(y), ptr(geo), ncells, ptr(work), stream_ptr(stream)))
 
 
 def affine_tables(tables, weights) -> np.ndarray:

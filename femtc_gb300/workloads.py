@@ -161,6 +161,24 @@ def make_custom(name: str, op: int, degree: int, nquad: int, ncells: int, seed: 
                     np.ascontiguousarray(geo), seed)
 
 
+def box_dofmap(nx: int, ny: int, nz: int, degree: int):
+    """DOF map of an nx x ny x nz box of hexahedra of degree P with shared
+    (continuous) DOFs: cells in lexicographic order (x slowest), local DOF
+    (i0, i1, i2) of cell (cx, cy, cz) -> global grid point
+    (cx P + i0, cy P + i1, cz P + i2) of the (nx P + 1)(ny P + 1)(nz P + 1)
+    grid, numbered with the last index fastest.  Returns (dofmap int32
+    [ncells, N^3], ndofs)."""
+    p, n = degree, degree + 1
+    gy, gz = ny * p + 1, nz * p + 1
+    cx, cy, cz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    i0, i1, i2 = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    gx_ = cx.reshape(-1, 1) * p + i0.reshape(1, -1)
+    gy_ = cy.reshape(-1, 1) * p + i1.reshape(1, -1)
+    gz_ = cz.reshape(-1, 1) * p + i2.reshape(1, -1)
+    dofmap = (gx_ * gy + gy_) * gz + gz_
+    return np.ascontiguousarray(dofmap, dtype=np.int32), (nx * p + 1) * gy * gz
+
+
 def random_reference_inputs(op: int, degree: int, ncells: int, seed: int):
     """Inputs like the reference's own benchmark (bench_mass.cpp:72-88):
     random tables, U, and detJ/G, all U(0,1), Q = N.  Returns

@@ -28,6 +28,7 @@
 #define FEMTC_GPU_H
 
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -150,6 +151,28 @@ int femtc_affine_apply(int op, int dtype, int degree, int nquad, const void* tab
 /* The same with host buffers (as femtc_mass_apply_host). */
 int femtc_affine_apply_host(int op, int dtype, int degree, int nquad, const void* tables,
                             const void* u, void* y, const void* cgeo, size_t ncells);
+
+/* Assembled (global-DOF) action y = sum_c P_c^T A_c P_c x for mass or
+ * stiffness (op FEMTC_OP_MASS / FEMTC_OP_STIFFNESS), any dtype and
+ * semantics of the cell operators.  dofmap: device [ncells][N^3] int32,
+ * the global index of each local DOF (the cell-local order of u, y);
+ * offsets [ndofs+1], entries [ncells*N^3]: its transpose in CSR form
+ * (device copies of femtc_dofmap_transpose's output).  x, y: device
+ * [ndofs] in the dtype's storage type (FP64 for F64/F64E, else FP32);
+ * geo as for the cell operators; work: device scratch of
+ * femtc_assembled_work_bytes() bytes, 256-byte aligned.  y is written in a
+ * fixed summation order (no atomics).  No reference counterpart: the
+ * reference is cell-local only (src/mass.hpp:10-49). */
+int femtc_assembled_apply(int op, int dtype, int semantics, int degree, int nquad,
+                          const void* tables, const int32_t* dofmap, const int32_t* offsets,
+                          const int32_t* entries, size_t ndofs, const void* x, void* y,
+                          const void* geo, size_t ncells, void* work, void* stream);
+size_t femtc_assembled_work_bytes(int dtype, int degree, size_t ncells);
+/* Host: transpose a DOF map (ncells x n3 int32, values in [0, ndofs)) into
+ * CSR form: offsets[ndofs+1], entries[ncells*n3] = local positions c*n3+i
+ * in increasing order per global DOF. */
+int femtc_dofmap_transpose(const int32_t* dofmap, size_t ncells, int n3, size_t ndofs,
+                           int32_t* offsets, int32_t* entries);
 
 /* Host-buffer forms of mass and stiffness: every pointer is host memory
  * (pinned memory copies fastest).  Copies u and dw/G to the device, applies

@@ -15,6 +15,7 @@
 // femtc_dofmap_transpose builds the transposed map on the host.
 #include "femtc_gpu.h"
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <cuda_runtime.h>
@@ -28,27 +29,39 @@ namespace
 {
 constexpr int kThreads = 256;
 
+// Indices outside their arrays (a map that does not match the vectors) are
+// not dereferenced: they yield NaN, which the result then shows.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    gather_kernel(const T* __restrict__ x, const int32_t* __restrict__ dofmap,
+    gather_kernel(const T* __restrict__ x, long long ndofs, const int32_t* __restrict__ dofmap,
                   T* __restrict__ u, long long n)
 {
   for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n;
        i += (long long)gridDim.x * kThreads)
-    u[i] = x[dofmap[i]];
+  {
+    const int32_t g = dofmap[i];
+    u[i] = (g >= 0 && g < ndofs) ? x[g] : T(NAN);
+  }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    sum_kernel(const T* __restrict__ yloc, const int32_t* __restrict__ offsets,
+    sum_kernel(const T* __restrict__ yloc, long long nloc, const int32_t* __restrict__ offsets,
                const int32_t* __restrict__ entries, T* __restrict__ y, long long ndofs)
 {
   for (long long g = blockIdx.x * (long long)kThreads + threadIdx.x; g < ndofs;
        g += (long long)gridDim.x * kThreads)
   {
     T s = T(0);
-    for (int k = offsets[g]; k < offsets[g + 1]; ++k)
-      s += yloc[entries[k]];
+    const int k0 = offsets[g], k1 = offsets[g + 1];
+    if (k0 < 0 || k1 < k0 || k1 > nloc)
+      s = T(NAN);
+    else
+      for (int k = k0; k < k1; ++k)
+      {
+        const int32_t e = entries[k];
+        s += (e >= 0 && e < nloc) ? yloc[e] : T(NAN);
+      }
     y[g] = s;
   }
 }
@@ -79,7 +92,7 @@ int run(int op, int dtype, int semantics, int degree, int nquad, const void* tab
   const long long nloc = (long long)ncells * n3;
   T* u = static_cast<T*>(work);
   T* yl = reinterpret_cast<T*>(static_cast<char*>(work) + round256((size_t)nloc * sizeof(T)));
-  gather_kernel<T><<<grid_for(nloc), kThreads, 0, st>>>(x, dofmap, u, nloc);
+  gather_kernel<T><<<grid_for(nloc), kThreads, 0, st>>>(x, (long long)ndofs, dofmap, u, nloc);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
@@ -90,7 +103,7 @@ int run(int op, int dtype, int semantics, int degree, int nquad, const void* tab
                                              geo, ncells, st);
   if (rc != FEMTC_OK)
     return rc;
-  sum_kernel<T><<<grid_for((long long)ndofs), kThreads, 0, st>>>(yl, offsets, entries, y,
+  sum_kernel<T><<<grid_for((long long)ndofs), kThreads, 0, st>>>(yl, nloc, offsets, entries, y,
                                                                  (long long)ndofs);
   e = cudaGetLastError();
   return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));

@@ -161,7 +161,8 @@ int femtc_affine_apply_host(int op, int dtype, int degree, int nquad, const void
  * [ndofs] in the dtype's storage type (FP64 for F64/F64E, else FP32);
  * geo as for the cell operators; work: device scratch of
  * femtc_assembled_work_bytes() bytes, 256-byte aligned.  y is written in a
- * fixed summation order (no atomics).  No reference counterpart: the
+ * fixed summation order (no atomics).  Map entries outside [0, ndofs) (or a
+ * transpose that does not match) are not dereferenced: they give NaN.  No reference counterpart: the
  * reference is cell-local only (src/mass.hpp:10-49). */
 int femtc_assembled_apply(int op, int dtype, int semantics, int degree, int nquad,
                           const void* tables, const int32_t* dofmap, const int32_t* offsets,

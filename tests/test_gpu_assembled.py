@@ -77,3 +77,20 @@ def test_assembled_deterministic_and_symmetric(femtc, dev):
     y2 = run(femtc, op, dtype, P, w, nd, b)
     lhs, rhs = float(x2 @ y1), float(x @ y2)
     assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0) * 10
+
+
+def test_assembled_bad_map_entry_gives_nan(femtc, dev):
+    """A map entry outside [0, ndofs) is not dereferenced (the kernels check
+    every index): the DOFs it touches come out NaN, the rest are unchanged."""
+    import torch
+    op, dtype, P = 0, 0, 2
+    w, dm, nd, x, b = setup(femtc, dev, op, dtype, P, (3, 3, 3), seed=5)
+    y_ok = run(femtc, op, dtype, P, w, nd, b)
+    bad = dm.copy()
+    bad[4, 0] = nd + 1000  # cell 4, local DOF 0
+    b["dm"].copy_(torch.from_numpy(bad).to(dev))
+    y = run(femtc, op, dtype, P, w, nd, b)
+    hit = np.unique(dm[4])  # every DOF of cell 4 sees the NaN through its cell result
+    assert np.isnan(y[hit]).all()
+    rest = np.setdiff1d(np.arange(nd), hit)
+    assert np.array_equal(y[rest], y_ok[rest])

@@ -502,6 +502,89 @@ def run_serve(args, rank, world, dev, pg):
         print(json.dumps(line), flush=True)
 
 
+def box_shape(ncells: int):
+    """nx >= ny >= nz with nx*ny*nz = ncells, as near a cube as the factors allow."""
+    best = (ncells, 1, 1)
+    for nz in range(1, int(round(ncells ** (1 / 3))) + 2):
+        if ncells % nz:
+            continue
+        rest = ncells // nz
+        for ny in range(nz, int(rest ** 0.5) + 2):
+            if rest % ny == 0 and rest // ny >= ny:
+                cand = (rest // ny, ny, nz)
+                if max(cand) < max(best):
+                    best = cand
+    return best
+
+
+def run_assembled(args, rank, world, dev, pg):
+    """The workload's cells as a box mesh with shared (continuous) DOFs,
+    through femtc_assembled_apply: gather by the DOF map, the cell operator,
+    and the deterministic sum per global DOF.  GDoF/s counts global DOFs."""
+    import torch
+    import femtc_gb300 as F
+    from femtc_gb300 import workloads as W
+    w = W.make(args.workload, ncells=args.cells)
+    shape = box_shape(w.ncells)
+    dm, nd = W.box_dofmap(*shape, w.degree)
+    off, ent = F.dofmap_transpose(dm, nd)
+    stream = torch.cuda.current_stream()
+    n, q, op = w.n, w.nquad, w.op
+    forms = {}
+    launches = 0
+    for dtype in (F.F64, F.F32):
+        tdt = torch.float64 if dtype == F.F64 else torch.float32
+        dmd, offd, entd = (torch.from_numpy(a).to(dev) for a in (dm, off, ent))
+        x = torch.from_numpy(np.random.default_rng(w.seed).uniform(-1, 1, nd)).to(dev, tdt)
+        y = torch.empty_like(x)
+        g = torch.from_numpy(w.geo).to(dev, tdt)
+        work = torch.empty(F.assembled_work_bytes(dtype, w.degree, w.ncells), device=dev,
+                           dtype=torch.uint8)
+        u = torch.empty((w.ncells, n ** 3), device=dev, dtype=tdt)
+        F.autotune(op, dtype, F.EXACT, w.degree, q, w.tables, u, torch.empty_like(u), g, w.ncells,
+                   stream)
+        del u
+
+        def step():
+            F.assembled_apply(op, dtype, F.EXACT, w.degree, q, w.tables, dmd, offd, entd, nd, x, y,
+                              g, w.ncells, work, stream)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = F.operator_launches()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches += F.operator_launches() - l0
+        ms = replicas_max(e0.elapsed_time(e1), dev, world) / args.steps
+        forms[F.DTYPE_NAMES[dtype]] = {"ms": ms, "global_gdofs": world * nd / ms / 1e6,
+                                       "cell_gdofs": world * w.ndofs / ms / 1e6}
+    if rank == 0:
+        head = forms["f64"]
+        hbm, src = peaks()
+        print(json.dumps({
+            "metric": f"GDoF/s assembled {'stiffness' if op == 1 else 'mass'} action "
+                      f"(global DOFs, P={w.degree}, Q={q})",
+            "value": head["global_gdofs"], "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.workload}_assembled", "cells": w.ncells, "box": shape,
+                       "global_dofs": nd, "cell_dofs": w.ndofs, "parallelism": f"replicas{world}"},
+            "gpu_launches": launches, "forms": forms, "peak_hbm_gbs": hbm, "peak_source": src,
+        }), flush=True)
+
+
+def replicas_max(x, dev, world):
+    if world == 1:
+        return x
+    from femtc_gb300 import replicas
+    return replicas.max_over_ranks(x, device=dev)
+
+
 def torch_free_bytes(dev):
     import torch
     free, _ = torch.cuda.mem_get_info(dev)
@@ -527,6 +610,9 @@ def main():
     ap.add_argument("--no-batch-tune", action="store_true",
                     help="batch64: built-in tile layouts (no autotuning launches; profiling)")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
+    ap.add_argument("--assembled", action="store_true",
+                    help="the workload's cells as a box mesh with shared DOFs, through the "
+                         "assembled (global-DOF) entry point, F64 and F32")
     ap.add_argument("--geometry", default="per-point", choices=["per-point", "affine"],
                     help="affine: the same degree and cell count on affine cells through the "
                          "affine operator forms (one geometry set per cell), F64 and F32")
@@ -557,6 +643,11 @@ def main():
     F.load()
     if args.workload in ("batch64", "serve"):
         (run_batch if args.workload == "batch64" else run_serve)(args, rank, world, dev, pg)
+        if pg is not None:
+            pg.destroy_process_group()
+        return
+    if args.assembled:
+        run_assembled(args, rank, world, dev, pg)
         if pg is not None:
             pg.destroy_process_group()
         return

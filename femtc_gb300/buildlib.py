@@ -70,7 +70,7 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
                 sys.stderr.write(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
+    with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     target = lib_path()
     if force or _stale(objs, objs, target):

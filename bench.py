@@ -13,13 +13,21 @@ inputs resident in HBM; `e2e` goes through the host-buffer C-ABI entry point
 (femtc_stiffness_apply_host) with pinned host buffers, so each step includes
 the host->device copy of u and G and the device->host copy of y.
 
+The default run also measures the other benchmark configurations in the
+same process and reports them under "extra": mass P=3 at 4096 cells, the
+precision workload (stiffness P=6, Q=8, 131072 cells, every form's error
+against the FP64 oracle), the 64-mesh batch (one graph launch) and the
+serving stream (p50/p99).  --extra none skips them.
+
 --impl reference times the CPU implementation of the same operator on the
 host cores instead (the reference's algorithm restated in C, OpenMP over
-cells, FP64): that is the reference arm.
+cells, FP64, built with the reference's -Ofast and native-ISA flags): that is
+the reference arm.  It loads nothing of the GPU library.
 
 Multi-GPU: cells are independent (the operator is block diagonal), so N
 ranks run N independent replicas of the workload (weak scaling, no data
-exchange); the step time is the max over ranks.
+exchange); the step time is the max over ranks.  --gpus N without a
+launcher's environment starts the N ranks itself (torch.distributed.run).
 """
 from __future__ import annotations
 
@@ -38,9 +46,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# FP64 FMA throughput measured on a GB300 with a dependent-chain FMA kernel
-# (profiles/gb300_pipe_peaks.md); the measured-peaks file (HBM copy, bf16
-# GEMM) carries no FP64 figure.
+# FP64 FMA throughput of a GB300, measured with an FMA-throughput kernel
+# (8 independent FMA chains per thread on every SM, CUDA events); the
+# measured-peaks file (HBM copy, bf16 GEMM) carries no FP64 figure.
 FP64_PEAK_TFLOPS = 1.20
 FALLBACK_HBM_GBS = 6800.0
 L2_BYTES = 129e6  # GB300 L2
@@ -124,8 +132,9 @@ def bytes_per_cell(op: int, n: int, q: int, es: int, affine: bool = False) -> fl
     return es * (2 * n ** 3 + (1 if op == 0 else 6) * (1 if affine else q ** 3))
 
 
-# DRAM bytes (read + write) of one launch of the headline kernel, measured
-# by ncu on the full workload (profiles/stiffness_p4_32k_cells_slab_kernels.md)
+# DRAM bytes (read + write) of one launch of the headline kernels, from one
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel on
+# the full workload
 MEASURED_TRAFFIC = {("stiffness_p4", 32768, 0): 399.7e6, ("stiffness_p4", 32768, 1): 196.7e6}
 
 
@@ -142,8 +151,10 @@ def roofline(head, ach_tf, ach_gbs, hbm, hbm_src, traffic=None, flop_count=None,
         return {"bound": "fp64", "achieved": ach_tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
                 "frac": ach_tf / FP64_PEAK_TFLOPS, "flop_count": flop_count,
                 "fp64_pipe_instruction_frac": pipe_frac, "traffic": traffic,
-                "traffic_unit": "bytes per launch (ncu, profiles/stiffness_p4_32k_cells_slab_kernels.md)",
-                "peak_source": "measured FP64 FMA pipe (profiles/gb300_pipe_peaks.md)",
+                "traffic_unit": "DRAM bytes per launch (ncu dram__bytes_read.sum + "
+                                "dram__bytes_write.sum, one capture of this kernel on this workload)",
+                "peak_source": "measured FP64 FMA rate of a GB300 (FMA-throughput kernel, "
+                               "CUDA events)",
                 "hbm": hbm_part}
     return {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s", "frac": ach_gbs / hbm,
             "traffic": traffic, "peak_source": hbm_src}
@@ -248,58 +259,99 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def metric_name(base: int, degree: int, nquad: int) -> str:
+    return f"GDoF/s {'stiffness' if base == 1 else 'mass'} action (P={degree}, Q={nquad})"
+
+
+def workload_config(w, world: int, es: int) -> dict:
+    """The `config` of an operator workload's line (both arms)."""
+    bpc = bytes_per_cell(w.base_op, w.n, w.nquad, es, w.affine)
+    flush = bpc * w.ncells < 1.5 * L2_BYTES
+    return {"workload": w.name, "cells": w.ncells, "degree": w.degree, "nquad": w.nquad,
+            "dofs": w.ndofs, "parallelism": f"replicas{world}",
+            "geometry": ("affine: one factor set per cell, weights in the backward tables"
+                         if w.affine else "per quadrature point"),
+            "l2": (f"inputs {bpc * w.ncells / 1e6:.0f} MB "
+                   + ("< 1.5 x 129 MB L2: a 512 MB write between launches flushes it; "
+                      "time = sum of the launches' events" if flush
+                      else "> 1.5 x 129 MB L2, no flush"))}
+
+
+def _cpu_fn(base):
+    import oracle
+    return oracle.mass if base == 0 else oracle.stiffness
+
+
+def cpu_sample(w, fn, cores, seconds):
+    """Cells per call for a call of about `seconds` on `cores` threads,
+    calibrated on a short call."""
+    import oracle
+    c0 = int(min(w.ncells, max(64, 32 * cores)))
+    g = w.point_geometry(c0)
+    fn(oracle.EXACT, w.degree, w.nquad, w.tables, w.u[:c0], g, nthreads=cores, fast=True)
+    t0 = time.perf_counter()
+    fn(oracle.EXACT, w.degree, w.nquad, w.tables, w.u[:c0], g, nthreads=cores, fast=True)
+    per_cell = max((time.perf_counter() - t0) / c0, 1e-9)
+    return int(min(w.ncells, max(c0, seconds / per_cell)))
+
+
 def run_reference(args, rank, world):
-    """CPU arm: the oracle's C restatement of the reference's algorithm."""
+    """CPU arm: the oracle's C restatement of the reference's algorithm,
+    built with the reference's -Ofast and native-ISA flags, OpenMP over
+    cells on every host core; tables from the oracle's own tabulation, so
+    nothing of the GPU library is loaded.  Rank 0 only."""
     if rank != 0:
         return
     import oracle
     from femtc_gb300 import workloads as W
-    oracle.lib()
-    w = W.make(args.workload)
+    if args.workload in ("batch64", "serve"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the reference has no batched or serving path (one operator of one "
+                          "degree per call, src/mass.hpp:196-219)"}), flush=True)
+        return
+    w = W.make(args.workload, ncells=args.cells, tabulate=oracle.tabulate)
     n, q = w.n, w.nquad
-    # bounded sample: enough cells for ~2 s per step on the host cores
-    per_cell_s = 40e-6 if w.op == 1 else 15e-6
     cores = os.cpu_count() or 1
-    sample = int(min(w.ncells, max(256, 2.0 * cores / per_cell_s)))
+    fn = _cpu_fn(w.op)
+    # bounded sample per step: about 1.5 s of CPU work on all host cores
+    sample = cpu_sample(w, fn, cores, 1.5)
     u, g = w.u[:sample], w.geo[:sample]
-    fn = oracle.mass if w.op == 0 else oracle.stiffness
     times = []
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        fn(oracle.EXACT, w.degree, q, w.tables, u, g, nthreads=cores)
+        fn(oracle.EXACT, w.degree, q, w.tables, u, g, nthreads=cores, fast=True)
         t1 = time.perf_counter()
         if i >= args.warmup:
             times.append(t1 - t0)
     t = float(np.mean(times))
     gdofs = sample * n ** 3 / t / 1e9
     line = {
-        "metric": f"GDoF/s {'stiffness' if w.op == 1 else 'mass'} action (P={w.degree}, Q={q})",
+        "metric": metric_name(w.op, w.degree, q),
         "value": gdofs, "unit": "GDoF/s", "impl": "reference", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": args.workload, "cells": w.ncells, "degree": w.degree,
-                                        "nquad": q, "sample_cells": sample},
+        "data": "synthetic", "config": workload_config(w, world, 8),
         "cpu_baseline": {"value": gdofs, "unit": "GDoF/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample} of {w.ncells} cells per step, FP64, OpenMP over cells"},
+                         "sample": f"{sample} of {w.ncells} cells per step, FP64, exact "
+                                   f"operator, OpenMP over cells",
+                         "flags": oracle.fast_flags()},
         "e2e": {"value": gdofs, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 def cpu_baseline(w, seconds=10.0):
-    """Time the oracle's C restatement on the host cores on a bounded sample
-    (affine workloads: the per-point operator on the same mesh, the only
-    form the reference has)."""
+    """Time the oracle's C restatement (its -Ofast native-ISA build) on the
+    host cores on a bounded sample (affine workloads: the per-point operator
+    on the same mesh, the only form the reference has), and on one core."""
     import oracle
-    oracle.lib()
     cores = os.cpu_count() or 1
-    fn = oracle.mass if w.base_op == 0 else oracle.stiffness
-    sample = w.ncells
+    fn = _cpu_fn(w.base_op)
+    sample = cpu_sample(w, fn, cores, 0.5)
     u, g = w.u[:sample], w.point_geometry(sample)
-    fn(oracle.EXACT, w.degree, w.nquad, w.tables, u, g, nthreads=cores)  # warm
     reps, t0 = 0, time.perf_counter()
     while True:
-        fn(oracle.EXACT, w.degree, w.nquad, w.tables, u, g, nthreads=cores)
+        fn(oracle.EXACT, w.degree, w.nquad, w.tables, u, g, nthreads=cores, fast=True)
         reps += 1
         el = time.perf_counter() - t0
         if el >= seconds:
@@ -310,13 +362,15 @@ def cpu_baseline(w, seconds=10.0):
     u1, g1 = u[:s1], g[:s1]
     reps1, t0 = 0, time.perf_counter()
     while True:
-        fn(oracle.EXACT, w.degree, w.nquad, w.tables, u1, g1, nthreads=1)
+        fn(oracle.EXACT, w.degree, w.nquad, w.tables, u1, g1, nthreads=1, fast=True)
         reps1 += 1
         el1 = time.perf_counter() - t0
         if el1 >= seconds / 4:
             break
     return {"value": v, "unit": "GDoF/s", "cores": cores, "kind": "port",
-            "sample": f"{reps} x {sample} cells of the workload, FP64, OpenMP over cells, {el:.1f} s",
+            "sample": f"{reps} x {sample} cells of the workload, FP64, exact operator, "
+                      f"OpenMP over cells, {el:.1f} s",
+            "flags": oracle.fast_flags(),
             "value_1core": reps1 * s1 * w.n ** 3 / el1 / 1e9,
             "sample_1core": f"{reps1} x {s1} cells, one thread, {el1:.1f} s"}
 
@@ -377,11 +431,21 @@ def run_batch(args, rank, world, dev, pg):
     out["f64"] = {"separate": {"ms": ms64, "gdofs": ndofs / ms64 / 1e6,
                                "hbm_gbs": 2 * nbytes / ms64 / 1e6}}
 
+    # every mesh's error against the FP64 oracle on its first cells (the
+    # FP64 geometry the GPU computed, copied back)
+    import oracle
+    err_cells = [min(n, 128) for _, _, n in spec]
+    oracle_y = []
+    for (op, P, Q, tables, u64, y64, geo64, n), k in zip(meshes64, err_cells):
+        fn = oracle.mass if op == F.MASS else oracle.stiffness
+        oracle_y.append(fn(oracle.EXACT, P, Q, tables, u64[:k].cpu().numpy(),
+                           geo64[:k].cpu().numpy()))
+
     def max_rel_err():
         worst = 0.0
-        for m32, m64 in zip(meshes, meshes64):
-            y, y64 = m32[5], m64[5]
-            worst = max(worst, ((y.double() - y64).abs().max() / y64.abs().max()).item())
+        for m32, yo, k in zip(meshes, oracle_y, err_cells):
+            y = m32[5][:k].double().cpu().numpy()
+            worst = max(worst, float(np.abs(y - yo).max() / np.abs(yo).max()))
         return worst
 
     for dtype in (F.F32, F.BF16X3, F.F16X2):
@@ -399,7 +463,7 @@ def run_batch(args, rank, world, dev, pg):
             ms = timed(step)
             res[mode] = {"ms": ms, "gdofs": ndofs / ms / 1e6, "hbm_gbs": nbytes / ms / 1e6}
             if mode == "graph":
-                res["max_rel_err_vs_f64"] = max_rel_err()
+                res["max_rel_err_vs_fp64_oracle"] = max_rel_err()
         res["speedup_vs_f64_plain"] = res["graph"]["gdofs"] / out["f64"]["separate"]["gdofs"]
         res["info"] = b.info()
         b.close()
@@ -421,7 +485,8 @@ def run_batch(args, rank, world, dev, pg):
                          "frac": head["hbm_gbs"] / hbm, "traffic": None, "peak_source": src},
             "forms": out,
         }
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def run_serve(args, rank, world, dev, pg):
@@ -499,7 +564,8 @@ def run_serve(args, rank, world, dev, pg):
             "mean_outer_iters": float(np.mean([r["outer_iters"] for r in results])),
             "mean_inner_iters": float(np.mean([r["inner_iters"] for r in results])),
         }
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def box_shape(ncells: int):
@@ -591,68 +657,17 @@ def torch_free_bytes(dev):
     return free
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--impl", default="femtc", choices=["femtc", "reference"])
-    ap.add_argument("--workload", default="stiffness_p4",
-                    choices=["stiffness_p4", "mass_p3", "stiffness_p6", "batch64", "serve"])
-    ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
-    ap.add_argument("--serve-policy", default="shortest", choices=["shortest", "fifo"],
-                    help="serve: admission order (shortest estimated work first, with aging; "
-                         "or arrival order)")
-    ap.add_argument("--inner-dtype", default="f32", choices=["f32", "f16x2", "bf16x3"],
-                    help="serve: operator form of the inner CG (FP64 refinement outside)")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-batch-tune", action="store_true",
-                    help="batch64: built-in tile layouts (no autotuning launches; profiling)")
-    ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
-    ap.add_argument("--assembled", action="store_true",
-                    help="the workload's cells as a box mesh with shared DOFs, through the "
-                         "assembled (global-DOF) entry point, F64 and F32")
-    ap.add_argument("--geometry", default="per-point", choices=["per-point", "affine"],
-                    help="affine: the same degree and cell count on affine cells through the "
-                         "affine operator forms (one geometry set per cell), F64 and F32")
-    ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3,f64e,f64plain",
-                    help="comma list of forms to time; the first is the headline")
-    ap.add_argument("--tile-db", default=None,
-                    help="tile configuration file: loaded if it exists (no tuning), "
-                         "else written after autotuning")
-    args = ap.parse_args()
-    args.warmup = max(args.warmup, 3)
-    rank, world, local = dist_env()
-
-    if args.impl == "reference":
-        run_reference(args, rank, world)
-        return
-
+def run_operator(args, name, dtypes_arg, rank, world, dev, pg, local, e2e_on=True,
+                 cpu_seconds=10.0, ncells=None, clocks=True):
+    """One operator workload: every form in `dtypes_arg` (the first is the
+    headline) with inputs resident in HBM, the host-buffer entry point (e2e)
+    and the CPU baseline; returns the line (rank 0) or None."""
     import torch
     import femtc_gb300 as F
     from femtc_gb300 import workloads as W
+    from femtc_gb300 import replicas
 
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-        pg = dist
-    F.load()
-    if args.workload in ("batch64", "serve"):
-        (run_batch if args.workload == "batch64" else run_serve)(args, rank, world, dev, pg)
-        if pg is not None:
-            pg.destroy_process_group()
-        return
-    if args.assembled:
-        run_assembled(args, rank, world, dev, pg)
-        if pg is not None:
-            pg.destroy_process_group()
-        return
-
-    w = (W.make_affine if args.geometry == "affine" else W.make)(args.workload, ncells=args.cells)
+    w = (W.make_affine if args.geometry == "affine" else W.make)(name, ncells=ncells)
     # op: the entry point's operator code; base: mass (0) or stiffness (1)
     n, q, op, base = w.n, w.nquad, w.op, w.base_op
     tabs = w.op_tables()
@@ -664,15 +679,13 @@ def main():
     names["f64plain"] = F64PLAIN
     dname = dict(F.DTYPE_NAMES)
     dname[F64PLAIN] = "f64plain"
-    dtypes = [names[d] for d in args.dtypes.split(",")]
+    dtypes = [names[d] for d in dtypes_arg.split(",")]
     head = dtypes[0]
 
     def barrier():
         if pg is not None:
             pg.barrier()
         torch.cuda.synchronize()
-
-    from femtc_gb300 import replicas
 
     def maxreduce(x):
         return replicas.max_over_ranks(x, device=dev)
@@ -721,7 +734,7 @@ def main():
         barrier()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
-        sampler = ClockSampler(local) if key == head else None
+        sampler = ClockSampler(local) if (key == head and clocks) else None
         if sampler:
             sampler.__enter__()
         barrier()
@@ -736,7 +749,8 @@ def main():
             step()
             ev[i][1].record(stream)
         t_end.record(stream)
-        launches_timed[0] += F.operator_launches() - l0
+        if key == head:
+            launches_timed[0] += F.operator_launches() - l0
         barrier()
         if sampler:
             sampler.__exit__(None, None, None)
@@ -767,7 +781,7 @@ def main():
     # Grace-Blackwell link (zero-copy), mode 1 stages them through device
     # copies; both include every byte's host->device and device->host move
     e2e = {}
-    for dtype in ([] if args.no_e2e else [head]):
+    for dtype in ([head] if e2e_on else []):
         npdt = np.float64 if dtype in F.FP64_STORAGE else np.float32
         uh = torch.from_numpy(w.u.astype(npdt)).pin_memory()
         gh = torch.from_numpy(w.geo.astype(npdt)).pin_memory()
@@ -789,7 +803,8 @@ def main():
                 estep()
             barrier()
             el = maxreduce(time.perf_counter() - t0)
-            launches_timed[0] += F.operator_launches() - l0
+            if mode == 0:
+                launches_timed[0] += F.operator_launches() - l0
             e2e[(dtype, mode)] = dict(gdofs=world * args.steps * w.ndofs / el / 1e9,
                                       h2d=uh.numel() * uh.element_size() + gh.numel() * gh.element_size(),
                                       d2h=yh.numel() * yh.element_size())
@@ -823,46 +838,153 @@ def main():
             "tile": {"cells": res["tile"][0], "geo_staged": res["tile"][1], "threads": res["tile"][2],
                      "lanes_per_slab": res["tile"][3]},
         }
-    if rank == 0:
-        line = {
-            "metric": f"GDoF/s {'stiffness' if base == 1 else 'mass'} action (P={w.degree}, Q={q})",
-            "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": F.DTYPE_NAMES[head], "data": "synthetic",
-            "config": {"workload": w.name, "cells": w.ncells, "degree": w.degree, "nquad": q,
-                       "dofs": w.ndofs, "parallelism": f"replicas{world}",
-                       "geometry": ("affine: one factor set per cell, weights in the backward "
-                                    "tables" if w.affine else "per quadrature point"),
-                       "l2": (f"inputs {bpc * w.ncells / 1e6:.0f} MB "
-                              + ("< 1.5 x 129 MB L2: a 512 MB write between launches flushes "
-                                 "it; time = sum of the launches' events" if r["l2_flush"]
-                                 else "> 1.5 x 129 MB L2, no flush"))},
-            "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src,
-                                 traffic_for(w.name, w.ncells, head),
-                                 flop_count=("even-odd kernel operations per cell "
-                                             f"{fpc_head:.0f} (reference convention {fpc:.0f})")
-                                 if head == F.F64 else None, pipe_frac=pipe_frac),
-            "gpu_launches": launches_timed[0],
-            "clocks": r["clocks"],
-            "variants": variants,
-        }
-        if (head, 0) in e2e:
-            a, z, c = e2e[(head, 0)], e2e[(head, 2)], e2e[(head, 1)]
-            h2d_gbs, d2h_gbs = host_link_gbs(dev)
-            link_s = max(a["h2d"] / (h2d_gbs * 1e9), a["d2h"] / (d2h_gbs * 1e9))
-            line["e2e"] = {"value": a["gdofs"], "unit": "GDoF/s",
-                           "h2d_bytes_per_step": a["h2d"], "d2h_bytes_per_step": a["d2h"],
-                           "path": "femtc_*_apply_host, pinned host buffers, host-path mode "
-                                   "auto (tuned: zero-copy or staging pipeline)",
-                           "zero_copy_gdofs": z["gdofs"], "staging_pipeline_gdofs": c["gdofs"],
-                           "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
-                           "host_link_ceiling_gdofs": w.ndofs / link_s / 1e9}
-        if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(w)
-        print(json.dumps(line), flush=True)
-    if pg is not None:
-        pg.destroy_process_group()
+    if "f64plain" in variants:
+        base_g = variants["f64plain"]["gdofs"]
+        for k, v in variants.items():
+            v["vs_f64_plain"] = v["gdofs"] / base_g
+    if rank != 0:
+        return None
+    line = {
+        "metric": metric_name(base, w.degree, q),
+        "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": F.DTYPE_NAMES[head], "data": "synthetic",
+        "config": workload_config(w, world, 8 if head in F.FP64_STORAGE else 4),
+        "roofline": roofline(head, ach_tf, ach_gbs, hbm, hbm_src,
+                             traffic_for(w.name, w.ncells, head),
+                             flop_count=("even-odd kernel operations per cell "
+                                         f"{fpc_head:.0f} (reference convention {fpc:.0f})")
+                             if head == F.F64 else None, pipe_frac=pipe_frac),
+        "gpu_launches": launches_timed[0],
+        "clocks": r["clocks"],
+        "variants": variants,
+    }
+    if (head, 0) in e2e:
+        a, z, c = e2e[(head, 0)], e2e[(head, 2)], e2e[(head, 1)]
+        h2d_gbs, d2h_gbs = host_link_gbs(dev)
+        link_s = max(a["h2d"] / (h2d_gbs * 1e9), a["d2h"] / (d2h_gbs * 1e9))
+        line["e2e"] = {"value": a["gdofs"], "unit": "GDoF/s",
+                       "h2d_bytes_per_step": a["h2d"], "d2h_bytes_per_step": a["d2h"],
+                       "path": "femtc_*_apply_host, pinned host buffers, host-path mode "
+                               "auto (tuned: zero-copy or staging pipeline)",
+                       "zero_copy_gdofs": z["gdofs"], "staging_pipeline_gdofs": c["gdofs"],
+                       "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
+                       "host_link_ceiling_gdofs": w.ndofs / link_s / 1e9}
+    if cpu_seconds > 0:
+        line["cpu_baseline"] = cpu_baseline(w, cpu_seconds)
+    return line
+
+
+def self_launch(args) -> None:
+    """--gpus N > 1 outside a launcher: start N local ranks through
+    torch.distributed.run (one per GPU, rendezvous on 127.0.0.1) and exit
+    with their status."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={args.gpus}", "--master-addr", "127.0.0.1",
+           "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    sys.exit(subprocess.call(cmd))
+
+
+EXTRA_DEFAULT = "mass_p3,stiffness_p6,batch64,serve"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="femtc", choices=["femtc", "reference"])
+    ap.add_argument("--workload", default="stiffness_p4",
+                    choices=["stiffness_p4", "mass_p3", "stiffness_p6", "batch64", "serve"])
+    ap.add_argument("--extra", default=None,
+                    help="comma list of further workloads measured in the same run and "
+                         f"reported under 'extra' (default with the default workload: "
+                         f"{EXTRA_DEFAULT}; 'none' for none)")
+    ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
+    ap.add_argument("--serve-policy", default="shortest", choices=["shortest", "fifo"],
+                    help="serve: admission order (shortest estimated work first, with aging; "
+                         "or arrival order)")
+    ap.add_argument("--inner-dtype", default="f32", choices=["f32", "f16x2", "bf16x3"],
+                    help="serve: operator form of the inner CG (FP64 refinement outside)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch-tune", action="store_true",
+                    help="batch64: built-in tile layouts (no autotuning launches; profiling)")
+    ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling)")
+    ap.add_argument("--assembled", action="store_true",
+                    help="the workload's cells as a box mesh with shared DOFs, through the "
+                         "assembled (global-DOF) entry point, F64 and F32")
+    ap.add_argument("--geometry", default="per-point", choices=["per-point", "affine"],
+                    help="affine: the same degree and cell count on affine cells through the "
+                         "affine operator forms (one geometry set per cell), F64 and F32")
+    ap.add_argument("--dtypes", default="f64,f32,f16x2,bf16x3,f64e,f64plain",
+                    help="comma list of forms to time; the first is the headline")
+    ap.add_argument("--tile-db", default=None,
+                    help="tile configuration file: loaded if it exists (no tuning), "
+                         "else written after autotuning")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        self_launch(args)
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import femtc_gb300 as F
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    F.load()
+
+    def finish(line):
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        if pg is not None:
+            pg.destroy_process_group()
+
+    if args.workload in ("batch64", "serve"):
+        finish((run_batch if args.workload == "batch64" else run_serve)(args, rank, world, dev, pg))
+        return
+    if args.assembled:
+        run_assembled(args, rank, world, dev, pg)
+        finish(None)
+        return
+
+    line = run_operator(args, args.workload, args.dtypes, rank, world, dev, pg, local,
+                        e2e_on=not args.no_e2e,
+                        cpu_seconds=0.0 if args.no_cpu_baseline else 10.0, ncells=args.cells)
+    extra = args.extra
+    if extra is None:
+        extra = (EXTRA_DEFAULT if args.workload == "stiffness_p4" and args.cells is None
+                 and args.geometry == "per-point" else "none")
+    extras = {}
+    for name in [e for e in extra.split(",") if e and e != "none"]:
+        t0 = time.perf_counter()
+        if name in ("batch64", "serve"):
+            x = (run_batch if name == "batch64" else run_serve)(args, rank, world, dev, pg)
+        else:
+            x = run_operator(args, name, "f64,f32,f16x2,bf16x3,f64e,f64plain", rank, world, dev,
+                             pg, local, e2e_on=(name == "mass_p3" and not args.no_e2e),
+                             cpu_seconds=0.0 if args.no_cpu_baseline else 3.0, clocks=False)
+        if x is not None:
+            x["wall_s"] = time.perf_counter() - t0
+            extras[name] = x
+    if line is not None and extras:
+        line["extra"] = extras
+    finish(line)
 
 
 if __name__ == "__main__":

@@ -15,7 +15,10 @@ make_affine(name) gives the same degree, Q and cell count on affine cells
 (J = I + 0.1 N(0,1) per cell, u ~ U(-1,1)) with one geometry set per cell:
 detJ (mass) or detJ J^-1 J^-T (stiffness), for the affine operator forms.
 
-Layouts follow include/femtc_gpu.h.  Seeds are fixed per workload.
+Layouts follow include/femtc_gpu.h.  Seeds are fixed per workload.  The
+basis tables come from the library's femtc_tabulate unless the caller passes
+another `tabulate(degree, nquad)` with the same result (a CPU-only caller
+that must not load the GPU library).
 """
 from __future__ import annotations
 
@@ -109,19 +112,21 @@ def _spec(name: str):
     raise ValueError(f"unknown workload {name}")
 
 
-def make(name: str, ncells: int | None = None, seed: int | None = None) -> Workload:
+def make(name: str, ncells: int | None = None, seed: int | None = None,
+         tabulate=None) -> Workload:
     degree, nquad, op, nc, sd = _spec(name)
     return make_custom(name, op, degree, nquad, ncells or nc, sd if seed is None else seed,
-                       smooth=(name == "stiffness_p6"))
+                       smooth=(name == "stiffness_p6"), tabulate=tabulate)
 
 
-def make_affine(name: str, ncells: int | None = None, seed: int | None = None) -> Workload:
+def make_affine(name: str, ncells: int | None = None, seed: int | None = None,
+                tabulate=None) -> Workload:
     """The named workload's degree, Q and cell count on affine cells, with
     one geometry set per cell (the affine operator forms)."""
     degree, nquad, op, nc, sd = _spec(name)
     ncells = ncells or nc
     rng = np.random.default_rng(sd if seed is None else seed)
-    tables, _, w, _ = _lib.tabulate(degree, nquad)
+    tables, _, w, _ = (tabulate or _lib.tabulate)(degree, nquad)
     J = random_jacobians(rng, ncells)
     if op == _lib.MASS:
         geo, aop = np.linalg.det(J), _lib.MASS_AFFINE
@@ -134,10 +139,10 @@ def make_affine(name: str, ncells: int | None = None, seed: int | None = None) -
 
 
 def make_custom(name: str, op: int, degree: int, nquad: int, ncells: int, seed: int,
-                smooth: bool = False) -> Workload:
+                smooth: bool = False, tabulate=None) -> Workload:
     rng = np.random.default_rng(seed)
     n = degree + 1
-    tables, x, w, z = _lib.tabulate(degree, nquad)
+    tables, x, w, z = (tabulate or _lib.tabulate)(degree, nquad)
     w3 = tensor_weights(w)
     if op == _lib.MASS:
         detj = rng.uniform(0.5, 1.5, size=(ncells, nquad ** 3))

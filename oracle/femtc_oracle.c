@@ -3,6 +3,7 @@
  * CPU-baseline leg load it; nothing in the product calls it.
  *
  * Restates, in plain C, the per-cell algorithm of IgorBaratta/femtc:
+ *   linalg::gemm_micro         src/linalg.hpp:45-94
  *   linalg::gemm_blocked       src/linalg.hpp:101-182
  *   operators::mass_operator   src/mass.hpp:10-49
  *   transform                  src/stiffness.hpp:14-29
@@ -82,6 +83,35 @@ FORCE_INLINE void contract_axis(int axis, int d0, int d1, int d2, int M,
   }
 }
 
+/* One axis contraction in the reference's rotating form (src/linalg.hpp:
+ * 101-182, as the operators chain it, src/mass.hpp:36-47): `in` is K x L
+ * row-major (the contracted axis slowest, L = the other two axes), `out`
+ * is L x M row-major, out[j*M + m] = sum_p A(m,p) in[p*L + j] with
+ * A(m,p) = A[m*sm + p*sk].  The contracted axis becomes the fastest, so
+ * three contractions return a tensor to its axis order.  Products are added
+ * from zero in increasing p (gemm_micro's kij order, :73-79), into a row
+ * of L values that is then written with stride M (gemm_blocked's copy of
+ * its Ctemp block, :128-136). */
+FORCE_INLINE void rot_contract(int K, int L, int M, const double* A, int sm,
+                               int sk, const double* in, double* out)
+{
+  double row[4096];
+  for (int m = 0; m < M; ++m)
+  {
+    for (int j = 0; j < L; ++j)
+      row[j] = 0.0;
+    for (int p = 0; p < K; ++p)
+    {
+      const double a = A[m * sm + p * sk];
+      const double* x = in + p * L;
+      for (int j = 0; j < L; ++j)
+        row[j] += a * x[j];
+    }
+    for (int j = 0; j < L; ++j)
+      out[j * M + m] = row[j];
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 void oracle_gemm_blocked(int k, int m, int n, const double* a, const double* b,
                          double* c)
@@ -96,6 +126,18 @@ void oracle_gemm_blocked(int k, int m, int n, const double* a, const double* b,
         s += a[i + p * m] * b[p * n + j];
       c[i + j * m] = s;
     }
+}
+
+void oracle_gemm_micro(int k, int m, int nc, int lda, int ldb, int ldc,
+                       const double* a, const double* b, double* c)
+{
+  /* src/linalg.hpp:45-94: c(i,j) += sum_p a[i + p*lda] * b[p*ldb + j], c
+   * row-major with leading dimension ldc; the kij order (:73-79) adds the
+   * products into c in increasing p. */
+  for (int p = 0; p < k; ++p)
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < nc; ++j)
+        c[i * ldc + j] += a[i + p * lda] * b[p * ldb + j];
 }
 
 void oracle_gemm_blocked_batched(int k, int m, int n, const double* a,
@@ -135,17 +177,17 @@ FORCE_INLINE void mass_cell(int sem, int N, int Q, const double* phi,
                             const double* u, const double* D, double* y,
                             double* w1, double* w2, double* w3)
 {
-  contract_axis(0, N, N, N, Q, phi, 1, Q, u, w1);
-  contract_axis(1, Q, N, N, Q, phi, 1, Q, w1, w2);
-  contract_axis(2, Q, Q, N, Q, phi, 1, Q, w2, w3);
+  rot_contract(N, N * N, Q, phi, 1, Q, u, w1);
+  rot_contract(N, N * Q, Q, phi, 1, Q, w1, w2);
+  rot_contract(N, Q * Q, Q, phi, 1, Q, w2, w3);
   const int nq = Q * Q * Q;
   for (int i = 0; i < nq; ++i)
     w3[i] *= D[i];
   const int bsm = (sem == ORACLE_EXACT) ? Q : 1;
   const int bsk = (sem == ORACLE_EXACT) ? 1 : Q;
-  contract_axis(0, Q, Q, Q, N, phi, bsm, bsk, w3, w1);
-  contract_axis(1, N, Q, Q, N, phi, bsm, bsk, w1, w2);
-  contract_axis(2, N, N, Q, N, phi, bsm, bsk, w2, y);
+  rot_contract(Q, Q * Q, N, phi, bsm, bsk, w3, w1);
+  rot_contract(Q, Q * N, N, phi, bsm, bsk, w1, w2);
+  rot_contract(Q, N * N, N, phi, bsm, bsk, w2, y);
 }
 
 /* src/stiffness.hpp:14-29, G components [zz,yz,xz,yy,xy,xx] per point. */
@@ -163,34 +205,38 @@ FORCE_INLINE void transform(int nq, const double* G, double* f0, double* f1,
 }
 
 /* Forward 3-contraction chain with per-axis tables (forward tables
- * A(q,i) = t[q + i*Q]). */
+ * A(q,i) = t[q + i*Q]), axis 0 first. */
 FORCE_INLINE void chain_fwd(int N, int Q, const double* t0, const double* t1,
                             const double* t2, const double* u, double* out,
                             double* w1, double* w2)
 {
-  contract_axis(0, N, N, N, Q, t0, 1, Q, u, w1);
-  contract_axis(1, Q, N, N, Q, t1, 1, Q, w1, w2);
-  contract_axis(2, Q, Q, N, Q, t2, 1, Q, w2, out);
+  rot_contract(N, N * N, Q, t0, 1, Q, u, w1);
+  rot_contract(N, N * Q, Q, t1, 1, Q, w1, w2);
+  rot_contract(N, Q * Q, Q, t2, 1, Q, w2, out);
 }
 
 /* Backward chain: transposed tables (exact) or the forward tables again
- * (reference semantics, Q == N). */
+ * (reference semantics, Q == N), axis 0 first. */
 FORCE_INLINE void chain_bwd(int N, int Q, int sm, int sk, const double* t0,
                             const double* t1, const double* t2,
                             const double* f, double* out, double* w1,
                             double* w2)
 {
-  contract_axis(0, Q, Q, Q, N, t0, sm, sk, f, w1);
-  contract_axis(1, N, Q, Q, N, t1, sm, sk, w1, w2);
-  contract_axis(2, N, N, Q, N, t2, sm, sk, w2, out);
+  rot_contract(Q, Q * Q, N, t0, sm, sk, f, w1);
+  rot_contract(Q, Q * N, N, t1, sm, sk, w1, w2);
+  rot_contract(Q, N * N, N, t2, sm, sk, w2, out);
 }
 
 /* Stiffness, one cell.  Exact: y = sum_d D_d^T (G D u)_d with
- * D_x = Gamma x Phi x Phi (axis 0 = x, slowest).  Reference semantics
- * (src/stiffness.hpp:68-97): Wx = (Gamma,Phi,Phi)u, Wy = (Phi,Gamma,Phi)u,
- * Wz = (Phi,Phi,Phi)u (no derivative, :76-77), transform, and only the last
- * backward chain (Phi,Phi,Gamma) survives because each chain assigns W
- * (:85,91,97). */
+ * D_x = Gamma x Phi x Phi (axis 0 = x, slowest), evaluated with shared
+ * partial contractions: forward Phi_0 u and Gamma_0 u feed the three
+ * gradients (2 + 3 + 3 contractions), backward the x and y chains meet
+ * before their common last table (3 + 3 + 2), 16 contractions per cell
+ * against the reference's 17
+ * (src/stiffness.hpp:68-97).  Reference semantics (src/stiffness.hpp:68-97):
+ * Wx = (Gamma,Phi,Phi)u, Wy = (Phi,Gamma,Phi)u, Wz = (Phi,Phi,Phi)u (no
+ * derivative, :76-77), transform, and only the last backward chain
+ * (Phi,Phi,Gamma) survives because each chain assigns W (:85,91,97). */
 FORCE_INLINE void stiffness_cell(int sem, int N, int Q, const double* tab,
                                  const double* u, const double* G, double* y,
                                  double* gx, double* gy, double* gz,
@@ -198,26 +244,40 @@ FORCE_INLINE void stiffness_cell(int sem, int N, int Q, const double* tab,
 {
   const double* P = tab;
   const double* D = tab + Q * N;
-  const int nq = Q * Q * Q, nd = N * N * N;
-  chain_fwd(N, Q, D, P, P, u, gx, w1, w2);
-  chain_fwd(N, Q, P, D, P, u, gy, w1, w2);
-  if (sem == ORACLE_EXACT)
-    chain_fwd(N, Q, P, P, D, u, gz, w1, w2);
-  else
-    chain_fwd(N, Q, P, P, P, u, gz, w1, w2);
-  transform(nq, G, gx, gy, gz);
+  const int nq = Q * Q * Q, nd = N * N * N, nh = Q * N * N;
   if (sem == ORACLE_EXACT)
   {
-    chain_bwd(N, Q, Q, 1, D, P, P, gx, y, w1, w2);
-    chain_bwd(N, Q, Q, 1, P, D, P, gy, tmp, w1, w2);
+    /* forward: axis 0, then 1, then 2 (each contraction rotates the axes) */
+    rot_contract(N, N * N, Q, P, 1, Q, u, w1);    /* Phi_0 u   */
+    rot_contract(N, N * N, Q, D, 1, Q, u, w2);    /* Gamma_0 u */
+    rot_contract(N, N * Q, Q, P, 1, Q, w2, tmp);
+    rot_contract(N, Q * Q, Q, P, 1, Q, tmp, gx); /* d/dx */
+    rot_contract(N, N * Q, Q, D, 1, Q, w1, tmp);
+    rot_contract(N, Q * Q, Q, P, 1, Q, tmp, gy); /* d/dy */
+    rot_contract(N, N * Q, Q, P, 1, Q, w1, tmp);
+    rot_contract(N, Q * Q, Q, D, 1, Q, tmp, gz); /* d/dz */
+    transform(nq, G, gx, gy, gz);
+    /* backward: axis 0, then 1, then 2; the x and y chains share the last
+     * table (Phi_2^T), so they are summed before it */
+    rot_contract(Q, Q * Q, N, D, Q, 1, gx, w1);  /* Gamma_0^T fx */
+    rot_contract(Q, Q * Q, N, P, Q, 1, gy, w2);  /* Phi_0^T fy   */
+    rot_contract(Q, Q * Q, N, P, Q, 1, gz, gx);  /* Phi_0^T fz   */
+    rot_contract(Q, Q * N, N, P, Q, 1, w1, tmp); /* x: Phi_1^T   */
+    rot_contract(Q, Q * N, N, D, Q, 1, w2, gy);  /* y: Gamma_1^T */
+    rot_contract(Q, Q * N, N, P, Q, 1, gx, w1);  /* z: Phi_1^T   */
+    for (int i = 0; i < nh; ++i)
+      tmp[i] += gy[i];
+    rot_contract(Q, N * N, N, P, Q, 1, tmp, y);  /* x + y: Phi_2^T */
+    rot_contract(Q, N * N, N, D, Q, 1, w1, w2);  /* z: Gamma_2^T   */
     for (int i = 0; i < nd; ++i)
-      y[i] += tmp[i];
-    chain_bwd(N, Q, Q, 1, P, P, D, gz, tmp, w1, w2);
-    for (int i = 0; i < nd; ++i)
-      y[i] += tmp[i];
+      y[i] += w2[i];
   }
   else
   {
+    chain_fwd(N, Q, D, P, P, u, gx, w1, w2);
+    chain_fwd(N, Q, P, D, P, u, gy, w1, w2);
+    chain_fwd(N, Q, P, P, P, u, gz, w1, w2);
+    transform(nq, G, gx, gy, gz);
     chain_bwd(N, Q, 1, Q, P, P, D, gz, y, w1, w2);
   }
 }

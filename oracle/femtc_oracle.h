@@ -38,6 +38,12 @@ enum { ORACLE_EXACT = 0, ORACLE_REFERENCE = 1 };
 void oracle_gemm_blocked(int k, int m, int n, const double* a, const double* b,
                          double* c);
 
+/* linalg::gemm_micro restated (src/linalg.hpp:45-94): c += a.b with a
+ * column-major (m x k, leading dimension lda), b row-major (k x nc, ldb), c
+ * row-major (m x nc, ldc); products added in increasing p (kij order). */
+void oracle_gemm_micro(int k, int m, int nc, int lda, int ldb, int ldc,
+                       const double* a, const double* b, double* c);
+
 /* One cell-batched axis contraction as used by the operators: for each cell
  * c, C_c[i + j*m] = sum_p A[i + p*m] * B_c[p*n + j]. */
 void oracle_gemm_blocked_batched(int k, int m, int n, const double* a,

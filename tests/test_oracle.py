@@ -51,7 +51,8 @@ def test_oracle_reference_semantics_vs_golden(orc, P, op):
     t, u, g = z[f"{op}_P{P}_tables"], z[f"{op}_P{P}_u"], z[f"{op}_P{P}_geo"]
     fn = orc.mass if op == "mass" else orc.stiffness
     y = fn(orc.REFERENCE, P, P + 1, t, u, g)
-    assert relerr(y, z[f"{op}_P{P}_f64_y"]) <= 1e-13
+    # the same products summed in the same order: bit for bit
+    assert np.array_equal(y, z[f"{op}_P{P}_f64_y"])
 
 
 @pytest.mark.skipif(not __import__("oracle").ref_available(), reason="oracle/_ref not built")
@@ -66,7 +67,7 @@ def test_oracle_vs_reference_fresh(orc, P):
         else:
             yr = orc.ref_stiffness(P, t, u, g)
             yo = orc.stiffness(orc.REFERENCE, P, P + 1, t, u, g)
-        assert relerr(yo, yr) <= 1e-13
+        assert np.array_equal(yo, yr)
 
 
 @pytest.mark.parametrize("P", [1, 2, 3, 4, 6, 7])
@@ -118,6 +119,44 @@ def test_apply_contractions_matches_dense(orc):
     M = [I.reshape(nb, na).T for I in (I0, I1, I2)]
     ref = np.einsum("ai,bj,ck,nijk->nabc", *M, B.reshape(nc, nb, nb, nb)).reshape(-1)
     assert relerr(a_nt, ref) <= 1e-14
+
+
+def test_oracle_tabulate_matches_library(femtc):
+    # two independent restatements of the GLL-to-Gauss tables (numpy's
+    # Legendre module vs the library's Newton iterations)
+    import oracle
+    for P in range(1, 26):
+        for Q in (P + 1, P + 2, P + 3):
+            for a, b in zip(oracle.tabulate(P, Q), femtc.tabulate(P, Q)):
+                assert np.abs(a - b).max() <= 1e-12 * max(1.0, np.abs(b).max())
+
+
+def test_fast_build_agrees_with_parity_build():
+    # the timing build (-Ofast, native ISA) computes the same operators to
+    # rounding
+    import oracle
+    from femtc_gb300 import workloads as W
+    for op, P, Q in ((0, 3, 5), (1, 4, 6)):
+        w = W.make_custom("t", op, P, Q, 17, seed=5, tabulate=oracle.tabulate)
+        fn = oracle.mass if op == 0 else oracle.stiffness
+        a = fn(oracle.EXACT, P, Q, w.tables, w.u, w.geo)
+        b = fn(oracle.EXACT, P, Q, w.tables, w.u, w.geo, fast=True)
+        assert relerr(b, a) <= 1e-13
+
+
+def test_gemm_micro_oracle_matches_loop(orc):
+    # src/linalg.hpp:45-94 at the reference's own test sizes
+    # (tests/test_micro.cpp:24-29: k=26, m=4, n=16, lda=4, ldb=ldc=16)
+    rng = np.random.default_rng(7)
+    k, m, n, lda, ldb, ldc = 26, 4, 16, 4, 16, 16
+    a, b, c0 = rng.uniform(size=lda * k), rng.uniform(size=k * ldb), rng.uniform(size=m * ldc)
+    c = orc.gemm_micro(k, m, n, lda, ldb, ldc, a, b, c0)
+    ref = c0.copy()
+    for i in range(m):
+        for j in range(n):
+            for p in range(k):
+                ref[i * ldc + j] += a[i + p * lda] * b[p * ldb + j]
+    assert np.abs(c - ref).max() <= 1e-12
 
 
 def test_cg_oracle_converges(orc, femtc):

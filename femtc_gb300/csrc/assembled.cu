@@ -163,9 +163,19 @@ int femtc_assembled_apply(int op, int dtype, int semantics, int degree, int nqua
     return aux_fail(FEMTC_ERR_INVALID, "assembled apply: degree must be at least 1");
   if (!femtc_supported(op, dtype, semantics, degree, nquad))
     return aux_fail(FEMTC_ERR_UNSUPPORTED, "assembled apply: no such cell operator variant");
-  if (ncells == 0 || ndofs == 0)
+  const size_t n = (size_t)degree + 1;
+  if (ncells * n * n * n >= (size_t)INT32_MAX || ndofs >= (size_t)INT32_MAX)
+    return aux_fail(FEMTC_ERR_INVALID,
+                    "assembled apply: more than 2^31 local or global DOFs (int32 maps)");
+  if (ndofs == 0)
     return FEMTC_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (ncells == 0)
+  {
+    // no cells: every global DOF's sum is empty
+    cudaError_t e = cudaMemsetAsync(y, 0, ndofs * elem_bytes(dtype), st);
+    return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  }
   if (elem_bytes(dtype) == 8)
     return run<double>(op, dtype, semantics, degree, nquad, tables, dofmap, offsets, entries,
                        ndofs, static_cast<const double*>(x), static_cast<double*>(y), geo,

@@ -117,6 +117,14 @@ namespace
 
 const BatchKernelInfo* batch_family_for(int dtype) { return family_for(dtype); }
 
+void register_batch_faults(std::vector<FaultReader>& f)
+{
+  f.push_back(batch_kernel_f32().read_fault);
+  f.push_back(batch_kernel_f32eo().read_fault);
+  f.push_back(batch_kernel_f16x2().read_fault);
+  f.push_back(batch_kernel_bf16x3().read_fault);
+}
+
 bool even_odd_tables_f32(const float* tab, int n, int q, int ntab); // femtc_abi.cu
 
 int batch_setup(femtc_batch* b, int dtype, const femtc_batch_item* items, int nitems,

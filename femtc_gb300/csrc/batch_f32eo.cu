@@ -8,6 +8,7 @@ namespace femtc
 BatchKernelInfo batch_kernel_f32eo()
 {
   return BatchKernelInfo{reinterpret_cast<const void*>(&batch_kernel<float, kFamilySlabEO>),
-                         kFamilySlabEO, 1, &batch_bytes<float, kFamilySlabEO>};
+                         kFamilySlabEO, 1, &batch_bytes<float, kFamilySlabEO>,
+                         &read_clear_fault_word};
 }
 } // namespace femtc

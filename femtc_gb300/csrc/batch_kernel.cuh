@@ -611,6 +611,7 @@ struct BatchKernelInfo
   // stage / work bytes of one tile of `variant` under layout l
   void (*bytes)(int variant, const BatchLayout& l, unsigned* bu,
                 unsigned* bg, unsigned* bw);
+  unsigned (*read_fault)(); // reads and clears the family unit's fault word
 };
 
 template <typename T, int FAMILY>

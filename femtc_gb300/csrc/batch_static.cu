@@ -21,7 +21,11 @@
 // * A batch whose schedule does not fit is rejected with FEMTC_ERR_INVALID
 //   and a message giving the capacity.
 // * No cudaMalloc, cudaFree or other allocating routine is called: the
-//   schedule is uploaded with cudaMemcpyAsync on the caller's stream.
+//   schedule is uploaded with cudaMemcpyAsync on the caller's stream, from
+//   host vectors that are freed when the call returns.  A copy recorded into
+//   a CUDA graph would keep pointers to that freed memory, so the call
+//   returns FEMTC_ERR_UNSUPPORTED, before any work, when `stream` is
+//   capturing.
 #include "batch_host.hpp"
 
 #include <cstdio>
@@ -78,6 +82,18 @@ using namespace femtc;
 extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items,
                                         int nitems, void* stream)
 {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t ce = cudaStreamIsCapturing(st, &cs);
+  if (ce != cudaSuccess)
+  {
+    cudaGetLastError();
+    return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(ce));
+  }
+  if (cs != cudaStreamCaptureStatusNone)
+    return aux_fail(FEMTC_ERR_UNSUPPORTED,
+                    "batch_apply_static: the stream is capturing; the schedule upload reads "
+                    "host memory that the call frees on return");
   if (nitems > kStaticMaxItems)
   {
     char msg[160];
@@ -116,7 +132,6 @@ extern "C" int femtc_batch_apply_static(int dtype, const femtc_batch_item* items
   rc = scratch_address(&base);
   if (rc != FEMTC_OK)
     return rc;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned char* p = static_cast<unsigned char*>(base);
   cudaError_t e = cudaMemcpyAsync(p, table.data(), sizeof(BatchItem<float>) * table.size(),
                                   cudaMemcpyHostToDevice, st);

@@ -116,15 +116,6 @@ void add_affine(std::vector<CellVariant>& v, int dtype)
   }
 }
 
-inline unsigned read_clear_fault_word()
-{
-  unsigned w = 0, z = 0;
-  if (cudaMemcpyFromSymbol(&w, g_fault_word, sizeof(w)) != cudaSuccess)
-    return 0;
-  if (w)
-    cudaMemcpyToSymbol(g_fault_word, &z, sizeof(z));
-  return w;
-}
 } // namespace femtc
 
 #define FEMTC_CELL_UNIT(NAME, T, DTYPE, OP, L)                                 \

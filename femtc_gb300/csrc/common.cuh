@@ -20,6 +20,20 @@ enum : unsigned
 // the host reads (and clears) it through the unit's registration hook.
 static __device__ unsigned g_fault_word;
 
+// Host: returns and clears this translation unit's fault word.  Internal
+// linkage, so that every unit that includes this header reads its own word
+// (an external inline function would be merged into one copy by the linker,
+// reading one unit's word for all of them).
+static inline unsigned read_clear_fault_word()
+{
+  unsigned w = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&w, g_fault_word, sizeof(w)) != cudaSuccess)
+    return 0;
+  if (w)
+    cudaMemcpyToSymbol(g_fault_word, &z, sizeof(z));
+  return w;
+}
+
 // Iteration limit of every mbarrier spin in this library.  try_wait suspends
 // for a bounded, hardware-chosen time per call, so the limit is a bound on
 // wall time of the order of a second, never an infinite loop.
@@ -63,11 +77,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// Returns false when the phase did not complete within kMbarSpinLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Returns false when the phase did not complete within `limit` polls
+// (kMbarSpinLimit for every kernel of the library; femtc_bounded_wait_check
+// passes a short one).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          int limit = kMbarSpinLimit)
 {
   const uint32_t a = smem_addr(bar);
-  for (int i = 0; i < kMbarSpinLimit; ++i)
+  for (int i = 0; i < limit; ++i)
   {
     uint32_t done;
     asm volatile("{\n\t.reg .pred p;\n\t"

@@ -47,15 +47,6 @@ void add_mma_all(std::vector<CellVariant>& v, int dtype)
   add_mma_degree<SPLIT, OP, 8>(v, dtype);
 }
 
-inline unsigned read_clear_fault_word_mma()
-{
-  unsigned w = 0, z = 0;
-  if (cudaMemcpyFromSymbol(&w, g_fault_word, sizeof(w)) != cudaSuccess)
-    return 0;
-  if (w)
-    cudaMemcpyToSymbol(g_fault_word, &z, sizeof(z));
-  return w;
-}
 } // namespace femtc
 
 #define FEMTC_MMA_UNIT(NAME, SPLIT, DTYPE, OP)                                 \
@@ -64,6 +55,6 @@ inline unsigned read_clear_fault_word_mma()
   void NAME(std::vector<CellVariant>& v, std::vector<FaultReader>& f)          \
   {                                                                            \
     add_mma_all<SPLIT, OP>(v, DTYPE);                                          \
-    f.push_back(&read_clear_fault_word_mma);                                   \
+    f.push_back(&read_clear_fault_word);                                       \
   }                                                                            \
   }

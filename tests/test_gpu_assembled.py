@@ -94,3 +94,14 @@ def test_assembled_bad_map_entry_gives_nan(femtc, dev):
     assert np.isnan(y[hit]).all()
     rest = np.setdiff1d(np.arange(nd), hit)
     assert np.array_equal(y[rest], y_ok[rest])
+
+
+def test_assembled_no_cells_gives_zero(femtc, dev):
+    """With no cells every global DOF's sum is empty: y is written as zero."""
+    import torch
+    op, dtype, P = 0, 0, 2
+    w, dm, nd, x, b = setup(femtc, dev, op, dtype, P, (2, 2, 2), seed=3)
+    femtc.assembled_apply(op, dtype, femtc.EXACT, P, P + 2, w.tables, b["dm"], b["off"], b["ent"],
+                          nd, b["x"], b["y"], b["g"], 0, b["work"])
+    torch.cuda.synchronize()
+    assert np.array_equal(b["y"].cpu().numpy(), np.zeros(nd))

@@ -54,6 +54,53 @@ def test_static_batch_matches_batch_launch(femtc, dev, dtype):
         batch.close()
 
 
+def test_static_batch_leaves_free_memory_unchanged(femtc, dev):
+    # the call allocates no device memory: after a first call (which may load
+    # the kernel's module), the device's free bytes stay the same across calls
+    import torch
+    ms = meshes(femtc, dev, 13, 1)
+    for m in ms:
+        m[5] = torch.empty_like(m[4])
+    ms = [tuple(m) for m in ms]
+    femtc.batch_apply_static(1, ms)
+    torch.cuda.synchronize()
+    before = torch.cuda.mem_get_info(dev)[0]
+    for _ in range(3):
+        femtc.batch_apply_static(1, ms)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(dev)[0] == before
+    assert femtc.device_status() == 0
+
+
+def test_static_batch_rejects_a_capturing_stream(femtc, dev):
+    # the schedule is copied from host memory freed on return: a copy
+    # recorded into a graph would read freed memory at replay, so the call
+    # refuses a capturing stream before doing any work
+    import torch
+    ms = meshes(femtc, dev, 14, 1)
+    for m in ms:
+        m[5] = torch.empty_like(m[4])
+    ms = [tuple(m) for m in ms]
+    femtc.batch_apply_static(1, ms)  # first call on the device, outside capture
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream(device=dev)
+    g = torch.cuda.CUDAGraph()
+    err = None
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        try:
+            femtc.batch_apply_static(1, ms, stream=s)
+        except femtc.FemtcError as e:
+            err = e
+        g.capture_end()
+    torch.cuda.synchronize()
+    assert err is not None and err.status == -2  # FEMTC_ERR_UNSUPPORTED
+    del g
+    femtc.batch_apply_static(1, ms)  # still usable afterwards
+    torch.cuda.synchronize()
+    assert femtc.device_status() == 0
+
+
 def test_static_batch_rejects_oversize(femtc, dev):
     import torch
     # more meshes than the static mesh table holds

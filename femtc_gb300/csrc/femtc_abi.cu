@@ -80,6 +80,8 @@ Registry& registry()
     register_mma_f16x2_stiffness(r.cells, r.faults);
     register_mma_bf16x3_mass(r.cells, r.faults);
     register_mma_bf16x3_stiffness(r.cells, r.faults);
+    register_batch_faults(r.faults);
+    register_diag(r.cells, r.faults);
   });
   return r;
 }
@@ -501,11 +503,11 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
   if (op_affine(op) && sem != FEMTC_EXACT)
     return fail(FEMTC_ERR_INVALID, "affine forms: exact semantics only");
   const CellVariant* v = find_cell(op, dtype, sem, degree + 1, nquad);
-  if (!v)
+  if (!v && !general_supported(op, dtype, sem, degree + 1, nquad))
     return fail(FEMTC_ERR_UNSUPPORTED,
                 "no %s kernel for dtype %d, semantics %d, degree %d, nquad %d",
                 names[op], dtype, sem, degree, nquad);
-  *out = v;
+  *out = v; // null: the general-degree kernel (cell_general.cu)
   return FEMTC_OK;
 }
 
@@ -684,6 +686,16 @@ int apply(int op, int dtype, int sem, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return FEMTC_OK;
+  if (!v)
+  {
+    if (!aligned16(u) || !aligned16(y) || !aligned16(geo))
+      return fail(FEMTC_ERR_INVALID, "u, y and the geometry must be 16-byte aligned");
+    rc = launch_general(op, dtype, sem, degree + 1, nquad, tables, u, y, geo, ncells,
+                        static_cast<cudaStream_t>(stream));
+    if (rc == FEMTC_OK)
+      g_launches.fetch_add(1, std::memory_order_relaxed);
+    return rc;
+  }
   const auto sel = select_variant(op, dtype, sem, degree + 1, nquad);
   return launch_variant(*sel.first, sel.second, tables, u, y, geo, ncells,
                         static_cast<cudaStream_t>(stream));
@@ -793,14 +805,31 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return FEMTC_OK;
+  if (!v && mode == 2)
+    return fail(FEMTC_ERR_INVALID, "zero-copy host mode: not for the general-degree kernel");
   int dev = 0;
   cudaGetDevice(&dev);
+  if (g_host.device != dev)
+  {
+    // a different device: drop the streams and buffers of the old one (they
+    // stay valid on it until freed; free them with that device current), so
+    // both paths below use streams of the current device
+    g_host.stream = nullptr;
+    g_host.in = nullptr;
+    g_host.out = nullptr;
+    for (int i = 0; i < 3; ++i)
+    {
+      g_host.buf[i] = nullptr;
+      g_host.cap[i] = 0;
+    }
+    g_host.device = dev;
+  }
   // Pinned host buffers: the kernel reads u and the geometry and writes y
   // over the coherent host link directly (no staging copies).
   const void* du = nullptr;
   void* dy = nullptr;
   const void* dg = nullptr;
-  if (mode != 1 && device_view(u, &du) && device_view(y, (const void**)&dy) &&
+  if (v && mode != 1 && device_view(u, &du) && device_view(y, (const void**)&dy) &&
       device_view(geo, &dg))
   {
     if (!g_host.stream &&
@@ -817,20 +846,6 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
   }
   if (mode == 2)
     return fail(FEMTC_ERR_INVALID, "zero-copy host mode needs pinned host buffers");
-  if (g_host.device != dev)
-  {
-    // a different device: drop buffers of the old one (they stay valid on
-    // it until freed; free them with that device current)
-    g_host.stream = nullptr;
-    g_host.in = nullptr;
-    g_host.out = nullptr;
-    for (int i = 0; i < 3; ++i)
-    {
-      g_host.buf[i] = nullptr;
-      g_host.cap[i] = 0;
-    }
-    g_host.device = dev;
-  }
   if (!g_host.stream)
   {
     cudaError_t e =
@@ -839,14 +854,34 @@ int apply_host_locked(int op, int dtype, int sem, int degree, int nquad,
       return cuda_fail(e, "cudaStreamCreate");
   }
   const size_t es = elem_size(dtype);
-  const size_t n3 = (size_t)v->n * v->n * v->n;
+  const size_t nn = (size_t)degree + 1, nqd = (size_t)nquad;
+  const size_t n3 = nn * nn * nn;
   // geometry values per cell: per quadrature point, or one set (affine)
-  const size_t q3 = op_affine(op) ? (size_t)cell_nc(op) : (size_t)v->q * v->q * v->q * geo_nc(op);
+  const size_t q3 = op_affine(op) ? (size_t)cell_nc(op) : nqd * nqd * nqd * geo_nc(op);
   const size_t bu = ncells * n3 * es, bg = ncells * q3 * es;
   if ((rc = host_buffer(0, bu)) != FEMTC_OK ||
       (rc = host_buffer(1, bu)) != FEMTC_OK ||
       (rc = host_buffer(2, bg)) != FEMTC_OK)
     return rc;
+  if (!v)
+  {
+    // general-degree kernel: whole copies in, one launch, the copy out
+    cudaStream_t st = g_host.stream;
+    cudaError_t e = cudaMemcpyAsync(g_host.buf[0], u, bu, cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(g_host.buf[2], geo, bg, cudaMemcpyDefault, st);
+    if (e != cudaSuccess)
+      return cuda_fail(e, "cudaMemcpyAsync");
+    rc = launch_general(op, dtype, sem, degree + 1, nquad, tables, g_host.buf[0], g_host.buf[1],
+                        g_host.buf[2], ncells, st);
+    if (rc != FEMTC_OK)
+      return rc;
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    e = cudaMemcpyAsync(y, g_host.buf[1], bu, cudaMemcpyDefault, st);
+    if (e == cudaSuccess)
+      e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? FEMTC_OK : cuda_fail(e, "host path copy");
+  }
   // Staging pipeline: chunk i's host->device copy (stream `in`), operator
   // (compute stream, after the copy's event) and device->host copy (stream
   // `out`, after the kernel's event) overlap with the neighbouring chunks.
@@ -1037,7 +1072,12 @@ int femtc_device_status(void)
 
 int femtc_supported(int op, int dtype, int semantics, int degree, int nquad)
 {
-  return find_cell(op, dtype, semantics, degree + 1, nquad) ? 1 : 0;
+  if (semantics == FEMTC_REFERENCE && nquad != degree + 1)
+    return 0;
+  return (find_cell(op, dtype, semantics, degree + 1, nquad) ||
+          general_supported(op, dtype, semantics, degree + 1, nquad))
+             ? 1
+             : 0;
 }
 
 int femtc_mass_apply(int dtype, int semantics, int degree, int nquad,
@@ -1185,6 +1225,8 @@ int femtc_autotune_host(int op, int dtype, int semantics, int degree,
                          g_host.stream, 1, cb, geo_staged, threads, best_ms);
   if (rc != FEMTC_OK)
     return rc;
+  if (!find_cell(op, dtype, semantics, degree + 1, nquad))
+    return FEMTC_OK; // the general-degree kernel: one transfer mode (copies)
   // then the transfer mode: whole calls (copies, kernels, synchronisation)
   // of the zero-copy path and of the staging pipeline, wall clock, the two
   // modes alternating; the best call of each counts
@@ -1230,6 +1272,19 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
     return rc;
   if (ncells == 0)
     return fail(FEMTC_ERR_INVALID, "autotune needs at least one cell");
+  if (!v)
+  {
+    // the general-degree kernel has no tile shape: one cell per CTA
+    if (cb)
+      *cb = 1;
+    if (geo_staged)
+      *geo_staged = 0;
+    if (threads)
+      *threads = 256;
+    if (best_ms)
+      *best_ms = 0.0f;
+    return FEMTC_OK;
+  }
   // candidates: for each (staging, threads), the cell counts per tile with
   // the best lane efficiency that fit in shared memory, and -- for calls of
   // a few waves, where whole SMs idle when the tile count is just past a

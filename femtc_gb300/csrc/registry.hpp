@@ -51,5 +51,13 @@ void register_mma_f16x2_mass(std::vector<CellVariant>&, std::vector<FaultReader>
 void register_mma_f16x2_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_bf16x3_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_mma_bf16x3_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+// General-degree kernels (cell_general.cu): runtime N and Q, mass and
+// stiffness, FP64 and FP32, for the (N, Q) the slab kernels do not cover.
+bool general_supported(int op, int dtype, int sem, int n, int q);
+int launch_general(int op, int dtype, int sem, int n, int q, const void* tables, const void* u,
+                   void* y, const void* geo, size_t ncells, cudaStream_t st);
+// fault words of the batch kernel families and of the diagnostic unit
+void register_batch_faults(std::vector<FaultReader>&);
+void register_diag(std::vector<CellVariant>&, std::vector<FaultReader>&);
 
 } // namespace femtc

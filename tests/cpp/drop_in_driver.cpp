@@ -39,6 +39,25 @@ static void run_template(bool mass, std::vector<T>& phi, std::vector<T>& U,
         phi, U, W, geo, num_cells);
 }
 
+// The reference's runtime ladder covers degrees 1..25 (src/mass.hpp:57-137,
+// src/stiffness.hpp:109-181): the templated signature at every one of them.
+template <typename T, int P = 1>
+static bool run_template_ladder(int degree, bool mass, std::vector<T>& phi, std::vector<T>& U,
+                                std::vector<T>& W, std::vector<T>& geo, std::size_t num_cells)
+{
+  if constexpr (P <= 25)
+  {
+    if (degree == P)
+    {
+      run_template<T, P>(mass, phi, U, W, geo, num_cells);
+      return true;
+    }
+    return run_template_ladder<T, P + 1>(degree, mass, phi, U, W, geo, num_cells);
+  }
+  else
+    return false;
+}
+
 template <typename T>
 static int run(bool mass, int degree, int num_cells, const std::string& out)
 {
@@ -67,16 +86,10 @@ static int run(bool mass, int degree, int num_cells, const std::string& out)
   dump(out + "/W_dispatch.bin", W);
 
   std::vector<T> W2(num_cells * ndofs, 0.0);
-  switch (degree)
+  if (!run_template_ladder<T>(degree, mass, phi, U, W2, geo, num_cells))
   {
-  case 1: run_template<T, 1>(mass, phi, U, W2, geo, num_cells); break;
-  case 2: run_template<T, 2>(mass, phi, U, W2, geo, num_cells); break;
-  case 3: run_template<T, 3>(mass, phi, U, W2, geo, num_cells); break;
-  case 4: run_template<T, 4>(mass, phi, U, W2, geo, num_cells); break;
-  case 5: run_template<T, 5>(mass, phi, U, W2, geo, num_cells); break;
-  case 6: run_template<T, 6>(mass, phi, U, W2, geo, num_cells); break;
-  case 7: run_template<T, 7>(mass, phi, U, W2, geo, num_cells); break;
-  default: std::cerr << "degree not in 1..7\n"; return 2;
+    std::cerr << "degree not in 1..25\n";
+    return 2;
   }
   dump(out + "/W_template.bin", W2);
   dump(out + "/phi.bin", phi);

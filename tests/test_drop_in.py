@@ -27,10 +27,14 @@ def test_header_compiles(femtc, tmp_path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("op", ["mass", "stiffness"])
 @pytest.mark.parametrize("dtype", ["double", "float"])
-@pytest.mark.parametrize("degree", [1, 3, 4, 7])
+@pytest.mark.parametrize("degree", [1, 3, 4, 7, 8, 12, 15, 25])
 def test_drop_in_matches_oracle(femtc, orc, dev, tmp_path, op, dtype, degree):
+    """Degrees 1..7 run the slab kernels, 8..25 the general-degree kernel
+    (shared-memory work buffers up to about N = 16, a device workspace
+    above).  FP32 tolerance: 2e-6 to degree 7; sums of up to 26^3 positive
+    products at the higher degrees are allowed 1e-5."""
     exe = compile_driver(femtc, str(tmp_path))
-    ncells = 129
+    ncells = 129 if degree <= 15 else 37
     r = subprocess.run([exe, op, str(degree), str(ncells), dtype, str(tmp_path)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -43,7 +47,9 @@ def test_drop_in_matches_oracle(femtc, orc, dev, tmp_path, op, dtype, degree):
         ref = orc.mass(orc.REFERENCE, degree, n, tables, U, geo.reshape(ncells, -1))
     else:
         ref = orc.stiffness(orc.REFERENCE, degree, n, tables, U, geo.reshape(ncells, -1))
-    tol = 1e-12 if dtype == "double" else 2e-6
+    tol = 1e-12 if dtype == "double" else (2e-6 if degree <= 7 else 1e-5)
+    assert femtc.supported(0 if op == "mass" else 1, 0 if dtype == "double" else 1,
+                           femtc.REFERENCE, degree, degree + 1)
     for f in ("W_dispatch.bin", "W_template.bin"):
         W = rd(f).reshape(ncells, -1)
         assert np.abs(W - ref).max() / np.abs(ref).max() <= tol

@@ -10,7 +10,7 @@ from ._lib import (  # noqa: F401
     DTYPE_NAMES, helmholtz_apply, helmholtz_geometry,
     MASS_AFFINE, STIFFNESS_AFFINE, affine_apply, affine_tables,
     assembled_apply, assembled_work_bytes, dofmap_transpose,
-    FemtcError, apply, apply_contractions, apply_host, autotune, autotune_host, gemm_blocked, geometry, check, device_status, get_tile_config, load,
+    FemtcError, apply, apply_contractions, apply_host, autotune, autotune_host, gemm_blocked, gemm_micro, geometry, check, device_status, get_tile_config, load,
     even_odd_used, operator_launches, set_even_odd, set_host_path, set_tile_config, supported, tabulate, tile_db_load, tile_db_save,
 )
 from .buildlib import build, lib_path  # noqa: F401

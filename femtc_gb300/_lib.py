@@ -43,6 +43,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_operator_launches": ([], ctypes.c_longlong),
         "femtc_last_error": ([], ctypes.c_char_p),
         "femtc_device_status": ([], c_int),
+        "femtc_bounded_wait_check": ([c_int, vp], c_int),
         "femtc_supported": ([c_int] * 5, c_int),
         "femtc_mass_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
         "femtc_stiffness_apply": ([c_int] * 4 + [vp] * 4 + [c_size, vp], c_int),
@@ -70,6 +71,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_tabulate": ([c_int, c_int, dp, dp, dp, dp], c_int),
         "femtc_set_host_path": ([c_int], c_int),
         "femtc_gemm_blocked": ([c_int] * 4 + [vp] * 3 + [c_size, vp], c_int),
+        "femtc_gemm_micro": ([c_int] * 7 + [vp] * 3 + [c_size] * 4 + [vp], c_int),
         "femtc_apply_contractions": ([c_int] * 4 + [vp] * 5 + [c_size, vp], c_int),
         "femtc_geometry": ([c_int, c_int, vp, vp, c_int, vp, vp, c_size, vp], c_int),
         "femtc_batch_create": ([c_int, vp, c_int, c_int, ctypes.POINTER(vp)], c_int),
@@ -342,6 +344,14 @@ def gemm_blocked(dtype: int, k: int, m: int, n: int, a, b, c, batch: int, stream
     tab = host_tables(a, dtype)
     check(load().femtc_gemm_blocked(dtype, k, m, n, tab.ctypes.data, ptr(b), ptr(c), batch,
                                     stream_ptr(stream)))
+
+
+def gemm_micro(dtype: int, k: int, m: int, nc: int, lda: int, ldb: int, ldc: int, a, b, c,
+               batch: int = 1, strides=(0, 0, 0), stream=None) -> None:
+    """Batched linalg::gemm_micro on the device: C += A B (a, b, c device
+    buffers; strides in elements between items)."""
+    check(load().femtc_gemm_micro(dtype, k, m, nc, lda, ldb, ldc, ptr(a), ptr(b), ptr(c), batch,
+                                  strides[0], strides[1], strides[2], stream_ptr(stream)))
 
 
 def apply_contractions(dtype: int, na: int, nb: int, tr: bool, i0, i1, i2, b, a, ncells: int,

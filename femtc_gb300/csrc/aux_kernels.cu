@@ -1,5 +1,8 @@
 // Stand-alone contraction entry points and the FP64 geometry kernel.
 //
+//  femtc_gemm_micro          linalg::gemm_micro (src/linalg.hpp:45-94),
+//                            batched: C_b += A_b B_b with A column-major
+//                            (lda), B and C row-major (ldb, ldc).
 //  femtc_gemm_blocked        linalg::gemm_blocked (src/linalg.hpp:101-182),
 //                            batched over cells: C_c = A B_c with A column-
 //                            major m x k, B_c row-major k x n, C_c column-
@@ -59,6 +62,32 @@ __global__ void __launch_bounds__(256)
         acc = fma(p.a[i + q * p.m], b[q * p.n + j], acc);
       c[i + j * p.m] = acc;
     }
+  }
+}
+
+// One thread per output element (item, i, j), j fastest (coalesced rows of
+// C and B): c(i,j) += sum_p a[i + p*lda] b[p*ldb + j], the products added
+// into c in increasing p (gemm_micro's kij order, src/linalg.hpp:73-79).
+template <typename T>
+__global__ void __launch_bounds__(256)
+    gemm_micro_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ c, int k,
+                      int m, int nc, int lda, int ldb, int ldc, long long batch, long long sa,
+                      long long sb, long long sc)
+{
+  const long long per = (long long)m * nc;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < batch * per;
+       t += (long long)gridDim.x * blockDim.x)
+  {
+    const long long item = t / per;
+    const int r = (int)(t - item * per);
+    const int i = r / nc, j = r - i * nc;
+    const T* ai = a + item * sa + i;
+    const T* bj = b + item * sb + j;
+    T* cij = c + item * sc + (long long)i * ldc + j;
+    T acc = *cij;
+    for (int p = 0; p < k; ++p)
+      acc = fma(ai[(long long)p * lda], bj[(long long)p * ldb], acc);
+    *cij = acc;
   }
 }
 
@@ -284,6 +313,37 @@ __global__ void __launch_bounds__(256)
 }
 
 extern "C" {
+
+int femtc_gemm_micro(int dtype, int k, int m, int nc, int lda, int ldb, int ldc, const void* a,
+                     const void* b, void* c, size_t batch, size_t stride_a, size_t stride_b,
+                     size_t stride_c, void* stream)
+{
+  if (dtype != FEMTC_F64 && dtype != FEMTC_F32)
+    return aux_fail(FEMTC_ERR_INVALID, "gemm_micro: dtype must be F64 or F32");
+  if (k < 1 || m < 1 || nc < 1 || lda < m || ldb < nc || ldc < nc)
+    return aux_fail(FEMTC_ERR_INVALID,
+                    "gemm_micro: need k, m, nc >= 1, lda >= m, ldb >= nc, ldc >= nc");
+  if (!a || !b || !c)
+    return aux_fail(FEMTC_ERR_INVALID, "gemm_micro: null pointer");
+  if (batch > 1 && stride_c < (size_t)(m - 1) * ldc + nc)
+    return aux_fail(FEMTC_ERR_INVALID,
+                    "gemm_micro: items' C blocks overlap (stride_c below one block)");
+  if (batch == 0)
+    return FEMTC_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long work = (long long)batch * m * nc;
+  if (dtype == FEMTC_F64)
+    gemm_micro_kernel<double><<<grid_for(work, 256), 256, 0, st>>>(
+        static_cast<const double*>(a), static_cast<const double*>(b), static_cast<double*>(c), k,
+        m, nc, lda, ldb, ldc, (long long)batch, (long long)stride_a, (long long)stride_b,
+        (long long)stride_c);
+  else
+    gemm_micro_kernel<float><<<grid_for(work, 256), 256, 0, st>>>(
+        static_cast<const float*>(a), static_cast<const float*>(b), static_cast<float*>(c), k, m,
+        nc, lda, ldb, ldc, (long long)batch, (long long)stride_a, (long long)stride_b,
+        (long long)stride_c);
+  return launch_error(cudaGetLastError());
+}
 
 int femtc_gemm_blocked(int dtype, int k, int m, int n, const void* a,
                        const void* b, void* c, size_t batch, void* stream)

@@ -79,9 +79,21 @@ long long femtc_operator_launches(void);
 const char* femtc_last_error(void);
 
 /* Reads and clears the device fault word of every kernel unit (bits set by
- * bounded waits that gave up).  Synchronises the device.  Returns the OR of
- * the words, 0 when clean, or a negative status. */
+ * bounded waits that gave up: 1 = an mbarrier wait timed out, 2 = a batched
+ * work item named an unknown variant).  Synchronises the device.  Returns
+ * the OR of the words, 0 when clean, or a negative status. */
 int femtc_device_status(void);
+
+/* Diagnostic, no reference counterpart (the reference has no device code):
+ * launches one CTA on `stream` whose mbarrier wait cannot complete (armed
+ * for transaction bytes that no copy delivers) and that waits through the
+ * library's bounded wait with a limit of `polls` polls (1..2^22; the
+ * library's kernels use 2^22).  The wait gives up, the kernel sets
+ * FAULT bit 1 (mbarrier wait timed out) in its fault word and returns:
+ * femtc_device_status() then reports 1.  No copy is issued and no memory is
+ * touched, so the GPU stays usable; this shows that a stalled copy in any
+ * kernel of the library ends as a status word, not a hang. */
+int femtc_bounded_wait_check(int polls, void* stream);
 
 /* Whether (op, dtype, semantics, degree, nquad) has a compiled kernel:
  * 1 yes, 0 no. */
@@ -254,6 +266,21 @@ int femtc_autotune_host(int op, int dtype, int semantics, int degree,
 int femtc_tile_db_save(const char* path);
 int femtc_tile_db_load(const char* path);
 
+/* linalg::gemm_micro (src/linalg.hpp:45-94), batched over `batch` items:
+ * C_b += A_b B_b with A column-major m x k (element (i,p) at a[i + p*lda]),
+ * B row-major k x nc (b[p*ldb + j]) and C row-major m x nc (c[i*ldc + j]);
+ * C is accumulated into, as the reference's micro-kernel does, with the
+ * products added in increasing p (one FMA each).  Item b's matrices start
+ * stride_a, stride_b, stride_c elements after item b-1's (0 shares A or B
+ * between items; C blocks must not overlap).  dtype FEMTC_F64 or
+ * FEMTC_F32; a, b, c are device pointers.  The reference's test of it is
+ * tests/test_micro.cpp:12-53 (k = 26, m = 4, nc = 16, lda = 4,
+ * ldb = ldc = 16). */
+int femtc_gemm_micro(int dtype, int k, int m, int nc, int lda, int ldb, int ldc,
+                     const void* a, const void* b, void* c, size_t batch,
+                     size_t stride_a, size_t stride_b, size_t stride_c,
+                     void* stream);
+
 /* One batched axis contraction, as linalg::gemm_blocked
  * (src/linalg.hpp:101-182) for every cell c: C_c = A B_c with A column-major
  * m x k (HOST memory, k, m <= 32), B_c row-major k x n and C_c column-major
@@ -352,9 +379,12 @@ void femtc_batch_destroy(femtc_batch* b);
  * call allocates nothing.  Limits: at most 4096 meshes and as many tiles as
  * fit in 8 MiB (about 349,000); larger batches are rejected with
  * FEMTC_ERR_INVALID.  The first call on a device sets up the array's address
- * (cudaGetSymbolAddress): make it before any stream capture.  Every call
- * reuses the array, so calls whose work overlaps on the GPU (different
- * streams or threads) race; calls on one stream are ordered. */
+ * (cudaGetSymbolAddress): make it before any stream capture.  The schedule
+ * is copied from host memory that the call frees on return, so a call on a
+ * stream that is capturing is rejected with FEMTC_ERR_UNSUPPORTED before it
+ * does any work.  Every call reuses the array, so calls whose work overlaps
+ * on the GPU (different streams or threads) race; calls on one stream are
+ * ordered. */
 int femtc_batch_apply_static(int dtype, const femtc_batch_item* items,
                              int nitems, void* stream);
 

@@ -166,3 +166,34 @@ def test_even_odd_selection(femtc):
         assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, t4)
     finally:
         femtc.set_even_odd(True)
+
+
+def test_bounded_wait_check_rejects_bad_limits(femtc):
+    # checked before any launch (no GPU needed)
+    lib = femtc.load()
+    assert lib.femtc_bounded_wait_check(0, None) == -1
+    assert lib.femtc_bounded_wait_check((1 << 22) + 1, None) == -1
+
+
+def test_gemm_micro_rejects_bad_shapes_before_launch(femtc):
+    lib = femtc.load()
+    # lda < m
+    assert lib.femtc_gemm_micro(0, 4, 4, 16, 3, 16, 16, 16, 16, 16, 1, 0, 0, 0, None) == -1
+    # ldc < nc
+    assert lib.femtc_gemm_micro(0, 4, 4, 16, 4, 16, 8, 16, 16, 16, 1, 0, 0, 0, None) == -1
+    # overlapping C blocks
+    assert lib.femtc_gemm_micro(0, 4, 4, 16, 4, 16, 16, 16, 16, 16, 2, 0, 0, 8, None) == -1
+
+
+def test_supported_general_degrees(femtc):
+    # the reference's ladder runs degrees 1..25 (src/mass.hpp:57-137)
+    for P in range(8, 26):
+        for op in (femtc.MASS, femtc.STIFFNESS):
+            for dt in (femtc.F64, femtc.F32):
+                assert femtc.supported(op, dt, femtc.REFERENCE, P, P + 1)
+                assert femtc.supported(op, dt, femtc.EXACT, P, P + 2)
+                assert not femtc.supported(op, dt, femtc.REFERENCE, P, P + 2)
+        assert not femtc.supported(femtc.MASS, femtc.F64E, femtc.EXACT, P, P + 2)
+        assert not femtc.supported(femtc.STIFFNESS, femtc.BF16X3, femtc.EXACT, P, P + 2)
+    assert not femtc.supported(femtc.MASS, femtc.F64, femtc.REFERENCE, 26, 27)
+    assert not femtc.supported(femtc.MASS, femtc.F64, femtc.EXACT, 25, 29)

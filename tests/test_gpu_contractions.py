@@ -1,5 +1,8 @@
 """GPU: the stand-alone contraction entries and the FP64 geometry kernel.
 
+femtc_gemm_micro mirrors the reference's micro-kernel test
+(tests/test_micro.cpp:12-53: k = 26, m = 4, n = 16, lda = 4, ldb = ldc = 16,
+accumulating into C) against the oracle's restatement at 1e-12 absolute;
 femtc_gemm_blocked mirrors the reference's own unit test
 (tests/test_gemm.cpp: P = 1..25, A (P+1)x(P+1) column-major, B row-major,
 1e-10 absolute) and the golden vectors of the reference's gemm_blocked;
@@ -33,6 +36,57 @@ def test_gemm_blocked_like_reference_test(femtc, dev, P):
     for c in range(batch):
         ref = (Am @ B[c].reshape(k, n)).T.reshape(-1)  # column-major m x n
         assert np.abs(C[c] - ref).max() <= 1e-10
+
+
+def test_gemm_micro_like_reference_test(femtc, orc, dev):
+    import torch
+    k, m, n, lda, ldb, ldc = 26, 4, 16, 4, 16, 16
+    rng = np.random.default_rng(26)
+    A = rng.uniform(size=lda * k)   # column-major 4 x k
+    B = rng.uniform(size=k * ldb)   # row-major k x 16
+    C0 = np.zeros(m * ldc)          # row-major 4 x 16, accumulated into
+    d = lambda x: torch.from_numpy(x).to(dev)
+    Cd = d(C0)
+    femtc.gemm_micro(femtc.F64, k, m, n, lda, ldb, ldc, d(A), d(B), Cd)
+    torch.cuda.synchronize()
+    ref = orc.gemm_micro(k, m, n, lda, ldb, ldc, A, B, C0)
+    assert np.abs(Cd.cpu().numpy() - ref).max() <= 1e-12  # tests/test_micro.cpp:47
+
+
+@pytest.mark.parametrize("dtype", [0, 1])
+def test_gemm_micro_batched_accumulates_with_strides(femtc, orc, dev, dtype):
+    # padded leading dimensions, a shared A, per-item B and C, C nonzero on
+    # entry (+= semantics); padding columns of C are left untouched
+    import torch
+    k, m, n, lda, ldb, ldc, batch = 7, 5, 9, 6, 11, 10, 13
+    rng = np.random.default_rng(5 + dtype)
+    A = rng.uniform(-1, 1, size=lda * k)
+    B = rng.uniform(-1, 1, size=(batch, k * ldb))
+    C0 = rng.uniform(-1, 1, size=(batch, m * ldc))
+    tdt = torch.float64 if dtype == 0 else torch.float32
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(dev, tdt)
+    Cd = d(C0)
+    femtc.gemm_micro(dtype, k, m, n, lda, ldb, ldc, d(A), d(B), Cd, batch=batch,
+                     strides=(0, k * ldb, m * ldc))
+    torch.cuda.synchronize()
+    C = Cd.double().cpu().numpy()
+    tol = 1e-12 if dtype == 0 else 2e-6
+    for c in range(batch):
+        a, b, c0 = A, B[c], C0[c]
+        if dtype == 1:
+            a, b, c0 = (x.astype(np.float32).astype(np.float64) for x in (a, b, c0))
+        ref = orc.gemm_micro(k, m, n, lda, ldb, ldc, a, b, c0)
+        assert np.abs(C[c] - ref).max() <= tol * max(1.0, np.abs(ref).max())
+        pad = np.ones(m * ldc, bool)
+        pad.reshape(m, ldc)[:, :n] = False
+        assert np.array_equal(C[c][pad], d(C0[c]).double().cpu().numpy()[pad])
+
+
+def test_gemm_micro_rejects_overlapping_items(femtc, dev):
+    import torch
+    x = torch.zeros(64, dtype=torch.float64, device=dev)
+    with pytest.raises(femtc.FemtcError):
+        femtc.gemm_micro(femtc.F64, 2, 2, 2, 2, 2, 2, x, x, x, batch=2, strides=(0, 0, 0))
 
 
 @pytest.mark.parametrize("P", range(1, 9))

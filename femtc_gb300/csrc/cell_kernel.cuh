@@ -31,6 +31,7 @@
 
 #include "common.cuh"
 #include "df64.cuh"
+#include "slab_strides.hpp"
 
 #include <cuda.h> // CUtensorMap (the type only)
 
@@ -620,8 +621,8 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
 //   backward : one thread per slab contracts axes 1 and 2 back in registers
 //              and writes y[c][i0][:][:].
 // Only the fused pass exchanges data across threads, through the B buffers,
-// whose slab and cell strides (p.sq, p.sbc) are chosen on the host to keep
-// both access patterns free of shared-memory bank conflicts.
+// whose slab and cell strides (SQ, SBC, from slab_strides.hpp) keep both
+// access patterns free of shared-memory bank conflicts.
 // ---------------------------------------------------------------------------
 // S lanes share one slab (consecutive lanes of a warp): lane s of the group
 // takes the q2 columns s, s+S, ...; the slab loads are shared-memory
@@ -688,6 +689,12 @@ struct SlabTile
   static constexpr int kStages = 2;
   static constexpr int NBUF =
       (op_base(OP) == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
+  // work-buffer strides (slab_strides.hpp): compile-time, so every work
+  // buffer access takes an immediate offset; the host sets the same values
+  // in the launch parameters (p.sq, p.sbc) to size the tile
+  static constexpr int SQ = slab_strides(N, Q, (int)sizeof(T), LANES).sq;
+  static constexpr int SBC = slab_strides(N, Q, (int)sizeof(T), LANES).sbc;
+  static_assert(SQ >= Q * Q && SBC >= N * SQ, "no stride table entry for this slab variant");
   // tables: forward A(q,i) = tab[q + i*Q]; backward exact A(i,q) = tab[q + i*Q],
   // reference A(i,q) = tab[i + q*Q] (the forward table reused, Q == N)
   static constexpr int BSM = (SEM == SEM_EXACT) ? Q : 1;
@@ -782,7 +789,7 @@ struct SlabTile
     using E = EO<Q, N>; // forward tables: Q x N
     const T* __restrict__ PF = p.P;
     const T* __restrict__ DF = p.D;
-    const int bstride = w.ncb * p.sbc;
+    const int bstride = w.ncb * SBC;
     for (int sl = w.c0 * N + w.tid; sl < w.c1 * N; sl += w.nthr)
     {
       const int c = sl / N, i0 = sl - c * N;
@@ -797,7 +804,7 @@ struct SlabTile
           xe[i1][k] = x[i1 * N + k] + x[i1 * N + N - 1 - k];
           xo[i1][k] = x[i1 * N + k] - x[i1 * N + N - 1 - k];
         }
-      T* b0 = sw + c * p.sbc + i0 * p.sq;
+      T* b0 = sw + c * SBC + i0 * SQ;
       T* b1 = b0 + bstride;
       T* b2 = b1 + bstride;
       // axis 1 of one column: AA, AG, BA
@@ -899,7 +906,7 @@ struct SlabTile
     }
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
-    const int bstride = w.ncb * p.sbc;
+    const int bstride = w.ncb * SBC;
     // With S lanes per slab the q2 columns of a lane depend on the lane, so
     // their table entries are not compile-time constants: load them into
     // registers once per call (lane_s == threadIdx.x % S for every slab of
@@ -924,7 +931,7 @@ struct SlabTile
       const int c = sl / N, i0 = sl - c * N;
       T x[N2];
       load_slab(su + sl * US, x);
-      T* b0 = sw + c * p.sbc + i0 * p.sq;
+      T* b0 = sw + c * SBC + i0 * SQ;
       T* b1 = b0 + bstride;
       T* b2 = b1 + bstride;
 #pragma unroll UNR
@@ -1002,14 +1009,14 @@ struct SlabTile
     // ones transposed
     const T* __restrict__ PB = (EVOD || kAffine) ? p.PB : p.P;
     const T* __restrict__ DB = (EVOD || kAffine) ? p.DB : p.D;
-    const int bstride = w.ncb * p.sbc;
+    const int bstride = w.ncb * SBC;
     for (int t = w.c0 * Q2 + w.tid; t < w.c1 * Q2; t += w.nthr)
     {
       const int c = t / Q2, r = t - c * Q2;
-      T* b0 = sw + c * p.sbc + r;
+      T* b0 = sw + c * SBC + r;
       T* b1 = b0 + bstride;
       T* b2 = b1 + bstride;
-      const int sq = p.sq;
+      constexpr int sq = SQ;
       if constexpr (OP == OP_MASS_AFFINE)
       {
         // detJ scales the pencil's N inputs (the weights are in PB)
@@ -1147,11 +1154,11 @@ struct SlabTile
     using E = EO<N, Q>; // backward tables: N x Q
     const T* __restrict__ PB = p.PB;
     const T* __restrict__ DB = p.DB;
-    const int bstride = w.ncb * p.sbc;
+    const int bstride = w.ncb * SBC;
     for (int sl = w.c0 * N + w.tid; sl < w.c1 * N; sl += w.nthr)
     {
       const int c = sl / N, i0 = sl - c * N;
-      const T* b0 = sw + c * p.sbc + i0 * p.sq;
+      const T* b0 = sw + c * SBC + i0 * SQ;
       const T* b1 = b0 + bstride;
       const T* b2 = b1 + bstride;
       T A[N][E::M2 > 0 ? E::M2 : 1], B[N][E::M2 > 0 ? E::M2 : 1], Mid[N];
@@ -1273,7 +1280,7 @@ struct SlabTile
     const T* __restrict__ D = kAffine ? p.DB : p.D;
     // every lane of a warp takes part in the shuffle reduction, so all
     // threads of the part run the same number of rounds
-    const int bstride = w.ncb * p.sbc;
+    const int bstride = w.ncb * SBC;
     const int base = w.c0 * N * S, cnt = (w.c1 - w.c0) * N * S;
     const int rounds = (cnt + w.nthr - 1) / w.nthr;
     // axis-2 backward table entries of this lane's q2 columns (see forward)
@@ -1299,7 +1306,7 @@ struct SlabTile
       const int ts = base + idx;
       const int sl = live ? ts / S : 0, lane_s = ts - (ts / S) * S;
       const int c = sl / N, i0 = sl - c * N;
-      const T* b0 = sw + c * p.sbc + i0 * p.sq;
+      const T* b0 = sw + c * SBC + i0 * SQ;
       const T* b1 = b0 + bstride;
       const T* b2 = b1 + bstride;
       T y[N2];

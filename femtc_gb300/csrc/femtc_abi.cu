@@ -189,105 +189,14 @@ std::map<Key, TileChoice> g_tile_cfg_host; // host-resident (zero-copy) operands
 
 constexpr unsigned kSmemPerSmTarget = 113 * 1024; // 2 CTAs per SM
 
-// Shared-memory wavefronts of one warp-wide access of `esize`-byte elements
-// at element indices a[0..31]: 32 four-byte banks; 8-byte accesses are
-// served per half warp (16 x 8 bytes = one 128-byte wavefront when the
-// element indices are distinct modulo 16).
-int wavefronts(const long long* a, int esize)
-{
-  if (esize == 4)
-  {
-    int worst = 0;
-    for (int b = 0; b < 32; ++b)
-    {
-      long long seen[32];
-      int n = 0;
-      for (int t = 0; t < 32; ++t)
-        if (((a[t] % 32) + 32) % 32 == b)
-        {
-          bool dup = false;
-          for (int k = 0; k < n; ++k)
-            dup = dup || seen[k] == a[t];
-          if (!dup)
-            seen[n++] = a[t];
-        }
-      worst = std::max(worst, n);
-    }
-    return worst;
-  }
-  int total = 0;
-  for (int h = 0; h < 2; ++h)
-  {
-    int worst = 0;
-    for (int b = 0; b < 16; ++b)
-    {
-      long long seen[16];
-      int n = 0;
-      for (int t = 16 * h; t < 16 * h + 16; ++t)
-        if (((a[t] % 16) + 16) % 16 == b)
-        {
-          bool dup = false;
-          for (int k = 0; k < n; ++k)
-            dup = dup || seen[k] == a[t];
-          if (!dup)
-            seen[n++] = a[t];
-        }
-      worst = std::max(worst, n);
-    }
-    total += worst;
-  }
-  return total;
-}
-
 // Strides of the slab kernels' work buffers: a slab (c, i0) starts at
-// c*sbc + i0*sq.  The forward/backward passes access them with one thread per
-// slab (addresses c*sbc + i0*sq + const), the fused pass with one thread per
-// pencil (c, r) (addresses c*sbc + r + const).  Pick the strides that
-// minimise the modelled bank-conflict wavefronts of both patterns.
+// c*sbc + i0*sq.  The kernels take them as compile-time constants from the
+// same table (slab_strides.hpp, chosen to minimise shared-memory bank
+// conflicts of the slab and pencil access patterns).
 std::pair<int, int> slab_layout(int n, int q, int esize, int lanes)
 {
-  static std::mutex m;
-  static std::map<std::tuple<int, int, int, int>, std::pair<int, int>> cache;
-  std::lock_guard<std::mutex> lk(m);
-  auto key = std::make_tuple(n, q, esize, lanes);
-  auto it = cache.find(key);
-  if (it != cache.end())
-    return it->second;
-  const int q2 = q * q;
-  double best = 1e30;
-  std::pair<int, int> res{q2, n * q2};
-  long long a[32];
-  for (int sq = q2; sq < q2 + 32; ++sq)
-    for (int sbc = n * sq; sbc < n * sq + 32; ++sbc)
-    {
-      double cost = 0.0;
-      for (int mm = 0; mm < n; ++mm)
-      {
-        for (int t = 0; t < 32; ++t)
-        {
-          const long long ts = 32LL * mm + t, sl = ts / lanes;
-          a[t] = (sl / n) * sbc + (sl % n) * sq + ts % lanes;
-        }
-        cost += double(wavefronts(a, esize)) / n;
-      }
-      for (int mm = 0; mm < q2; ++mm)
-      {
-        for (int t = 0; t < 32; ++t)
-        {
-          const long long pp = 32LL * mm + t;
-          a[t] = (pp / q2) * sbc + pp % q2;
-        }
-        cost += double(wavefronts(a, esize)) / q2;
-      }
-      cost += 1e-6 * sbc; // then the smaller footprint
-      if (cost < best)
-      {
-        best = cost;
-        res = {sq, sbc};
-      }
-    }
-  cache[key] = res;
-  return res;
+  const SlabStride s = slab_strides(n, q, esize, lanes);
+  return {s.sq, s.sbc};
 }
 
 // Lane efficiency of a tile of `cb` cells: useful thread slots over issued

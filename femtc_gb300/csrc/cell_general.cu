@@ -1,6 +1,7 @@
 // General-degree cell kernels: the mass and stiffness action for any degree
 // P = 1..25 (N = P+1 <= 26 DOFs per axis) and Q <= 28 quadrature points per
-// axis, FP64 and FP32, exact and reference semantics, with runtime sizes.
+// axis, FP64 and FP32 (exact and reference semantics) and the FP64-accurate
+// double-float form F64E (exact semantics), with runtime sizes.
 //
 // The reference dispatches degrees 1..25 (src/mass.hpp:57-137,
 // src/stiffness.hpp:109-181).  The slab kernels (cell_kernel.cuh) hold a
@@ -18,6 +19,13 @@
 // backward 3 + 2 + 1 with two-input contractions), the same tree as the
 // oracle's restatement of src/stiffness.hpp:34-99.
 //
+// Each thread computes two outputs of a contraction that share their input
+// column (one load of each input value feeds two accumulations: more
+// independent work per thread, half the input loads).  The double-float
+// form converts each cell's u from FP64 once into a work buffer (the
+// contractions then read double-float pairs) and its outputs back to FP64;
+// its multiply-adds run on the FP32 pipes (df64.cuh).
+//
 // Work buffers (max(N,Q)^3 values each; 3 for mass, 6 for stiffness) live
 // in shared memory when they fit next to the tables, else in a per-CTA
 // slice of a stream-ordered device workspace (cudaMallocAsync /
@@ -27,7 +35,10 @@
 // work buffers' traffic stays in L1/L2.
 #include "femtc_gpu.h"
 
+#include "df64.cuh"
 #include "registry.hpp"
+
+#include <type_traits>
 
 #include <algorithm>
 #include <cstring>
@@ -42,12 +53,43 @@ constexpr int kGenMaxN = 26; // degree 25
 constexpr int kGenMaxQ = 28;
 constexpr int kGenThreads = 256;
 
+// Storage type of an arithmetic type: double-float keeps FP64 storage.
+template <typename T>
+struct gen_storage
+{
+  using type = T;
+};
+template <>
+struct gen_storage<df64>
+{
+  using type = double;
+};
+
+template <typename T, typename S>
+__device__ __forceinline__ T load_as(S v)
+{
+  if constexpr (std::is_same<T, df64>::value && !std::is_same<S, df64>::value)
+    return to_df64(v);
+  else
+    return v;
+}
+
+template <typename S, typename T>
+__device__ __forceinline__ S store_as(T v)
+{
+  if constexpr (std::is_same<T, df64>::value && !std::is_same<S, df64>::value)
+    return to_double(v);
+  else
+    return v;
+}
+
 template <typename T>
 struct GenParams
 {
-  const T* u;      // [ncells][N^3]
-  T* y;            // [ncells][N^3]
-  const T* geo;    // mass [ncells][Q^3]; stiffness [ncells][Q^3][6]
+  using ST = typename gen_storage<T>::type;
+  const ST* u;     // [ncells][N^3]
+  ST* y;           // [ncells][N^3]
+  const ST* geo;   // mass [ncells][Q^3]; stiffness [ncells][Q^3][6]
   T* work;         // device workspace (null: the buffers are in shared memory)
   long long ncells;
   long long work_cta; // workspace elements per CTA
@@ -59,50 +101,62 @@ struct GenParams
 };
 
 // out[j*M + m] = sum_p A(m,p) in[p*L + j], A(m,p) = A[m*sm + p*sk], over all
-// threads of the CTA (no barrier inside).
-template <typename T>
-__device__ __forceinline__ void rot(int K, int L, int M, const T* __restrict__ A, int sm, int sk,
-                                    const T* __restrict__ in, T* __restrict__ out)
-{
-  const int total = L * M;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x)
-  {
-    const int j = idx / M, m = idx - j * M;
-    const T* a = A + m * sm;
-    const T* x = in + j;
-    T acc = a[0] * x[0];
-    for (int p = 1; p < K; ++p)
-      acc = fma(a[p * sk], x[(long long)p * L], acc);
-    out[idx] = acc;
-  }
-}
-
-// out = A in1 + B in2 (two contractions of the same shape into one output)
-template <typename T>
+// threads of the CTA (no barrier inside); with a second table/input pair
+// (B, in2) the sum also runs over B(m,p) in2[p*L + j].  A work item is an
+// output column j and two rows m, m+1 that share the input loads.
+template <typename T, typename O>
 __device__ __forceinline__ void rot2(int K, int L, int M, const T* __restrict__ A,
                                      const T* __restrict__ B, int sm, int sk,
                                      const T* __restrict__ in1, const T* __restrict__ in2,
-                                     T* __restrict__ out)
+                                     O* __restrict__ out)
 {
-  const int total = L * M;
+  const int mp = (M + 1) >> 1; // row pairs
+  const int total = L * mp;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x)
   {
-    const int j = idx / M, m = idx - j * M;
+    const int j = idx / mp, m = 2 * (idx - j * mp);
+    const bool two = m + 1 < M;
     const T* a = A + m * sm;
-    const T* b = B + m * sm;
-    T acc = a[0] * in1[j];
+    const T* a1 = A + (two ? m + 1 : m) * sm;
+    const T* x = in1 + j;
+    T acc0 = a[0] * x[0], acc1 = a1[0] * x[0];
     for (int p = 1; p < K; ++p)
-      acc = fma(a[p * sk], in1[(long long)p * L + j], acc);
-    for (int p = 0; p < K; ++p)
-      acc = fma(b[p * sk], in2[(long long)p * L + j], acc);
-    out[idx] = acc;
+    {
+      const T v = x[(long long)p * L];
+      acc0 = fma(a[p * sk], v, acc0);
+      acc1 = fma(a1[p * sk], v, acc1);
+    }
+    if (B)
+    {
+      const T* b = B + m * sm;
+      const T* b1 = B + (two ? m + 1 : m) * sm;
+      const T* z = in2 + j;
+      for (int p = 0; p < K; ++p)
+      {
+        const T v = z[(long long)p * L];
+        acc0 = fma(b[p * sk], v, acc0);
+        acc1 = fma(b1[p * sk], v, acc1);
+      }
+    }
+    out[j * M + m] = store_as<O>(acc0);
+    if (two)
+      out[j * M + m + 1] = store_as<O>(acc1);
   }
+}
+
+template <typename T, typename O>
+__device__ __forceinline__ void rot(int K, int L, int M, const T* __restrict__ A, int sm, int sk,
+                                    const T* __restrict__ in, O* __restrict__ out)
+{
+  rot2<T, O>(K, L, M, A, (const T*)nullptr, sm, sk, in, (const T*)nullptr, out);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kGenThreads)
     general_cell_kernel(const __grid_constant__ GenParams<T> p)
 {
+  using ST = typename gen_storage<T>::type;
+  constexpr bool kConvert = !std::is_same<T, ST>::value; // double-float: FP64 storage
   extern __shared__ __align__(16) unsigned char smem[];
   const int n = p.n, q = p.q, nq = n * q;
   const int n3 = n * n * n, q3 = q * q * q;
@@ -125,8 +179,21 @@ __global__ void __launch_bounds__(kGenThreads)
   __syncthreads();
   for (long long c = blockIdx.x; c < p.ncells; c += gridDim.x)
   {
-    const T* uc = p.u + c * n3;
-    T* yc = p.y + c * n3;
+    const ST* ug = p.u + c * n3;
+    ST* yc = p.y + c * n3;
+    // the forward contractions' input: u itself, or (double-float) u
+    // converted once into a work buffer that is free until it is read
+    const T* uc;
+    if constexpr (kConvert)
+    {
+      T* ub = stiff ? w5 : w2;
+      for (int i = threadIdx.x; i < n3; i += blockDim.x)
+        ub[i] = load_as<T>(ug[i]);
+      __syncthreads();
+      uc = ub;
+    }
+    else
+      uc = ug;
     if (!stiff)
     {
       // src/mass.hpp:36-47
@@ -136,9 +203,9 @@ __global__ void __launch_bounds__(kGenThreads)
       __syncthreads();
       rot(n, q * q, q, tP, 1, q, w1, w2);
       __syncthreads();
-      const T* dw = p.geo + c * q3;
+      const ST* dw = p.geo + c * q3;
       for (int i = threadIdx.x; i < q3; i += blockDim.x)
-        w2[i] *= dw[i];
+        w2[i] *= load_as<T>(dw[i]);
       __syncthreads();
       rot(q, q * q, n, tP, bsm, bsk, w2, w0);
       __syncthreads();
@@ -164,17 +231,19 @@ __global__ void __launch_bounds__(kGenThreads)
     rot(n, q * q, q, exact ? tD : tP, 1, q, w4, w5);
     __syncthreads();
     // G transform per point, [zz,yz,xz,yy,xy,xx] (src/stiffness.hpp:14-29)
-    const T* G = p.geo + c * q3 * 6;
+    const ST* G = p.geo + c * q3 * 6;
     for (int i = threadIdx.x; i < q3; i += blockDim.x)
     {
-      const T* g = G + 6 * i;
+      const ST* gs = G + 6 * i;
+      const T g0 = load_as<T>(gs[0]), g1 = load_as<T>(gs[1]), g2 = load_as<T>(gs[2]);
       const T a0 = w0[i], a1 = w1[i], a2 = w5[i];
       if (exact)
       {
-        w0[i] = g[5] * a0 + g[4] * a1 + g[2] * a2;
-        w1[i] = g[4] * a0 + g[3] * a1 + g[1] * a2;
+        const T g3 = load_as<T>(gs[3]), g4 = load_as<T>(gs[4]), g5 = load_as<T>(gs[5]);
+        w0[i] = g5 * a0 + g4 * a1 + g2 * a2;
+        w1[i] = g4 * a0 + g3 * a1 + g1 * a2;
       }
-      w5[i] = g[2] * a0 + g[1] * a1 + g[0] * a2;
+      w5[i] = g2 * a0 + g1 * a1 + g0 * a2;
     }
     __syncthreads();
     if (exact)
@@ -221,14 +290,15 @@ int sms()
 }
 
 template <typename T>
-int launch(int op, int sem, int n, int q, const T* tables, const void* u, void* y,
-           const void* geo, size_t ncells, cudaStream_t st)
+int launch(int op, int sem, int n, int q, const typename gen_storage<T>::type* tables,
+           const void* u, void* y, const void* geo, size_t ncells, cudaStream_t st)
 {
+  using ST = typename gen_storage<T>::type;
   GenParams<T> p;
   std::memset(&p, 0, sizeof(p));
-  p.u = static_cast<const T*>(u);
-  p.y = static_cast<T*>(y);
-  p.geo = static_cast<const T*>(geo);
+  p.u = static_cast<const ST*>(u);
+  p.y = static_cast<ST*>(y);
+  p.geo = static_cast<const ST*>(geo);
   p.ncells = (long long)ncells;
   p.n = n;
   p.q = q;
@@ -237,7 +307,13 @@ int launch(int op, int sem, int n, int q, const T* tables, const void* u, void* 
   const bool stiff = op == FEMTC_OP_STIFFNESS;
   // mass reads Phi only (the reference's mass table holds (P+1)^2 values)
   const int ntab = stiff ? 2 : 1;
-  std::memcpy(p.tab, tables, sizeof(T) * ntab * n * q);
+  for (int i = 0; i < ntab * n * q; ++i)
+  {
+    if constexpr (std::is_same<T, df64>::value)
+      p.tab[i] = host_df64(tables[i]);
+    else
+      p.tab[i] = tables[i];
+  }
   const int big = std::max(n, q);
   const int align = 16 / (int)sizeof(T);
   p.buf = (big * big * big + align - 1) / align * align;
@@ -287,10 +363,12 @@ bool general_supported(int op, int dtype, int sem, int n, int q)
 {
   if (op != FEMTC_OP_MASS && op != FEMTC_OP_STIFFNESS)
     return false;
-  if (dtype != FEMTC_F64 && dtype != FEMTC_F32)
+  if (dtype != FEMTC_F64 && dtype != FEMTC_F32 && dtype != FEMTC_F64E)
     return false;
   if (n < 2 || n > kGenMaxN || q < 1 || q > kGenMaxQ)
     return false;
+  if (dtype == FEMTC_F64E)
+    return sem == FEMTC_EXACT; // the double-float form: exact semantics
   return sem == FEMTC_EXACT || (sem == FEMTC_REFERENCE && q == n);
 }
 
@@ -304,6 +382,9 @@ int launch_general(int op, int dtype, int sem, int n, int q, const void* tables,
   if (dtype == FEMTC_F64)
     return launch<double>(op, sem, n, q, static_cast<const double*>(tables), u, y, geo, ncells,
                           st);
+  if (dtype == FEMTC_F64E)
+    return launch<df64>(op, sem, n, q, static_cast<const double*>(tables), u, y, geo, ncells,
+                        st);
   return launch<float>(op, sem, n, q, static_cast<const float*>(tables), u, y, geo, ncells, st);
 }
 } // namespace femtc

@@ -114,8 +114,9 @@ constexpr SlabStride kSlabStrides[] = {
     {9, 10, 8, 2, 102, 918}
 };
 
-// {sq, sbc} of (n, q, esize, lanes); sq = 0 when the table has no entry
-__host__ __device__ constexpr SlabStride slab_strides(int n, int q, int esize, int lanes)
+// {sq, sbc} of (n, q, esize, lanes); sq = 0 when the table has no entry.
+// Host function: device code uses it only in constant expressions.
+constexpr SlabStride slab_strides(int n, int q, int esize, int lanes)
 {
   for (const SlabStride& s : kSlabStrides)
     if (s.n == n && s.q == q && s.esize == esize && s.lanes == lanes)

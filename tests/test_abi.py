@@ -193,7 +193,8 @@ def test_supported_general_degrees(femtc):
                 assert femtc.supported(op, dt, femtc.REFERENCE, P, P + 1)
                 assert femtc.supported(op, dt, femtc.EXACT, P, P + 2)
                 assert not femtc.supported(op, dt, femtc.REFERENCE, P, P + 2)
-        assert not femtc.supported(femtc.MASS, femtc.F64E, femtc.EXACT, P, P + 2)
+        assert femtc.supported(femtc.MASS, femtc.F64E, femtc.EXACT, P, P + 2)
+        assert not femtc.supported(femtc.MASS, femtc.F64E, femtc.REFERENCE, P, P + 1)
         assert not femtc.supported(femtc.STIFFNESS, femtc.BF16X3, femtc.EXACT, P, P + 2)
     assert not femtc.supported(femtc.MASS, femtc.F64, femtc.REFERENCE, 26, 27)
     assert not femtc.supported(femtc.MASS, femtc.F64, femtc.EXACT, 25, 29)

@@ -26,7 +26,7 @@ def relerr(a, b):
 
 @pytest.mark.parametrize("name,ncells,dtypes", [
     ("stiffness_p4", 2048, [0, 1, 2, 3, 4]),
-    ("stiffness_p6", 4096, [0, 1, 2, 3]),
+    ("stiffness_p6", 4096, [0, 1, 2, 3, 4]),
     ("mass_p3", 4096, [0, 1, 2, 3, 4]),
 ])
 def test_workload_forms_vs_oracle(femtc, orc, dev, name, ncells, dtypes):

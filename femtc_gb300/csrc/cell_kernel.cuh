@@ -275,11 +275,11 @@ __device__ __forceinline__ void mv(const T* __restrict__ A, const T (&x)[K],
 #pragma unroll
   for (int m = 0; m < M; ++m)
   {
-    T acc = A[m * SM] * x[0];
+    acc_t<T> acc = acc_mul(A[m * SM], x[0]);
 #pragma unroll
     for (int k = 1; k < K; ++k)
-      acc = fma(A[m * SM + k * SK], x[k], acc);
-    y[m] = acc;
+      acc = acc_fma(A[m * SM + k * SK], x[k], acc);
+    y[m] = acc_val(acc);
   }
 }
 
@@ -291,11 +291,11 @@ __device__ __forceinline__ void mv_acc(const T* __restrict__ A,
 #pragma unroll
   for (int m = 0; m < M; ++m)
   {
-    T acc = y[m];
+    acc_t<T> acc = acc_from(y[m]);
 #pragma unroll
     for (int k = 0; k < K; ++k)
-      acc = fma(A[m * SM + k * SK], x[k], acc);
-    y[m] = acc;
+      acc = acc_fma(A[m * SM + k * SK], x[k], acc);
+    y[m] = acc_val(acc);
   }
 }
 
@@ -334,16 +334,17 @@ __device__ __forceinline__ void mv_eo(const T* __restrict__ t, const T (&x)[K], 
 #pragma unroll
   for (int m = 0; m < S::M2; ++m)
   {
-    T s = t[m * K + S::E] * xe[0];
+    acc_t<T> sa = acc_mul(t[m * K + S::E], xe[0]);
 #pragma unroll
     for (int k = 1; k < S::K2; ++k)
-      s = fma(t[m * K + S::E + k], xe[k], s);
+      sa = acc_fma(t[m * K + S::E + k], xe[k], sa);
     if constexpr (S::KM)
-      s = fma(t[m * K + S::C], x[S::K2], s);
-    T d = t[m * K + S::O] * xo[0];
+      sa = acc_fma(t[m * K + S::C], x[S::K2], sa);
+    acc_t<T> da = acc_mul(t[m * K + S::O], xo[0]);
 #pragma unroll
     for (int k = 1; k < S::K2; ++k)
-      d = fma(t[m * K + S::O + k], xo[k], d);
+      da = acc_fma(t[m * K + S::O + k], xo[k], da);
+    const T s = acc_val(sa), d = acc_val(da);
     y[m] = s + d;
     y[M - 1 - m] = SIG > 0 ? s - d : d - s;
   }
@@ -352,21 +353,21 @@ __device__ __forceinline__ void mv_eo(const T* __restrict__ t, const T (&x)[K], 
     constexpr int m = S::M2;
     if constexpr (SIG > 0)
     {
-      T s = t[m * K + S::E] * xe[0];
+      acc_t<T> sa = acc_mul(t[m * K + S::E], xe[0]);
 #pragma unroll
       for (int k = 1; k < S::K2; ++k)
-        s = fma(t[m * K + S::E + k], xe[k], s);
+        sa = acc_fma(t[m * K + S::E + k], xe[k], sa);
       if constexpr (S::KM)
-        s = fma(t[m * K + S::C], x[S::K2], s);
-      y[m] = s;
+        sa = acc_fma(t[m * K + S::C], x[S::K2], sa);
+      y[m] = acc_val(sa);
     }
     else
     {
-      T d = t[m * K + S::O] * xo[0];
+      acc_t<T> da = acc_mul(t[m * K + S::O], xo[0]);
 #pragma unroll
       for (int k = 1; k < S::K2; ++k)
-        d = fma(t[m * K + S::O + k], xo[k], d);
-      y[m] = d;
+        da = acc_fma(t[m * K + S::O + k], xo[k], da);
+      y[m] = acc_val(da);
     }
   }
 }
@@ -828,16 +829,18 @@ struct SlabTile
       };
       // even and odd sums of row i1 against row j of an even-odd table
       auto sums = [&](const T* __restrict__ t, int j, int i1, T& s, T& d) {
-        s = t[j * N + E::E] * xe[i1][0];
+        acc_t<T> sa = acc_mul(t[j * N + E::E], xe[i1][0]);
 #pragma unroll
         for (int k = 1; k < E::K2; ++k)
-          s = fma(t[j * N + E::E + k], xe[i1][k], s);
+          sa = acc_fma(t[j * N + E::E + k], xe[i1][k], sa);
         if constexpr (E::KM)
-          s = fma(t[j * N + E::C], x[i1 * N + E::K2], s);
-        d = t[j * N + E::O] * xo[i1][0];
+          sa = acc_fma(t[j * N + E::C], x[i1 * N + E::K2], sa);
+        acc_t<T> da = acc_mul(t[j * N + E::O], xo[i1][0]);
 #pragma unroll
         for (int k = 1; k < E::K2; ++k)
-          d = fma(t[j * N + E::O + k], xo[i1][k], d);
+          da = acc_fma(t[j * N + E::O + k], xo[i1][k], da);
+        s = acc_val(sa);
+        d = acc_val(da);
       };
 #pragma unroll
       for (int j = 0; j < E::M2; ++j) // column pair (j, Q-1-j)
@@ -867,20 +870,20 @@ struct SlabTile
 #pragma unroll
         for (int i1 = 0; i1 < N; ++i1)
         {
-          T s = PF[j * N + E::E] * xe[i1][0];
+          acc_t<T> sa = acc_mul(PF[j * N + E::E], xe[i1][0]);
 #pragma unroll
           for (int k = 1; k < E::K2; ++k)
-            s = fma(PF[j * N + E::E + k], xe[i1][k], s);
+            sa = acc_fma(PF[j * N + E::E + k], xe[i1][k], sa);
           if constexpr (E::KM)
-            s = fma(PF[j * N + E::C], x[i1 * N + E::K2], s);
-          a[i1] = s;
+            sa = acc_fma(PF[j * N + E::C], x[i1 * N + E::K2], sa);
+          a[i1] = acc_val(sa);
           if constexpr (kGrad)
           {
-            T d = DF[j * N + E::O] * xo[i1][0];
+            acc_t<T> da = acc_mul(DF[j * N + E::O], xo[i1][0]);
 #pragma unroll
             for (int k = 1; k < E::K2; ++k)
-              d = fma(DF[j * N + E::O + k], xo[i1][k], d);
-            g[i1] = d;
+              da = acc_fma(DF[j * N + E::O + k], xo[i1][k], da);
+            g[i1] = acc_val(da);
           }
         }
         emit(j, a, g);
@@ -947,42 +950,42 @@ struct SlabTile
 #pragma unroll
         for (int i1 = 0; i1 < N; ++i1)
         {
-          T acc = pq(0) * x[i1 * N];
+          acc_t<T> acc = acc_mul(pq(0), x[i1 * N]);
 #pragma unroll
           for (int i2 = 1; i2 < N; ++i2)
-            acc = fma(pq(i2), x[i1 * N + i2], acc);
-          a[i1] = acc;
+            acc = acc_fma(pq(i2), x[i1 * N + i2], acc);
+          a[i1] = acc_val(acc);
           if constexpr (kGrad && SEM == SEM_EXACT)
           {
-            T gcc = dq(0) * x[i1 * N];
+            acc_t<T> gcc = acc_mul(dq(0), x[i1 * N]);
 #pragma unroll
             for (int i2 = 1; i2 < N; ++i2)
-              gcc = fma(dq(i2), x[i1 * N + i2], gcc);
-            g[i1] = gcc;
+              gcc = acc_fma(dq(i2), x[i1 * N + i2], gcc);
+            g[i1] = acc_val(gcc);
           }
         }
 #pragma unroll
         for (int q1 = 0; q1 < Q; ++q1)
         {
-          T o0 = P[q1] * a[0];
+          acc_t<T> o0 = acc_mul(P[q1], a[0]);
 #pragma unroll
           for (int i1 = 1; i1 < N; ++i1)
-            o0 = fma(P[q1 + i1 * Q], a[i1], o0);
-          b0[q1 * Q + q2] = o0; // AA = Phi_1 Phi_2 u
+            o0 = acc_fma(P[q1 + i1 * Q], a[i1], o0);
+          b0[q1 * Q + q2] = acc_val(o0); // AA = Phi_1 Phi_2 u
           if constexpr (kGrad)
           {
-            T o1 = D[q1] * a[0];
+            acc_t<T> o1 = acc_mul(D[q1], a[0]);
 #pragma unroll
             for (int i1 = 1; i1 < N; ++i1)
-              o1 = fma(D[q1 + i1 * Q], a[i1], o1);
-            b1[q1 * Q + q2] = o1; // AG = Gamma_1 Phi_2 u
+              o1 = acc_fma(D[q1 + i1 * Q], a[i1], o1);
+            b1[q1 * Q + q2] = acc_val(o1); // AG = Gamma_1 Phi_2 u
             if constexpr (SEM == SEM_EXACT)
             {
-              T o2 = P[q1] * g[0];
+              acc_t<T> o2 = acc_mul(P[q1], g[0]);
 #pragma unroll
               for (int i1 = 1; i1 < N; ++i1)
-                o2 = fma(P[q1 + i1 * Q], g[i1], o2);
-              b2[q1 * Q + q2] = o2; // BA = Phi_1 Gamma_2 u
+                o2 = acc_fma(P[q1 + i1 * Q], g[i1], o2);
+              b2[q1 * Q + q2] = acc_val(o2); // BA = Phi_1 Gamma_2 u
             }
           }
         }
@@ -1161,14 +1164,15 @@ struct SlabTile
       const T* b0 = sw + c * SBC + i0 * SQ;
       const T* b1 = b0 + bstride;
       const T* b2 = b1 + bstride;
-      T A[N][E::M2 > 0 ? E::M2 : 1], B[N][E::M2 > 0 ? E::M2 : 1], Mid[N];
+      // accumulators (double-float: lazily renormalised, see df64acc)
+      acc_t<T> A[N][E::M2 > 0 ? E::M2 : 1], B[N][E::M2 > 0 ? E::M2 : 1], Mid[N];
 #pragma unroll
       for (int i1 = 0; i1 < N; ++i1)
       {
 #pragma unroll
         for (int i2 = 0; i2 < E::M2; ++i2)
-          A[i1][i2] = B[i1][i2] = T(0);
-        Mid[i1] = T(0);
+          A[i1][i2] = B[i1][i2] = acc_zero<T>();
+        Mid[i1] = acc_zero<T>();
       }
       // axis 1 back of column q2: u1 = Phi^T X (+ Gamma^T Y), u2 = Phi^T Z
       auto column = [&](int q2, T(&u1)[N], T(&u2)[N]) {
@@ -1206,22 +1210,22 @@ struct SlabTile
 #pragma unroll
           for (int i2 = 0; i2 < E::M2; ++i2)
           {
-            A[i1][i2] = fma(PB[i2 * Q + E::E + j], e1, A[i1][i2]);
-            B[i1][i2] = fma(PB[i2 * Q + E::O + j], o1, B[i1][i2]);
+            A[i1][i2] = acc_fma(PB[i2 * Q + E::E + j], e1, A[i1][i2]);
+            B[i1][i2] = acc_fma(PB[i2 * Q + E::O + j], o1, B[i1][i2]);
           }
           if constexpr (E::MM)
-            Mid[i1] = fma(PB[E::M2 * Q + E::E + j], e1, Mid[i1]);
+            Mid[i1] = acc_fma(PB[E::M2 * Q + E::E + j], e1, Mid[i1]);
           if constexpr (kGrad)
           {
             const T e2 = u2a[i1] + u2b[i1], o2 = u2a[i1] - u2b[i1];
 #pragma unroll
             for (int i2 = 0; i2 < E::M2; ++i2)
             {
-              A[i1][i2] = fma(DB[i2 * Q + E::O + j], o2, A[i1][i2]); // d_Gamma
-              B[i1][i2] = fma(DB[i2 * Q + E::E + j], e2, B[i1][i2]); // s_Gamma
+              A[i1][i2] = acc_fma(DB[i2 * Q + E::O + j], o2, A[i1][i2]); // d_Gamma
+              B[i1][i2] = acc_fma(DB[i2 * Q + E::E + j], e2, B[i1][i2]); // s_Gamma
             }
             if constexpr (E::MM)
-              Mid[i1] = fma(DB[E::M2 * Q + E::O + j], o2, Mid[i1]);
+              Mid[i1] = acc_fma(DB[E::M2 * Q + E::O + j], o2, Mid[i1]);
           }
         }
       }
@@ -1235,12 +1239,12 @@ struct SlabTile
 #pragma unroll
           for (int i2 = 0; i2 < E::M2; ++i2)
           {
-            A[i1][i2] = fma(PB[i2 * Q + E::C], u1[i1], A[i1][i2]); // s_Phi
+            A[i1][i2] = acc_fma(PB[i2 * Q + E::C], u1[i1], A[i1][i2]); // s_Phi
             if constexpr (kGrad)
-              B[i1][i2] = fma(DB[i2 * Q + E::C], u2[i1], B[i1][i2]); // s_Gamma
+              B[i1][i2] = acc_fma(DB[i2 * Q + E::C], u2[i1], B[i1][i2]); // s_Gamma
           }
           if constexpr (E::MM) // Gamma^T vanishes at the centre
-            Mid[i1] = fma(PB[E::M2 * Q + E::C], u1[i1], Mid[i1]);
+            Mid[i1] = acc_fma(PB[E::M2 * Q + E::C], u1[i1], Mid[i1]);
         }
       }
       T y[N2];
@@ -1250,11 +1254,12 @@ struct SlabTile
 #pragma unroll
         for (int i2 = 0; i2 < E::M2; ++i2)
         {
-          y[i1 * N + i2] = A[i1][i2] + B[i1][i2];
-          y[i1 * N + N - 1 - i2] = A[i1][i2] - B[i1][i2];
+          const T av = acc_val(A[i1][i2]), bv = acc_val(B[i1][i2]);
+          y[i1 * N + i2] = av + bv;
+          y[i1 * N + N - 1 - i2] = av - bv;
         }
         if constexpr (E::MM)
-          y[i1 * N + E::M2] = Mid[i1];
+          y[i1 * N + E::M2] = acc_val(Mid[i1]);
       }
       store_slab(sy + sl * US, y);
     }
@@ -1309,10 +1314,10 @@ struct SlabTile
       const T* b0 = sw + c * SBC + i0 * SQ;
       const T* b1 = b0 + bstride;
       const T* b2 = b1 + bstride;
-      T y[N2];
+      acc_t<T> ya[N2]; // accumulators (double-float: lazily renormalised)
 #pragma unroll
       for (int k = 0; k < N2; ++k)
-        y[k] = T(0);
+        ya[k] = acc_zero<T>();
 #pragma unroll UNR
       for (int jq = 0; jq < QS; ++jq)
       {
@@ -1334,22 +1339,22 @@ struct SlabTile
 #pragma unroll
         for (int i1 = 0; i1 < N; ++i1)
         {
-          T acc = P[i1 * BSM] * X[0];
+          acc_t<T> acc = acc_mul(P[i1 * BSM], X[0]);
 #pragma unroll
           for (int q1 = 1; q1 < Q; ++q1)
-            acc = fma(P[i1 * BSM + q1 * BSK], X[q1], acc);
+            acc = acc_fma(P[i1 * BSM + q1 * BSK], X[q1], acc);
           if constexpr (kGrad && SEM == SEM_EXACT)
           {
 #pragma unroll
             for (int q1 = 0; q1 < Q; ++q1)
-              acc = fma(D[i1 * BSM + q1 * BSK], Y[q1], acc);
-            T acc2 = P[i1 * BSM] * Z[0];
+              acc = acc_fma(D[i1 * BSM + q1 * BSK], Y[q1], acc);
+            acc_t<T> acc2 = acc_mul(P[i1 * BSM], Z[0]);
 #pragma unroll
             for (int q1 = 1; q1 < Q; ++q1)
-              acc2 = fma(P[i1 * BSM + q1 * BSK], Z[q1], acc2);
-            U2[i1] = acc2;
+              acc2 = acc_fma(P[i1 * BSM + q1 * BSK], Z[q1], acc2);
+            U2[i1] = acc_val(acc2);
           }
-          U1[i1] = acc;
+          U1[i1] = acc_val(acc);
         }
         // axis 2 back (q2 -> i2), accumulated over q2
 #pragma unroll
@@ -1362,7 +1367,7 @@ struct SlabTile
             t1 = T2[i2 * BSM + q2 * BSK];
 #pragma unroll
           for (int i1 = 0; i1 < N; ++i1)
-            y[i1 * N + i2] = fma(t1, U1[i1], y[i1 * N + i2]);
+            ya[i1 * N + i2] = acc_fma(t1, U1[i1], ya[i1 * N + i2]);
           if constexpr (kGrad && SEM == SEM_EXACT)
           {
             T t2;
@@ -1372,10 +1377,14 @@ struct SlabTile
               t2 = D[i2 * BSM + q2 * BSK];
 #pragma unroll
             for (int i1 = 0; i1 < N; ++i1)
-              y[i1 * N + i2] = fma(t2, U2[i1], y[i1 * N + i2]);
+              ya[i1 * N + i2] = acc_fma(t2, U2[i1], ya[i1 * N + i2]);
           }
         }
       }
+      T y[N2];
+#pragma unroll
+      for (int k = 0; k < N2; ++k)
+        y[k] = acc_val(ya[k]);
       if constexpr (S > 1)
       {
 #pragma unroll

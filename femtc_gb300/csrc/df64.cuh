@@ -109,6 +109,93 @@ __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c)
   return df64(hi, lo);
 }
 
+// ---------------------------------------------------------------------------
+// Lazy accumulation of a sum of products, sum_k a_k x_k, in double-float:
+// the high parts are summed with TwoSum and every rounding error (of the
+// products, by the FMA-based TwoProduct, and of the sums) is gathered in one
+// FP32 word; the pair is renormalised once, when the value is read.  That is
+// the compensated dot product of Ogita, Rump and Oishi ("Accurate sum and
+// dot product", SIAM J. Sci. Comput. 26, 2005, Dot2) applied to double-float
+// operands: 12 FP32 operations per term instead of 15 for a renormalised
+// df64 fma, and only the high-part addition lies on the chain from one term
+// to the next.  The result keeps double-float accuracy (about 2^-48
+// relative to the sum of |a_k x_k|).
+struct df64acc
+{
+  float s, e; // value s + e, not normalised
+};
+
+__device__ __forceinline__ df64acc acc_mul(df64 a, df64 b)
+{
+  df64acc r;
+  r.s = two_prod(a.h, b.h, r.e);
+  r.e = __fmaf_rn(a.h, b.l, r.e);
+  r.e = __fmaf_rn(a.l, b.h, r.e);
+  return r;
+}
+
+__device__ __forceinline__ df64acc acc_fma(df64 a, df64 b, df64acc c)
+{
+  float pe;
+  const float p = two_prod(a.h, b.h, pe);
+  pe = __fmaf_rn(a.h, b.l, pe);
+  pe = __fmaf_rn(a.l, b.h, pe);
+  float t;
+  c.s = two_sum(c.s, p, t);
+  c.e += t + pe;
+  return c;
+}
+
+__device__ __forceinline__ df64 acc_val(df64acc c)
+{
+  float lo;
+  const float hi = fast_two_sum(c.s, c.e, lo);
+  return df64(hi, lo);
+}
+
+__device__ __forceinline__ df64acc acc_from(df64 v) { return df64acc{v.h, v.l}; }
+
+// The same interface for plain FP32 / FP64 arithmetic: the accumulator is
+// the value and every call is the ordinary operation.
+template <typename T>
+struct acc_of
+{
+  using type = T;
+};
+template <>
+struct acc_of<df64>
+{
+  using type = df64acc;
+};
+template <typename T>
+using acc_t = typename acc_of<T>::type;
+
+template <typename T>
+__device__ __forceinline__ acc_t<T> acc_zero();
+template <>
+__device__ __forceinline__ float acc_zero<float>()
+{
+  return 0.f;
+}
+template <>
+__device__ __forceinline__ double acc_zero<double>()
+{
+  return 0.0;
+}
+template <>
+__device__ __forceinline__ df64acc acc_zero<df64>()
+{
+  return df64acc{0.f, 0.f};
+}
+__device__ __forceinline__ float acc_mul(float a, float b) { return a * b; }
+__device__ __forceinline__ double acc_mul(double a, double b) { return a * b; }
+__device__ __forceinline__ float acc_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double acc_fma(double a, double b, double c) { return ::fma(a, b, c); }
+__device__ __forceinline__ float acc_val(float c) { return c; }
+__device__ __forceinline__ double acc_val(double c) { return c; }
+__device__ __forceinline__ float acc_from(float v) { return v; }
+__device__ __forceinline__ double acc_from(double v) { return v; }
+
 __device__ __forceinline__ df64 shfl_xor(df64 v, int lane_mask)
 {
   return df64(__shfl_xor_sync(0xffffffffu, v.h, lane_mask),

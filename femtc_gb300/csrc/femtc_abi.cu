@@ -1063,7 +1063,11 @@ int femtc_even_odd_used(int op, int dtype, int semantics, int degree, int nquad,
     return fail(FEMTC_ERR_INVALID, "null tables");
   const auto sel = select_variant(op, dtype, semantics, degree + 1, nquad);
   if (!sel.first)
+  {
+    if (general_supported(op, dtype, semantics, degree + 1, nquad))
+      return 0; // the general-degree kernel has no even-odd form
     return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
+  }
   return launch_form(*sel.first, tables).eo;
 }
 
@@ -1369,7 +1373,20 @@ int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
 {
   const auto sel = select_variant(op, dtype, semantics, degree + 1, nquad);
   if (!sel.first)
-    return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
+  {
+    if (!general_supported(op, dtype, semantics, degree + 1, nquad))
+      return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
+    // the general-degree kernel: one cell per CTA of 256 threads
+    if (lanes)
+      *lanes = 1;
+    if (cb)
+      *cb = 1;
+    if (geo_staged)
+      *geo_staged = 0;
+    if (threads)
+      *threads = 256;
+    return FEMTC_OK;
+  }
   const TileCfg c = sel.second;
   if (lanes)
     *lanes = sel.first->lanes;

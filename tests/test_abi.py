@@ -198,3 +198,10 @@ def test_supported_general_degrees(femtc):
         assert not femtc.supported(femtc.STIFFNESS, femtc.BF16X3, femtc.EXACT, P, P + 2)
     assert not femtc.supported(femtc.MASS, femtc.F64, femtc.REFERENCE, 26, 27)
     assert not femtc.supported(femtc.MASS, femtc.F64, femtc.EXACT, 25, 29)
+
+
+def test_general_kernel_tile_config_and_even_odd_query(femtc):
+    # the general-degree kernel has one fixed shape and no even-odd form
+    t = femtc.tabulate(12, 14)[0]
+    assert femtc.get_tile_config(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 12, 14) == (1, 0, 256, 1)
+    assert femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 12, 14, t) is False

@@ -799,15 +799,20 @@ def run_operator(args, name, dtypes_arg, rank, world, dev, pg, local, e2e_on=Tru
             barrier()
             l0 = F.operator_launches()
             t0 = time.perf_counter()
+            marks = [t0]
             for _ in range(args.steps):
-                estep()
+                estep()  # synchronous: returns when y is written on the host
+                marks.append(time.perf_counter())
             barrier()
             el = maxreduce(time.perf_counter() - t0)
             if mode == 0:
                 launches_timed[0] += F.operator_launches() - l0
+            # per-call rates: the spread of the host-link rate between calls
+            per = sorted(w.ndofs / (b - a) / 1e9 for a, b in zip(marks, marks[1:]))
             e2e[(dtype, mode)] = dict(gdofs=world * args.steps * w.ndofs / el / 1e9,
                                       h2d=uh.numel() * uh.element_size() + gh.numel() * gh.element_size(),
-                                      d2h=yh.numel() * yh.element_size())
+                                      d2h=yh.numel() * yh.element_size(),
+                                      per_call=[per[0], per[len(per) // 2], per[-1]])
         F.set_host_path(0)
 
     r = results[head]
@@ -868,6 +873,7 @@ def run_operator(args, name, dtypes_arg, rank, world, dev, pg, local, e2e_on=Tru
                        "h2d_bytes_per_step": a["h2d"], "d2h_bytes_per_step": a["d2h"],
                        "path": "femtc_*_apply_host, pinned host buffers, host-path mode "
                                "auto (tuned: zero-copy or staging pipeline)",
+                       "per_call_gdofs_min_median_max": a["per_call"],
                        "zero_copy_gdofs": z["gdofs"], "staging_pipeline_gdofs": c["gdofs"],
                        "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
                        "host_link_ceiling_gdofs": w.ndofs / link_s / 1e9}

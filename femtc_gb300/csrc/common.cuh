@@ -159,6 +159,13 @@ __device__ __forceinline__ void bulk_wait0()
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
+// Hint: fetch the line holding p into L2 (no result, no register; p must
+// lie inside an allocation).
+__device__ __forceinline__ void prefetch_l2(const void* p)
+{
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void record_fault(unsigned bits)
 {
   atomicOr(&g_fault_word, bits);

@@ -76,6 +76,8 @@ Registry& registry()
     register_cell_affine_f64e_stiffness(r.cells, r.faults);
     register_cell_f64e_mass(r.cells, r.faults);
     register_cell_f64e_stiffness(r.cells, r.faults);
+    register_cell_f64e_mass_l2(r.cells, r.faults);
+    register_cell_f64e_stiffness_l2(r.cells, r.faults);
     register_mma_f16x2_mass(r.cells, r.faults);
     register_mma_f16x2_stiffness(r.cells, r.faults);
     register_mma_bf16x3_mass(r.cells, r.faults);

@@ -41,6 +41,8 @@ void register_cell_f64eeo_mass(std::vector<CellVariant>&, std::vector<FaultReade
 void register_cell_f64eeo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64e_mass_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64e_stiffness_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_affine_f64_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_affine_f64_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_affine_f32_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);

@@ -24,7 +24,8 @@
 // independent work per thread, half the input loads).  The double-float
 // form converts each cell's u from FP64 once into a work buffer (the
 // contractions then read double-float pairs) and its outputs back to FP64;
-// its multiply-adds run on the FP32 pipes (df64.cuh).
+// its multiply-adds run on the FP32 pipes, each sum renormalised once
+// (df64.cuh).
 //
 // Work buffers (max(N,Q)^3 values each; 3 for mass, 6 for stiffness) live
 // in shared memory when they fit next to the tables, else in a per-CTA
@@ -119,12 +120,13 @@ __device__ __forceinline__ void rot2(int K, int L, int M, const T* __restrict__ 
     const T* a = A + m * sm;
     const T* a1 = A + (two ? m + 1 : m) * sm;
     const T* x = in1 + j;
-    T acc0 = a[0] * x[0], acc1 = a1[0] * x[0];
+    // accumulators (double-float: renormalised once per sum, df64acc)
+    acc_t<T> acc0 = acc_mul(a[0], x[0]), acc1 = acc_mul(a1[0], x[0]);
     for (int p = 1; p < K; ++p)
     {
       const T v = x[(long long)p * L];
-      acc0 = fma(a[p * sk], v, acc0);
-      acc1 = fma(a1[p * sk], v, acc1);
+      acc0 = acc_fma(a[p * sk], v, acc0);
+      acc1 = acc_fma(a1[p * sk], v, acc1);
     }
     if (B)
     {
@@ -134,13 +136,13 @@ __device__ __forceinline__ void rot2(int K, int L, int M, const T* __restrict__ 
       for (int p = 0; p < K; ++p)
       {
         const T v = z[(long long)p * L];
-        acc0 = fma(b[p * sk], v, acc0);
-        acc1 = fma(b1[p * sk], v, acc1);
+        acc0 = acc_fma(b[p * sk], v, acc0);
+        acc1 = acc_fma(b1[p * sk], v, acc1);
       }
     }
-    out[j * M + m] = store_as<O>(acc0);
+    out[j * M + m] = store_as<O>(acc_val(acc0));
     if (two)
-      out[j * M + m + 1] = store_as<O>(acc1);
+      out[j * M + m + 1] = store_as<O>(acc_val(acc1));
   }
 }
 

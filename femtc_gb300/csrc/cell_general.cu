@@ -329,11 +329,8 @@ int launch(int op, int sem, int n, int q, const typename gen_storage<T>::type* t
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess)
     return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
-  // shared-memory buffers: 128-thread CTAs, more of them per SM, so that
-  // one CTA's barriers overlap the others' work; a workspace: 256 threads
-  const int nt = in_smem ? 128 : kGenThreads;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGenThreads, smem);
   if (e != cudaSuccess || per_sm < 1)
     return aux_fail(FEMTC_ERR_UNSUPPORTED, "general cell kernel does not fit on an SM");
   // workspace mode: two CTAs per SM bound the workspace (they are FP64- or
@@ -351,7 +348,7 @@ int launch(int op, int sem, int n, int q, const typename gen_storage<T>::type* t
     p.work = static_cast<T*>(work);
   }
   void* args[] = {&p};
-  e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3((unsigned)nt), args, smem, st);
+  e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kGenThreads), args, smem, st);
   if (work)
   {
     const cudaError_t f = cudaFreeAsync(work, st);
@@ -363,18 +360,6 @@ int launch(int op, int sem, int n, int q, const typename gen_storage<T>::type* t
   return FEMTC_OK;
 }
 } // namespace
-
-int general_threads(int op, int dtype, int n, int q)
-{
-  // the same rule as launch<T>: shared-memory buffers take 128-thread CTAs
-  const size_t es = dtype == FEMTC_F32 ? 4 : 8;
-  const int align = (int)(16 / es);
-  const int big = std::max(n, q);
-  const size_t buf = (size_t)(big * big * big + align - 1) / align * align;
-  const size_t tab = (size_t)(2 * n * q + align - 1) / align * align;
-  const int nbuf = op == FEMTC_OP_STIFFNESS ? 6 : 3;
-  return es * (tab + buf * nbuf) <= (size_t)max_smem_optin() ? 128 : kGenThreads;
-}
 
 bool general_supported(int op, int dtype, int sem, int n, int q)
 {

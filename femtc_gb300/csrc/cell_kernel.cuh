@@ -551,7 +551,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     if (staged)
       Tile::fused(tv, sw, ncb, sg(s), 0);
     else
-      Tile::fused(tv, sw, ncb, p.geo, tile * cb);
+      Tile::fused(tv, sw, ncb, p.geo, tile * cb, !p.host_io);
     if (warp0)
       bulk_wait_read0(); // the previous tile's stores have left sy
     __syncthreads();
@@ -996,15 +996,18 @@ struct SlabTile
   static __device__ __forceinline__ void fused(const TabView<T>& p,
                                                T* __restrict__ sw, int ncb,
                                                const ST* __restrict__ geo,
-                                               long long geo_cell0)
+                                               long long geo_cell0, bool l2pf = false)
   {
-    fused(p, sw, cta_part(ncb), geo, geo_cell0);
+    fused(p, sw, cta_part(ncb), geo, geo_cell0, l2pf);
   }
 
+  // l2pf: the per-point geometry is read from device memory; each thread
+  // asks L2 for its next pencil's geometry lines (one per point) while it
+  // computes this pencil, so those loads wait on L2 instead of HBM.
   static __device__ __forceinline__ void fused(const TabView<T>& p,
                                                T* __restrict__ sw, const Part& w,
                                                const ST* __restrict__ geo,
-                                               long long geo_cell0)
+                                               long long geo_cell0, bool l2pf = false)
   {
     const T* __restrict__ P = p.P;
     const T* __restrict__ D = p.D;
@@ -1020,6 +1023,18 @@ struct SlabTile
       T* b1 = b0 + bstride;
       T* b2 = b1 + bstride;
       constexpr int sq = SQ;
+      if constexpr (geo_nc(OP) > 0)
+      {
+        const int tn = t + w.nthr; // this thread's next pencil, if any
+        if (l2pf && tn < w.c1 * Q2)
+        {
+          const int cn = tn / Q2, rn = tn - cn * Q2;
+          const ST* gn = geo + ((geo_cell0 + cn) * Q3 + rn) * geo_nc(OP);
+#pragma unroll
+          for (int q = 0; q < Q; ++q)
+            prefetch_l2(gn + (long long)q * Q2 * geo_nc(OP));
+        }
+      }
       if constexpr (OP == OP_MASS_AFFINE)
       {
         // detJ scales the pencil's N inputs (the weights are in PB)
@@ -1600,29 +1615,12 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
       break;
     }
     const Part w{cb, c0, c1, lane, 32};
-    if constexpr (NC > 0)
-    {
-      // per-point geometry read in the fused pass from device memory: ask L2
-      // now for this warp's share of the next tile's geometry (one
-      // contiguous run of its cells), a whole tile ahead of its use
-      const long long nt = tile + gridDim.x;
-      if (!staged && !p.host_io && nt < ntiles)
-      {
-        const long long g0 = (nt * cb + min(cb, wc0)) * (long long)Q3NC;
-        const long long g1 = min((nt * cb + min(cb, wc1)) * (long long)Q3NC,
-                                 p.ncells * (long long)Q3NC);
-        const char* gb = reinterpret_cast<const char*>(p.geo + g0);
-        const long long nbytes = (g1 - g0) * (long long)sizeof(ST);
-        for (long long off = (long long)lane * 128; off < nbytes; off += 32 * 128)
-          prefetch_l2(gb + off);
-      }
-    }
     Tile::forward(tv, su(s), sw, w);
     __syncwarp();
     if (staged)
       Tile::fused(tv, sw, w, sg(s), 0);
     else
-      Tile::fused(tv, sw, w, p.geo, tile * cb);
+      Tile::fused(tv, sw, w, p.geo, tile * cb, !p.host_io);
     __syncwarp();
     if (lane == 0)
       mbar_arrive(&empty[s]); // this warp is done with stage s's u and geometry

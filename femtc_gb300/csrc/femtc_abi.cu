@@ -1378,7 +1378,7 @@ int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
   {
     if (!general_supported(op, dtype, semantics, degree + 1, nquad))
       return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
-    // the general-degree kernel: one cell at a time per CTA
+    // the general-degree kernel: one cell per CTA of 256 threads
     if (lanes)
       *lanes = 1;
     if (cb)
@@ -1386,7 +1386,7 @@ int femtc_get_tile_config(int op, int dtype, int semantics, int degree,
     if (geo_staged)
       *geo_staged = 0;
     if (threads)
-      *threads = general_threads(op, dtype, degree + 1, nquad);
+      *threads = 256;
     return FEMTC_OK;
   }
   const TileCfg c = sel.second;

@@ -483,17 +483,18 @@ struct MmaTile
     pass2(p, w, pt);
   }
 
+  // (the last argument is the slab tiles' L2 prefetch hint; not used here)
   static __device__ __forceinline__ void fused(const TabView<float>& p,
                                                float* __restrict__ w, int ncb,
                                                const float* __restrict__ geo,
-                                               long long geo_cell0)
+                                               long long geo_cell0, bool = false)
   {
     fused(p, w, cta_part(ncb), geo, geo_cell0);
   }
   static __device__ __forceinline__ void fused(const TabView<float>& p,
                                                float* __restrict__ w, const Part& pt,
                                                const float* __restrict__ geo,
-                                               long long geo_cell0)
+                                               long long geo_cell0, bool = false)
   {
     pass3(p, w, pt, geo, geo_cell0);
     sync(pt);

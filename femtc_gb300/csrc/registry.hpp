@@ -56,7 +56,6 @@ void register_mma_bf16x3_stiffness(std::vector<CellVariant>&, std::vector<FaultR
 // General-degree kernels (cell_general.cu): runtime N and Q, mass and
 // stiffness, FP64 and FP32, for the (N, Q) the slab kernels do not cover.
 bool general_supported(int op, int dtype, int sem, int n, int q);
-int general_threads(int op, int dtype, int n, int q); // threads per CTA of its launch
 int launch_general(int op, int dtype, int sem, int n, int q, const void* tables, const void* u,
                    void* y, const void* geo, size_t ncells, cudaStream_t st);
 // fault words of the batch kernel families and of the diagnostic unit

@@ -679,13 +679,11 @@ struct SlabTile
   static_assert(!kAffine || SEM == SEM_EXACT, "affine forms: exact semantics only");
   static_assert(!EVOD || (SEM == SEM_EXACT && LANES == 1), "even-odd: exact, one lane per slab");
   // Streaming loop: work split by warps (stream_tiles_warp) where its extra
-  // live state costs no occupancy -- FP32, N <= 4, and the double-float
-  // tiles up to N = 5, whose CTA-wide loop waited at its barriers (few busy
-  // threads in the slab passes); the register-heavy FP64 tiles of higher
-  // degree, bound by the FP64 pipe, keep the CTA-wide loop (stream_tiles).
-  // The host's tile model (lane_efficiency) follows the same rule.
-  static constexpr bool kWarpSplit =
-      sizeof(T) == 4 || N <= 4 || (std::is_same<T, df64>::value && N <= 5);
+  // live state costs no occupancy -- FP32 and N <= 4; the register-heavy
+  // FP64 and double-float tiles of higher degree keep the CTA-wide loop
+  // (stream_tiles).  The host's tile model (lane_efficiency) follows the
+  // same rule.
+  static constexpr bool kWarpSplit = sizeof(T) == 4 || N <= 4;
   // TMA stages.  The warp-split loop takes any count; a third stage (two
   // tiles in flight ahead of the one computed) measured slower than two:
   // its shared memory costs more occupancy than the deeper prefetch gains.

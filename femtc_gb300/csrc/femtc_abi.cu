@@ -215,7 +215,7 @@ double lane_efficiency(const CellVariant& v, int cb, int nt)
     // slab kernels spread each pass over the CTA
     passes = 3; // slabs forward, pencils fused, slabs backward
     const double lanes = v.lanes;
-    const bool split = v.esize == 4 || v.n <= 4 || (v.dtype == FEMTC_F64E && v.n <= 5);
+    const bool split = v.esize == 4 || v.n <= 4;
     const double cw = split ? std::ceil((double)cb / (nt / 32)) : cb;
     np[0] = n * cw * lanes; wk[0] = q * n * (n + q) / lanes;
     np[1] = q * q * cw;     wk[1] = 2 * q * n;

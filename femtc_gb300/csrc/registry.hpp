@@ -37,7 +37,6 @@ void register_cell_f64eo_mass(std::vector<CellVariant>&, std::vector<FaultReader
 void register_cell_f64eo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32eo_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f32eo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
-void register_cell_f32eo_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64eeo_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64eeo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);

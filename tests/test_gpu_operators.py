@@ -256,6 +256,39 @@ def test_fp64_even_odd_and_plain_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
 
 
 @pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", range(1, 5))
+@pytest.mark.parametrize("dq", [0, 1, 2])
+def test_fp32_even_odd_vs_plain_and_oracle(femtc, orc, dev, op, P, dq):
+    """FP32 with one lane per slab (the form that has even-odd twins): the
+    even-odd kernels (the default for tabulated tables) against the plain
+    kernels and the oracle, on a ragged cell count and on several tiles."""
+    from femtc_gb300 import workloads as W
+    Q = P + 1 + dq
+    w = W.make_custom("eo1", op, P, Q, 1001, seed=13 * P + dq + 5 * op)
+    ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
+    t32 = w.tables.astype(np.float32)
+    for cb, nt in ((8, 256), (12, 128), (20, 64)):
+        try:
+            femtc.set_tile_config(op, femtc.F32, femtc.EXACT, P, Q, cb, 0, nt, 1)
+        except femtc.FemtcError:
+            continue
+        try:
+            assert femtc.even_odd_used(op, femtc.F32, femtc.EXACT, P, Q, t32)
+            y_eo = run_gpu(femtc, dev, op, femtc.F32, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+            femtc.set_even_odd(False)
+            try:
+                y_plain = run_gpu(femtc, dev, op, femtc.F32, femtc.EXACT, P, Q, w.tables, w.u,
+                                  w.geo)
+            finally:
+                femtc.set_even_odd(True)
+        finally:
+            femtc.set_tile_config(op, femtc.F32, femtc.EXACT, P, Q, 0, 0)
+        assert relerr(y_eo, ref) <= 2e-6
+        assert relerr(y_plain, ref) <= 2e-6
+        assert relerr(y_eo, y_plain) <= 2e-6
+
+
+@pytest.mark.parametrize("op", [0, 1])
 @pytest.mark.parametrize("P", [2, 4, 6])
 def test_fp64_exact_nonsymmetric_tables(femtc, orc, dev, op, P):
     """Tables without the symmetry (random) run the plain kernels: still

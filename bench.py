@@ -467,6 +467,14 @@ def run_batch(args, rank, world, dev, pg):
         res["speedup_vs_f64_plain"] = res["graph"]["gdofs"] / out["f64"]["separate"]["gdofs"]
         res["info"] = b.info()
         b.close()
+        if not args.no_batch_tune:
+            # the untuned plan: every mesh in one persistent kernel, one graph
+            # launch (the tuner's split plan above may hold several kernels)
+            b1 = F.Batch(dtype, meshes, tune=False)
+            ms = timed(lambda: b1.launch(stream))
+            res["one_kernel_graph"] = {"ms": ms, "gdofs": ndofs / ms / 1e6,
+                                       "hbm_gbs": nbytes / ms / 1e6}
+            b1.close()
         out[F.DTYPE_NAMES[dtype]] = res
     if F.device_status() != 0:
         raise RuntimeError("device fault word set during the batch benchmark")

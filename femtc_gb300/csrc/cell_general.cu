@@ -8,9 +8,8 @@
 // cell's slabs in registers with compile-time sizes and are built for
 // N <= 8; every other (N, Q) of mass and stiffness runs here.
 //
-// One CTA applies the operator to a group of cells at a time (grid-stride
-// over groups; several cells when they are small, so that every
-// contraction keeps the CTA's threads busy).  Each axis contraction is the reference's rotating product
+// One CTA applies the operator to one cell at a time (grid-stride over
+// cells).  Each axis contraction is the reference's rotating product
 // (src/linalg.hpp:101-182 as chained in src/mass.hpp:36-47): the input is
 // K x L with the contracted axis slowest, the output L x M with the new
 // axis fastest, so three contractions return a tensor to its axis order.
@@ -96,36 +95,31 @@ struct GenParams
   long long ncells;
   long long work_cta; // workspace elements per CTA
   int n, q, op, sem;
-  int cpb;         // cells a CTA applies the operator to at once
-  int buf;         // elements per work buffer of one cell
+  int buf;         // elements per work buffer
   int tab_elems;   // shared-memory elements of the tables (padded)
   // Phi(q,i) = tab[q + i*Q], then Gamma (stiffness)
   T tab[2 * kGenMaxQ * kGenMaxN];
 };
 
-// For each of nc cells: out[j*M + m] = sum_p A(m,p) in[p*L + j], with
-// A(m,p) = A[m*sm + p*sk], the cells' inputs `is` and outputs `os` elements
-// apart; over all threads of the CTA (no barrier inside).  With a second
-// table/input pair (B, in2, inputs also `is` apart) the sum also runs over
-// B(m,p) in2[p*L + j].  A work item is one cell's output column j and two
-// rows m, m+1 that share the input loads.
+// out[j*M + m] = sum_p A(m,p) in[p*L + j], A(m,p) = A[m*sm + p*sk], over all
+// threads of the CTA (no barrier inside); with a second table/input pair
+// (B, in2) the sum also runs over B(m,p) in2[p*L + j].  A work item is an
+// output column j and two rows m, m+1 that share the input loads.
 template <typename T, typename O>
-__device__ __forceinline__ void rot2(int nc, int K, int L, int M, const T* __restrict__ A,
+__device__ __forceinline__ void rot2(int K, int L, int M, const T* __restrict__ A,
                                      const T* __restrict__ B, int sm, int sk,
                                      const T* __restrict__ in1, const T* __restrict__ in2,
-                                     long long is, O* __restrict__ out, long long os)
+                                     O* __restrict__ out)
 {
   const int mp = (M + 1) >> 1; // row pairs
-  const int per = L * mp;
-  const int total = nc * per;
+  const int total = L * mp;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x)
   {
-    const int cc = idx / per, r = idx - cc * per;
-    const int j = r / mp, m = 2 * (r - j * mp);
+    const int j = idx / mp, m = 2 * (idx - j * mp);
     const bool two = m + 1 < M;
     const T* a = A + m * sm;
     const T* a1 = A + (two ? m + 1 : m) * sm;
-    const T* x = in1 + cc * is + j;
+    const T* x = in1 + j;
     // accumulators (double-float: renormalised once per sum, df64acc)
     acc_t<T> acc0 = acc_mul(a[0], x[0]), acc1 = acc_mul(a1[0], x[0]);
     for (int p = 1; p < K; ++p)
@@ -138,7 +132,7 @@ __device__ __forceinline__ void rot2(int nc, int K, int L, int M, const T* __res
     {
       const T* b = B + m * sm;
       const T* b1 = B + (two ? m + 1 : m) * sm;
-      const T* z = in2 + cc * is + j;
+      const T* z = in2 + j;
       for (int p = 0; p < K; ++p)
       {
         const T v = z[(long long)p * L];
@@ -146,19 +140,17 @@ __device__ __forceinline__ void rot2(int nc, int K, int L, int M, const T* __res
         acc1 = acc_fma(b1[p * sk], v, acc1);
       }
     }
-    O* o = out + cc * os;
-    o[j * M + m] = store_as<O>(acc_val(acc0));
+    out[j * M + m] = store_as<O>(acc_val(acc0));
     if (two)
-      o[j * M + m + 1] = store_as<O>(acc_val(acc1));
+      out[j * M + m + 1] = store_as<O>(acc_val(acc1));
   }
 }
 
 template <typename T, typename O>
-__device__ __forceinline__ void rot(int nc, int K, int L, int M, const T* __restrict__ A, int sm,
-                                    int sk, const T* __restrict__ in, long long is,
-                                    O* __restrict__ out, long long os)
+__device__ __forceinline__ void rot(int K, int L, int M, const T* __restrict__ A, int sm, int sk,
+                                    const T* __restrict__ in, O* __restrict__ out)
 {
-  rot2<T, O>(nc, K, L, M, A, (const T*)nullptr, sm, sk, in, (const T*)nullptr, is, out, os);
+  rot2<T, O>(K, L, M, A, (const T*)nullptr, sm, sk, in, (const T*)nullptr, out);
 }
 
 template <typename T>
@@ -176,128 +168,108 @@ __global__ void __launch_bounds__(kGenThreads)
   for (int i = threadIdx.x; i < (stiff ? 2 : 1) * nq; i += blockDim.x)
     tP[i] = p.tab[i];
   T* base = p.work ? p.work + blockIdx.x * p.work_cta : tP + p.tab_elems;
-  // buffer k of cell cc: base + (k * cpb + cc) * buf
-  const int C = p.cpb;
-  const long long bs = p.buf; // cell stride inside a buffer
   T* w0 = base;
-  T* w1 = base + 1LL * C * bs;
-  T* w2 = base + 2LL * C * bs;
-  T* w3 = base + 3LL * C * bs;
-  T* w4 = base + 4LL * C * bs;
-  T* w5 = base + 5LL * C * bs;
+  T* w1 = base + p.buf;
+  T* w2 = base + 2 * p.buf;
+  T* w3 = base + 3 * p.buf;
+  T* w4 = base + 4 * p.buf;
+  T* w5 = base + 5 * p.buf;
   // backward tables: exact A(i,q) = t[q + i*Q] (the transpose); reference
   // A(i,q) = t[i + q*Q] (the forward table reused, Q == N)
   const bool exact = p.sem == FEMTC_EXACT;
   const int bsm = exact ? q : 1, bsk = exact ? 1 : q;
-  const long long ngroups = (p.ncells + C - 1) / C;
   __syncthreads();
-  for (long long g = blockIdx.x; g < ngroups; g += gridDim.x)
+  for (long long c = blockIdx.x; c < p.ncells; c += gridDim.x)
   {
-    const long long c0 = g * C;
-    const int nc = (int)((p.ncells - c0) < C ? (p.ncells - c0) : C);
-    const ST* ug = p.u + c0 * n3;
-    ST* yc = p.y + c0 * n3;
+    const ST* ug = p.u + c * n3;
+    ST* yc = p.y + c * n3;
     // the forward contractions' input: u itself, or (double-float) u
     // converted once into a work buffer that is free until it is read
     const T* uc;
-    long long us;
     if constexpr (kConvert)
     {
       T* ub = stiff ? w5 : w2;
-      for (int i = threadIdx.x; i < nc * n3; i += blockDim.x)
-      {
-        const int cc = i / n3, r = i - cc * n3;
-        ub[cc * bs + r] = load_as<T>(ug[i]);
-      }
+      for (int i = threadIdx.x; i < n3; i += blockDim.x)
+        ub[i] = load_as<T>(ug[i]);
       __syncthreads();
       uc = ub;
-      us = bs;
     }
     else
-    {
       uc = ug;
-      us = n3;
-    }
     if (!stiff)
     {
       // src/mass.hpp:36-47
-      rot(nc, n, n * n, q, tP, 1, q, uc, us, w0, bs);
+      rot(n, n * n, q, tP, 1, q, uc, w0);
       __syncthreads();
-      rot(nc, n, n * q, q, tP, 1, q, w0, bs, w1, bs);
+      rot(n, n * q, q, tP, 1, q, w0, w1);
       __syncthreads();
-      rot(nc, n, q * q, q, tP, 1, q, w1, bs, w2, bs);
+      rot(n, q * q, q, tP, 1, q, w1, w2);
       __syncthreads();
-      const ST* dw = p.geo + c0 * q3;
-      for (int i = threadIdx.x; i < nc * q3; i += blockDim.x)
-      {
-        const int cc = i / q3, r = i - cc * q3;
-        w2[cc * bs + r] *= load_as<T>(dw[i]);
-      }
+      const ST* dw = p.geo + c * q3;
+      for (int i = threadIdx.x; i < q3; i += blockDim.x)
+        w2[i] *= load_as<T>(dw[i]);
       __syncthreads();
-      rot(nc, q, q * q, n, tP, bsm, bsk, w2, bs, w0, bs);
+      rot(q, q * q, n, tP, bsm, bsk, w2, w0);
       __syncthreads();
-      rot(nc, q, q * n, n, tP, bsm, bsk, w0, bs, w1, bs);
+      rot(q, q * n, n, tP, bsm, bsk, w0, w1);
       __syncthreads();
-      rot(nc, q, n * n, n, tP, bsm, bsk, w1, bs, yc, (long long)n3);
+      rot(q, n * n, n, tP, bsm, bsk, w1, yc);
       __syncthreads();
       continue;
     }
     // stiffness, src/stiffness.hpp:34-99: forward Phi_0 u and Gamma_0 u
     // shared by the three gradients
-    rot(nc, n, n * n, q, tP, 1, q, uc, us, w0, bs); // Phi_0 u
-    rot(nc, n, n * n, q, tD, 1, q, uc, us, w1, bs); // Gamma_0 u
+    rot(n, n * n, q, tP, 1, q, uc, w0); // Phi_0 u
+    rot(n, n * n, q, tD, 1, q, uc, w1); // Gamma_0 u
     __syncthreads();
-    rot(nc, n, n * q, q, tP, 1, q, w1, bs, w2, bs); // x: Phi_1
-    rot(nc, n, n * q, q, tD, 1, q, w0, bs, w3, bs); // y: Gamma_1
-    rot(nc, n, n * q, q, tP, 1, q, w0, bs, w4, bs); // z: Phi_1
+    rot(n, n * q, q, tP, 1, q, w1, w2); // x: Phi_1
+    rot(n, n * q, q, tD, 1, q, w0, w3); // y: Gamma_1
+    rot(n, n * q, q, tP, 1, q, w0, w4); // z: Phi_1
     __syncthreads();
-    rot(nc, n, q * q, q, tP, 1, q, w2, bs, w0, bs); // d/dx
-    rot(nc, n, q * q, q, tP, 1, q, w3, bs, w1, bs); // d/dy
+    rot(n, q * q, q, tP, 1, q, w2, w0); // d/dx
+    rot(n, q * q, q, tP, 1, q, w3, w1); // d/dy
     // d/dz: Gamma_2 (exact); the reference's W_z carries no derivative
     // (src/stiffness.hpp:76-77)
-    rot(nc, n, q * q, q, exact ? tD : tP, 1, q, w4, bs, w5, bs);
+    rot(n, q * q, q, exact ? tD : tP, 1, q, w4, w5);
     __syncthreads();
     // G transform per point, [zz,yz,xz,yy,xy,xx] (src/stiffness.hpp:14-29)
-    const ST* G = p.geo + c0 * q3 * 6;
-    for (int i = threadIdx.x; i < nc * q3; i += blockDim.x)
+    const ST* G = p.geo + c * q3 * 6;
+    for (int i = threadIdx.x; i < q3; i += blockDim.x)
     {
-      const int cc = i / q3, r = i - cc * q3;
-      const long long k = cc * bs + r;
-      const ST* gs = G + 6LL * i;
+      const ST* gs = G + 6 * i;
       const T g0 = load_as<T>(gs[0]), g1 = load_as<T>(gs[1]), g2 = load_as<T>(gs[2]);
-      const T a0 = w0[k], a1 = w1[k], a2 = w5[k];
+      const T a0 = w0[i], a1 = w1[i], a2 = w5[i];
       if (exact)
       {
         const T g3 = load_as<T>(gs[3]), g4 = load_as<T>(gs[4]), g5 = load_as<T>(gs[5]);
-        w0[k] = g5 * a0 + g4 * a1 + g2 * a2;
-        w1[k] = g4 * a0 + g3 * a1 + g1 * a2;
+        w0[i] = g5 * a0 + g4 * a1 + g2 * a2;
+        w1[i] = g4 * a0 + g3 * a1 + g1 * a2;
       }
-      w5[k] = g2 * a0 + g1 * a1 + g0 * a2;
+      w5[i] = g2 * a0 + g1 * a1 + g0 * a2;
     }
     __syncthreads();
     if (exact)
     {
       // backward: x, y and z chains; y and x meet before their common
       // axis-2 table Phi_2^T, z keeps Gamma_2^T
-      rot(nc, q, q * q, n, tD, bsm, bsk, w0, bs, w2, bs); // x: Gamma_0^T
-      rot(nc, q, q * q, n, tP, bsm, bsk, w1, bs, w3, bs); // y: Phi_0^T
-      rot(nc, q, q * q, n, tP, bsm, bsk, w5, bs, w4, bs); // z: Phi_0^T
+      rot(q, q * q, n, tD, bsm, bsk, w0, w2); // x: Gamma_0^T
+      rot(q, q * q, n, tP, bsm, bsk, w1, w3); // y: Phi_0^T
+      rot(q, q * q, n, tP, bsm, bsk, w5, w4); // z: Phi_0^T
       __syncthreads();
-      rot2(nc, q, q * n, n, tP, tD, bsm, bsk, w2, w3, bs, w0, bs); // x: Phi_1^T, y: Gamma_1^T
-      rot(nc, q, q * n, n, tP, bsm, bsk, w4, bs, w1, bs);          // z: Phi_1^T
+      rot2(q, q * n, n, tP, tD, bsm, bsk, w2, w3, w0); // x: Phi_1^T, y: Gamma_1^T
+      rot(q, q * n, n, tP, bsm, bsk, w4, w1);          // z: Phi_1^T
       __syncthreads();
-      // Phi_2^T (x + y) + Gamma_2^T z
-      rot2(nc, q, n * n, n, tP, tD, bsm, bsk, w0, w1, bs, yc, (long long)n3);
+      rot2(q, n * n, n, tP, tD, bsm, bsk, w0, w1, yc); // Phi_2^T (x + y) + Gamma_2^T z
     }
     else
     {
       // only the last backward chain (Phi, Phi, Gamma) survives in the
       // reference (src/stiffness.hpp:85,91,97)
-      rot(nc, q, q * q, n, tP, bsm, bsk, w5, bs, w2, bs);
+      rot(q, q * q, n, tP, bsm, bsk, w5, w2);
       __syncthreads();
-      rot(nc, q, q * n, n, tP, bsm, bsk, w2, bs, w3, bs);
+      rot(q, q * n, n, tP, bsm, bsk, w2, w3);
       __syncthreads();
-      rot(nc, q, n * n, n, tD, bsm, bsk, w3, bs, yc, (long long)n3);
+      rot(q, n * n, n, tD, bsm, bsk, w3, yc);
     }
     __syncthreads();
   }
@@ -352,24 +324,8 @@ int launch(int op, int sem, int n, int q, const typename gen_storage<T>::type* t
   const size_t tab_bytes = sizeof(T) * p.tab_elems;
   const size_t buf_bytes = sizeof(T) * (size_t)p.buf * nbuf;
   const void* fn = reinterpret_cast<const void*>(&general_cell_kernel<T>);
-  const size_t smem_max = (size_t)max_smem_optin();
-  const bool in_smem = tab_bytes + buf_bytes <= smem_max;
-  // cells per CTA group: enough that the smallest contraction (n^2 columns,
-  // row pairs of min(n, q) rows) gives every thread about two work items,
-  // within shared memory and at most a quarter of it per CTA (so that
-  // several CTAs share an SM and overlap one another's barriers)
-  int cpb = 1;
-  if (in_smem)
-  {
-    const int items = n * n * ((std::min(n, q) + 1) / 2);
-    const int want = (2 * kGenThreads + items - 1) / items;
-    const size_t quarter = smem_max / 4;
-    const size_t fit = quarter > tab_bytes ? std::max<size_t>(1, (quarter - tab_bytes) / buf_bytes)
-                                           : 1;
-    cpb = (int)std::max<size_t>(1, std::min<size_t>((size_t)want, fit));
-  }
-  p.cpb = cpb;
-  const size_t smem = in_smem ? tab_bytes + buf_bytes * cpb : tab_bytes;
+  const bool in_smem = tab_bytes + buf_bytes <= (size_t)max_smem_optin();
+  const size_t smem = in_smem ? tab_bytes + buf_bytes : tab_bytes;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess)
     return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
@@ -381,8 +337,7 @@ int launch(int op, int sem, int n, int q, const typename gen_storage<T>::type* t
   // FP32-pipe bound, not latency bound)
   if (!in_smem)
     per_sm = std::min(per_sm, 2);
-  const long long groups = ((long long)ncells + cpb - 1) / cpb;
-  const long long grid = std::min<long long>(groups, (long long)per_sm * sms());
+  const long long grid = std::min<long long>((long long)ncells, (long long)per_sm * sms());
   void* work = nullptr;
   if (!in_smem)
   {

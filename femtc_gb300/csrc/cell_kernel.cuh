@@ -55,6 +55,18 @@ enum Op : int
   OP_STIFFNESS_AFFINE = 4
 };
 
+// How a slab or tensor-core kernel reads the per-point geometry (the
+// tile configuration's geo_staged value).
+enum GeoMode : int
+{
+  GEO_PENCIL_L2 = 0, // read in the fused pass; each thread asks L2 for the
+                     // lines of its next pencil while it computes this one
+  GEO_STAGED = 1,    // staged through shared memory with the DOF slab (TMA)
+  GEO_TILE_L2 = 2    // read in the fused pass; at the start of a tile each
+                     // warp (CTA-wide loop: the CTA) asks L2 for the lines
+                     // of its cells' geometry
+};
+
 __host__ __device__ constexpr bool op_affine(int op)
 {
   return op == OP_MASS_AFFINE || op == OP_STIFFNESS_AFFINE;
@@ -128,6 +140,11 @@ __device__ __forceinline__ T shfl_xor(T v, int lane_mask)
   return __shfl_xor_sync(0xffffffffu, v, lane_mask);
 }
 
+// Table slots in a launch's parameter block: FP32 kernels carry pair
+// tables beside the 1D tables (SlabTileF2).
+template <typename T>
+constexpr int kTabSlots = std::is_same<T, float>::value ? 8 : 4;
+
 template <typename T>
 struct CellParams
 {
@@ -144,15 +161,19 @@ struct CellParams
   const ST* geo;     // [ncells][Q^3][geo_nc(op)] (mass: [ncells][Q^3])
   long long ncells;
   int cb;            // cells per tile, a multiple of 4
-  int geo_staged;    // 1: geometry slab staged by TMA, 0: read in the fused pass
+  int geo_staged;    // geometry per point (GEO_*): 1 staged by TMA; 0 and 2
+                     // read in the fused pass, 0 with each thread asking L2
+                     // for its next pencil's geometry, 2 with the tile's
+                     // geometry asked of L2 at the start of the tile
   int sq;            // slab kernels: stride of one i0 slab in the work buffers
   int sbc;           // slab kernels: stride of one cell in the work buffers
   int host_io;       // 1: u, geo, y are host memory read/written over the
                      // coherent host link with plain vector accesses (no TMA)
   // Phi(q,i) = tab[0][q + i*Q], Gamma = tab[1]; even-odd kernels: the
   // even-odd tables of Phi, Gamma (forward) and Phi^T, Gamma^T (backward)
-  // in tab[0..3] (see mv_eo)
-  T tab[4][kMaxQ * kMaxN];
+  // in tab[0..3] (see mv_eo); the paired FP32 kernels: their pair tables
+  // in tab[2..6] (see SlabTileF2)
+  alignas(16) T tab[kTabSlots<T>][kMaxQ * kMaxN];
 };
 
 // What the tile passes read besides the data: the two 1D tables (pointers
@@ -166,6 +187,8 @@ struct TabView
   int sq, sbc;
   const T* __restrict__ PB = nullptr; // even-odd kernels: Phi^T table
   const T* __restrict__ DB = nullptr; // even-odd kernels: Gamma^T table
+  const T* __restrict__ X = nullptr;  // slot 0 of the parameter block's
+                                      // tables (pair tables: SlabTileF2)
 };
 
 template <int N, int Q, int OP, int SEM>
@@ -416,7 +439,7 @@ __host__ __device__ inline CellLayout tile_layout(const CellParams<T>& p)
   using ST = storage_t<T>;
   const unsigned bu = (unsigned)p.cb * N * Tile::US * sizeof(ST);
   const unsigned bg =
-      (NC > 0 && p.geo_staged) ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(ST) : 0u;
+      (NC > 0 && p.geo_staged == GEO_STAGED) ? (unsigned)p.cb * Q * Q * Q * NC * sizeof(ST) : 0u;
   return CellLayout(bu, bg, Tile::work_bytes(p), Tile::kStages);
 }
 
@@ -428,7 +451,8 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   constexpr int US = Tile::US;
   extern __shared__ __align__(128) unsigned char smem[];
   const int cb = p.cb;
-  const bool staged = NC > 0 && p.geo_staged != 0; // affine forms: nothing to stage
+  const bool staged = NC > 0 && p.geo_staged == GEO_STAGED; // affine forms: nothing to stage
+  const bool tile_pf = NC > 0 && p.geo_staged == GEO_TILE_L2 && !p.host_io;
   const long long ntiles = (p.ncells + cb - 1) / cb;
   static_assert(Tile::kStages == 2, "the CTA-wide loop keeps two stages");
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
@@ -446,7 +470,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
   const unsigned bx = tma ? (unsigned)cb * N * US * sizeof(ST) : bu;
   const int lane = threadIdx.x & 31;
   const bool warp0 = threadIdx.x < 32;
-  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3]};
+  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3], p.tab[0]};
 
   if (threadIdx.x == 0)
   {
@@ -498,6 +522,9 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     const bool full = is_full(tile); // loaded and stored by TMA
     // cells in this tile (never more than the stage holds)
     const int ncb = (int)((p.ncells - tile * cb) < cb ? (p.ncells - tile * cb) : cb);
+    if (tile_pf) // the fused pass reads this tile's geometry from L2
+      prefetch_range_l2(p.geo + tile * cb * Q3NC, (size_t)ncb * Q3NC * sizeof(ST),
+                        threadIdx.x, blockDim.x);
     bool ok = true;
     if (full)
     {
@@ -551,7 +578,7 @@ __device__ __forceinline__ void stream_tiles(const CellParams<T>& p)
     if (staged)
       Tile::fused(tv, sw, ncb, sg(s), 0);
     else
-      Tile::fused(tv, sw, ncb, p.geo, tile * cb, !p.host_io);
+      Tile::fused(tv, sw, ncb, p.geo, tile * cb, !p.host_io && !tile_pf);
     if (warp0)
       bulk_wait_read0(); // the previous tile's stores have left sy
     __syncthreads();
@@ -1417,6 +1444,530 @@ struct SlabTile
   }
 };
 
+// ---------------------------------------------------------------------------
+// FP32 slab tile on packed FP32 pairs.  sm_100 and later issue
+// fma.rn.f32x2 (__ffma2_rn): one instruction carries two independent FMAs,
+// each rounded as fmaf.  An operand may be a register pair, one register
+// broadcast to both halves, or an entry (broadcast) or an aligned pair of
+// entries of the launch's parameter block, so table operands stay constant-
+// bank operands.  The FP32 slab kernels are bound by instruction issue; here
+// every contraction computes two outputs per instruction:
+//  * forward : stiffness: {a, g} = {Phi, Gamma}(q2, :) . x(i1, :) for one
+//    column q2, then {AA, BA}(q1) = Phi(q1, :) . {a, g} and AG for two q1 at
+//    once (GF); mass: two columns q2 at once, then Phi(q1, :) broadcast;
+//  * fused   : {d/dy, d/dz} = Phi . {x_g, x_b} and d/dx at two points at
+//    once (GF); back: {y, z} with Phi broadcast, x for two DOFs at once (GB);
+//    mass: two points (PF) and two DOFs (PB) at once;
+//  * backward: {x, z} with Phi broadcast, y for two DOFs at once (GB); axis
+//    2 accumulates two DOFs of a row at once ((Phi or Gamma)(q2, i2..i2+1)).
+// Two lanes per slab keep the lane's table columns in registers (pairs);
+// one lane reads them from the pair tables.  Host-built pair tables (float2,
+// padded with zeros to whole pairs) in the parameter block's table slots:
+//   PG (slots 2-3) {Phi(q,i), Gamma(q,i)}      at q*N + i       (stiffness)
+//   PF (slot 2)    {Phi(q,i), Phi(q+1,i)}      at (q/2)*N + i   (mass)
+//   GF (slot 4)    {Gamma(q,i), Gamma(q+1,i)}  at (q/2)*N + i   (stiffness)
+//   GB (slot 5)    {Gamma(q,i), Gamma(q,i+1)}  at (i/2)*Q + q   (stiffness)
+//   PB (slot 6)    {Phi(q,i), Phi(q,i+1)}      at (i/2)*Q + q
+// Exact semantics, per-point mass and stiffness; the tile's layout, strides
+// and staging are SlabTile's.  Sums run in the order of SlabTile's except
+// the backward x-gradient sum of a slab column, which adds its Gamma part
+// to its Phi part at the end.
+// ---------------------------------------------------------------------------
+constexpr int kTabSlot = kMaxQ * kMaxN; // floats per table slot
+constexpr int kSlotPG = 2, kSlotPF = 2, kSlotGF = 4, kSlotGB = 5, kSlotPB = 6;
+
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c)
+{
+  return __ffma2_rn(a, b, c);
+}
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b)
+{
+  return __fmul2_rn(a, b);
+}
+__device__ __forceinline__ float2 f2b(float x)
+{
+  return make_float2(x, x);
+}
+
+// The tiles that run on packed pairs (see SlabTileF2): FP32, exact
+// semantics, per-point mass and stiffness, N <= 5.  Above N = 5 the pair
+// accumulators and register tables outgrow the register file (measured at
+// N = 7: 255 registers against 204, and slower).
+template <typename T, int N, int OP, int SEM, bool EVOD>
+__host__ __device__ constexpr bool paired_tile()
+{
+  return std::is_same<T, float>::value && SEM == SEM_EXACT && !EVOD &&
+         (OP == OP_MASS || OP == OP_STIFFNESS) && N <= 5;
+}
+
+template <int N, int Q, int OP, int LANES, bool SLOTS>
+struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
+{
+  using B = SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>;
+  static constexpr int S = B::S, N2 = B::N2, Q2 = B::Q2, Q3 = Q * Q * Q;
+  static constexpr int SQ = B::SQ, SBC = B::SBC, QS = B::QS, UNR = B::UNR;
+  static constexpr bool kGrad = B::kGrad;
+  static_assert(OP == OP_MASS || OP == OP_STIFFNESS, "paired tile: per-point mass and stiffness");
+  static_assert(N <= 8 && 2 * Q * N <= 2 * kTabSlot, "pair tables sized for the slab degrees");
+  static constexpr int NP = (N + 1) / 2, QP = (Q + 1) / 2; // whole pairs (padded)
+  static constexpr int NF = N / 2;                           // full pairs of N
+  static_assert(N <= 5, "see paired_tile");
+  static constexpr int CP = (QS + 1) / 2; // mass, two lanes: column pairs of a lane
+
+  static __device__ __forceinline__ const float2* slot(const TabView<float>& p, int k)
+  {
+    return reinterpret_cast<const float2*>(p.X + k * kTabSlot);
+  }
+
+  static __device__ __forceinline__ void forward(const TabView<float>& p,
+                                                 const float* __restrict__ su,
+                                                 float* __restrict__ sw, const Part& w)
+  {
+    const float* __restrict__ P = p.P;
+    const float* __restrict__ D = p.D;
+    const float2* __restrict__ PG = slot(p, kSlotPG);
+    const float2* __restrict__ PF = slot(p, kSlotPF);
+    const float2* __restrict__ GF = slot(p, kSlotGF);
+    const int bstride = w.ncb * SBC;
+    // two lanes: this lane's columns q2 = ls, ls + S, ... as register pairs
+    // (stiffness {Phi, Gamma}(q2, i2); mass {Phi(q2, i2), Phi(q2 + S, i2)})
+    constexpr int PR = S > 1 ? (kGrad ? QS : CP) : 1;
+    float2 pc[PR][S > 1 ? N : 1];
+    if constexpr (S > 1)
+    {
+      const int ls = threadIdx.x % S;
+#pragma unroll
+      for (int j = 0; j < PR; ++j)
+#pragma unroll
+        for (int i2 = 0; i2 < N; ++i2)
+        {
+          if constexpr (kGrad)
+          {
+            const int q2 = ls + j * S;
+            pc[j][i2] = q2 < Q ? make_float2(P[q2 + i2 * Q], D[q2 + i2 * Q]) : f2b(0.f);
+          }
+          else
+          {
+            const int qa = ls + 2 * j * S, qb = qa + S;
+            pc[j][i2] = make_float2(qa < Q ? P[qa + i2 * Q] : 0.f, qb < Q ? P[qb + i2 * Q] : 0.f);
+          }
+        }
+    }
+    for (int ts = w.c0 * N * S + w.tid; ts < w.c1 * N * S; ts += w.nthr)
+    {
+      const int sl = ts / S, lane_s = ts - sl * S;
+      const int c = sl / N, i0 = sl - c * N;
+      float x[N2];
+      B::load_slab(su + sl * B::US, x);
+      float* b0 = sw + c * SBC + i0 * SQ;
+      if constexpr (kGrad)
+      {
+        float* b1 = b0 + bstride;
+        float* b2 = b1 + bstride;
+#pragma unroll UNR
+        for (int jq = 0; jq < QS; ++jq)
+        {
+          const int q2 = S > 1 ? lane_s + jq * S : jq;
+          if (S > 1 && q2 >= Q)
+            break;
+          auto tg = [&](int i2) -> float2 {
+            if constexpr (S > 1)
+              return pc[jq][i2];
+            else
+              return PG[q2 * N + i2];
+          };
+          float2 ag[N]; // {a, g}(i1): axis 2 with Phi and with Gamma
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+          {
+            float2 acc = f2mul(tg(0), f2b(x[i1 * N]));
+#pragma unroll
+            for (int i2 = 1; i2 < N; ++i2)
+              acc = f2fma(tg(i2), f2b(x[i1 * N + i2]), acc);
+            ag[i1] = acc;
+          }
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1) // {AA, BA} = Phi_1 {a, g}
+          {
+            float2 o = f2mul(f2b(P[q1]), ag[0]);
+#pragma unroll
+            for (int i1 = 1; i1 < N; ++i1)
+              o = f2fma(f2b(P[q1 + i1 * Q]), ag[i1], o);
+            b0[q1 * Q + q2] = o.x;
+            b2[q1 * Q + q2] = o.y;
+          }
+#pragma unroll
+          for (int h = 0; h < QP; ++h) // AG = Gamma_1 a, two q1 at once
+          {
+            float2 o = f2mul(GF[h * N], f2b(ag[0].x));
+#pragma unroll
+            for (int i1 = 1; i1 < N; ++i1)
+              o = f2fma(GF[h * N + i1], f2b(ag[i1].x), o);
+            b1[(2 * h) * Q + q2] = o.x;
+            if (2 * h + 1 < Q)
+              b1[(2 * h + 1) * Q + q2] = o.y;
+          }
+        }
+      }
+      else
+      {
+        constexpr int NCP = S > 1 ? CP : QP;
+#pragma unroll
+        for (int h = 0; h < NCP; ++h) // two columns qa, qb at once
+        {
+          const int qa = S > 1 ? lane_s + 2 * h * S : 2 * h;
+          const int qb = qa + (S > 1 ? S : 1);
+          if (S > 1 && qa >= Q)
+            break;
+          auto tp = [&](int i2) -> float2 {
+            if constexpr (S > 1)
+              return pc[h][i2];
+            else
+              return PF[h * N + i2];
+          };
+          float2 a[N];
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+          {
+            float2 acc = f2mul(tp(0), f2b(x[i1 * N]));
+#pragma unroll
+            for (int i2 = 1; i2 < N; ++i2)
+              acc = f2fma(tp(i2), f2b(x[i1 * N + i2]), acc);
+            a[i1] = acc;
+          }
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+          {
+            float2 o = f2mul(f2b(P[q1]), a[0]);
+#pragma unroll
+            for (int i1 = 1; i1 < N; ++i1)
+              o = f2fma(f2b(P[q1 + i1 * Q]), a[i1], o);
+            b0[q1 * Q + qa] = o.x;
+            if (qb < Q)
+              b0[q1 * Q + qb] = o.y;
+          }
+        }
+      }
+    }
+  }
+
+  static __device__ __forceinline__ void fused(const TabView<float>& p,
+                                               float* __restrict__ sw, const Part& w,
+                                               const float* __restrict__ geo,
+                                               long long geo_cell0, bool l2pf = false)
+  {
+    const float* __restrict__ P = p.P;
+    const float2* __restrict__ PF = slot(p, kSlotPF);
+    const float2* __restrict__ GF = slot(p, kSlotGF);
+    const float2* __restrict__ GB = slot(p, kSlotGB);
+    const float2* __restrict__ PB = slot(p, kSlotPB);
+    constexpr int NCG = geo_nc(OP);
+    constexpr int sq = SQ;
+    const int bstride = w.ncb * SBC;
+    for (int t = w.c0 * Q2 + w.tid; t < w.c1 * Q2; t += w.nthr)
+    {
+      const int c = t / Q2, r = t - c * Q2;
+      float* b0 = sw + c * SBC + r;
+      const int tn = t + w.nthr; // this thread's next pencil, if any
+      if (l2pf && tn < w.c1 * Q2)
+      {
+        const int cn = tn / Q2, rn = tn - cn * Q2;
+        const float* gn = geo + ((geo_cell0 + cn) * Q3 + rn) * NCG;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+          prefetch_l2(gn + (long long)q * Q2 * NCG);
+      }
+      if constexpr (OP == OP_MASS)
+      {
+        const float* dw = geo + (geo_cell0 + c) * Q3 + r;
+        float xk[N], v[2 * QP];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          xk[k] = b0[k * sq];
+#pragma unroll
+        for (int h = 0; h < QP; ++h) // two points at once
+        {
+          float2 s = f2mul(PF[h * N], f2b(xk[0]));
+#pragma unroll
+          for (int k = 1; k < N; ++k)
+            s = f2fma(PF[h * N + k], f2b(xk[k]), s);
+          v[2 * h] = s.x;
+          v[2 * h + 1] = s.y;
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+          v[q] *= dw[q * Q2];
+#pragma unroll
+        for (int h = 0; h < NP; ++h) // two DOFs at once
+        {
+          float2 o = f2mul(PB[h * Q], f2b(v[0]));
+#pragma unroll
+          for (int q = 1; q < Q; ++q)
+            o = f2fma(PB[h * Q + q], f2b(v[q]), o);
+          b0[(2 * h) * sq] = o.x;
+          if (2 * h + 1 < N)
+            b0[(2 * h + 1) * sq] = o.y;
+        }
+      }
+      else
+      {
+        float* b1 = b0 + bstride;
+        float* b2 = b1 + bstride;
+        const float* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG;
+        float xa[N];
+        float2 xgb[N]; // {AG, BA} along axis 0
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+        {
+          xa[k] = b0[k * sq];
+          xgb[k] = make_float2(b1[k * sq], b2[k * sq]);
+        }
+        float2 fyz[Q]; // {d/dy, d/dz}: Phi on axis 0
+        float fx[2 * QP];
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+        {
+          float2 s = f2mul(f2b(P[q]), xgb[0]);
+#pragma unroll
+          for (int k = 1; k < N; ++k)
+            s = f2fma(f2b(P[q + k * Q]), xgb[k], s);
+          fyz[q] = s;
+        }
+#pragma unroll
+        for (int h = 0; h < QP; ++h) // d/dx: Gamma on axis 0, two points at once
+        {
+          float2 s = f2mul(GF[h * N], f2b(xa[0]));
+#pragma unroll
+          for (int k = 1; k < N; ++k)
+            s = f2fma(GF[h * N + k], f2b(xa[k]), s);
+          fx[2 * h] = s.x;
+          fx[2 * h + 1] = s.y;
+        }
+        // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx]
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+        {
+          const float2* g2 = reinterpret_cast<const float2*>(G + (long long)q * Q2 * NCG);
+          const float2 g01 = g2[0], g23 = g2[1], g45 = g2[2];
+          const float zz = g01.x, yz = g01.y, xz = g23.x, yy = g23.y, xy = g45.x, xx = g45.y;
+          const float w0 = fx[q], w1 = fyz[q].x, w2 = fyz[q].y;
+          fx[q] = xx * w0 + xy * w1 + xz * w2;
+          fyz[q] = make_float2(xy * w0 + yy * w1 + yz * w2, xz * w0 + yz * w1 + zz * w2);
+        }
+#pragma unroll
+        for (int k = 0; k < N; ++k) // {y, z} back: Phi^T
+        {
+          float2 o = f2mul(f2b(P[k * Q]), fyz[0]);
+#pragma unroll
+          for (int q = 1; q < Q; ++q)
+            o = f2fma(f2b(P[q + k * Q]), fyz[q], o);
+          b1[k * sq] = o.x;
+          b2[k * sq] = o.y;
+        }
+#pragma unroll
+        for (int h = 0; h < NP; ++h) // x back: Gamma^T, two DOFs at once
+        {
+          float2 o = f2mul(GB[h * Q], f2b(fx[0]));
+#pragma unroll
+          for (int q = 1; q < Q; ++q)
+            o = f2fma(GB[h * Q + q], f2b(fx[q]), o);
+          b0[(2 * h) * sq] = o.x;
+          if (2 * h + 1 < N)
+            b0[(2 * h + 1) * sq] = o.y;
+        }
+      }
+    }
+  }
+
+  static __device__ __forceinline__ void backward(const TabView<float>& p,
+                                                  const float* __restrict__ sw,
+                                                  float* __restrict__ sy, const Part& w)
+  {
+    const float* __restrict__ P = p.P;
+    const float* __restrict__ D = p.D;
+    const float2* __restrict__ GB = slot(p, kSlotGB);
+    const float2* __restrict__ PB = slot(p, kSlotPB);
+    const int bstride = w.ncb * SBC;
+    const int base = w.c0 * N * S, cnt = (w.c1 - w.c0) * N * S;
+    const int rounds = (cnt + w.nthr - 1) / w.nthr;
+    // two lanes: axis-2 table pairs of this lane's columns, {Phi(q2, i2),
+    // Phi(q2, i2 + 1)} and the same of Gamma (odd N: the last entry alone)
+    constexpr int PR = S > 1 ? QS : 1;
+    constexpr int ODD = N & 1;
+    float2 tp[PR][S > 1 && NF > 0 ? NF : 1], tg[PR][S > 1 && kGrad && NF > 0 ? NF : 1];
+    float tpl[PR], tgl[PR];
+    if constexpr (S > 1)
+    {
+      const int ls = threadIdx.x % S;
+#pragma unroll
+      for (int jq = 0; jq < PR; ++jq)
+      {
+        const int q2 = ls + jq * S;
+        const bool ok = q2 < Q;
+#pragma unroll
+        for (int h = 0; h < NF; ++h)
+        {
+          const int i = 2 * h;
+          tp[jq][h] = ok ? make_float2(P[q2 + i * Q], P[q2 + (i + 1) * Q]) : f2b(0.f);
+          if constexpr (kGrad)
+            tg[jq][h] = ok ? make_float2(D[q2 + i * Q], D[q2 + (i + 1) * Q]) : f2b(0.f);
+        }
+        if constexpr (ODD)
+        {
+          tpl[jq] = ok ? P[q2 + (N - 1) * Q] : 0.f;
+          tgl[jq] = (ok && kGrad) ? D[q2 + (N - 1) * Q] : 0.f;
+        }
+      }
+    }
+    for (int r = 0; r < rounds; ++r)
+    {
+      const int idx = r * w.nthr + w.tid;
+      const bool live = idx < cnt;
+      const int ts = base + idx;
+      const int sl = live ? ts / S : 0, lane_s = ts - (ts / S) * S;
+      const int c = sl / N, i0 = sl - c * N;
+      const float* b0 = sw + c * SBC + i0 * SQ;
+      const float* b1 = b0 + bstride;
+      const float* b2 = b1 + bstride;
+      float2 ya[N][NF > 0 ? NF : 1]; // y(i1, 2h), y(i1, 2h + 1)
+      float yl[N];                    // odd N: y(i1, N - 1)
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+      {
+#pragma unroll
+        for (int h = 0; h < NF; ++h)
+          ya[i1][h] = f2b(0.f);
+        yl[i1] = 0.f;
+      }
+#pragma unroll UNR
+      for (int jq = 0; jq < QS; ++jq)
+      {
+        const int q2 = S > 1 ? lane_s + jq * S : jq;
+        if (!live || (S > 1 && q2 >= Q))
+          break;
+        auto ttp = [&](int h) -> float2 {
+          if constexpr (S > 1)
+            return tp[jq][h];
+          else
+            return PB[h * Q + q2];
+        };
+        auto ttpl = [&]() -> float {
+          if constexpr (S > 1)
+            return tpl[jq];
+          else
+            return P[q2 + (N - 1) * Q];
+        };
+        if constexpr (kGrad)
+        {
+          auto ttg = [&](int h) -> float2 {
+            if constexpr (S > 1)
+              return tg[jq][h];
+            else
+              return GB[h * Q + q2];
+          };
+          auto ttgl = [&]() -> float {
+            if constexpr (S > 1)
+              return tgl[jq];
+            else
+              return D[q2 + (N - 1) * Q];
+          };
+          float2 xz[Q];
+          float yv[Q];
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+          {
+            xz[q1] = make_float2(b0[q1 * Q + q2], b2[q1 * Q + q2]);
+            yv[q1] = b1[q1 * Q + q2];
+          }
+          float u1[2 * NP], u2[N];
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1) // axis 1 back, Phi^T: {x, z}
+          {
+            float2 s = f2mul(f2b(P[i1 * Q]), xz[0]);
+#pragma unroll
+            for (int q1 = 1; q1 < Q; ++q1)
+              s = f2fma(f2b(P[q1 + i1 * Q]), xz[q1], s);
+            u1[i1] = s.x;
+            u2[i1] = s.y;
+          }
+#pragma unroll
+          for (int h = 0; h < NP; ++h) // Gamma^T y, two DOFs at once
+          {
+            float2 s = f2mul(GB[h * Q], f2b(yv[0]));
+#pragma unroll
+            for (int q1 = 1; q1 < Q; ++q1)
+              s = f2fma(GB[h * Q + q1], f2b(yv[q1]), s);
+            u1[2 * h] += s.x;
+            if (2 * h + 1 < N)
+              u1[2 * h + 1] += s.y;
+          }
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1) // axis 2 back
+          {
+#pragma unroll
+            for (int h = 0; h < NF; ++h)
+            {
+              ya[i1][h] = f2fma(ttp(h), f2b(u1[i1]), ya[i1][h]);
+              ya[i1][h] = f2fma(ttg(h), f2b(u2[i1]), ya[i1][h]);
+            }
+            if constexpr (ODD)
+            {
+              yl[i1] = fmaf(ttpl(), u1[i1], yl[i1]);
+              yl[i1] = fmaf(ttgl(), u2[i1], yl[i1]);
+            }
+          }
+        }
+        else
+        {
+          float X[Q], u[2 * NP];
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+            X[q1] = b0[q1 * Q + q2];
+#pragma unroll
+          for (int h = 0; h < NP; ++h) // axis 1 back, two DOFs at once
+          {
+            float2 s = f2mul(PB[h * Q], f2b(X[0]));
+#pragma unroll
+            for (int q1 = 1; q1 < Q; ++q1)
+              s = f2fma(PB[h * Q + q1], f2b(X[q1]), s);
+            u[2 * h] = s.x;
+            u[2 * h + 1] = s.y;
+          }
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1) // axis 2 back
+          {
+#pragma unroll
+            for (int h = 0; h < NF; ++h)
+              ya[i1][h] = f2fma(ttp(h), f2b(u[i1]), ya[i1][h]);
+            if constexpr (ODD)
+              yl[i1] = fmaf(ttpl(), u[i1], yl[i1]);
+          }
+        }
+      }
+      float y[N2];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+#pragma unroll
+        for (int i2 = 0; i2 < N; ++i2)
+          y[i1 * N + i2] = (ODD && i2 == N - 1) ? yl[i1]
+                                                : ((i2 & 1) ? ya[i1][i2 / 2].y : ya[i1][i2 / 2].x);
+      if constexpr (S > 1)
+      {
+#pragma unroll
+        for (int k = 0; k < N2; ++k)
+        {
+#pragma unroll
+          for (int o = 1; o < S; o <<= 1)
+            y[k] += shfl_xor(y[k], o);
+        }
+      }
+      // the S lanes of a slab hold the same sums: the store is one write
+      if (live)
+        B::store_slab(sy + sl * B::US, y);
+    }
+  }
+};
+
 // One warp copies n elements between global (or host) memory and shared
 // memory: 16-byte vector accesses when both addresses and n allow, else
 // scalar; unrolled so that several requests are in flight per lane.
@@ -1496,7 +2047,8 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   constexpr int US = Tile::US;
   extern __shared__ __align__(128) unsigned char smem[];
   const int cb = p.cb;
-  const bool staged = NC > 0 && p.geo_staged != 0; // affine forms: nothing to stage
+  const bool staged = NC > 0 && p.geo_staged == GEO_STAGED; // affine forms: nothing to stage
+  const bool tile_pf = NC > 0 && p.geo_staged == GEO_TILE_L2 && !p.host_io;
   const long long ntiles = (p.ncells + cb - 1) / cb;
   const CellLayout L = tile_layout<T, Tile, N, Q, NC>(p);
   constexpr int NS = Tile::kStages;
@@ -1516,7 +2068,7 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   const int nwarps = blockDim.x >> 5;
   const int cw = (cb + nwarps - 1) / nwarps; // cells per warp
   const int wc0 = min(cb, warp * cw), wc1 = min(cb, wc0 + cw);
-  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3]};
+  const TabView<T> tv{p.tab[0], p.tab[1], p.sq, p.sbc, p.tab[2], p.tab[3], p.tab[0]};
 
   if (threadIdx.x == 0)
   {
@@ -1590,6 +2142,9 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
     }
     const int ncb = (int)((p.ncells - tile * cb) < cb ? (p.ncells - tile * cb) : cb);
     const int c0 = min(ncb, wc0), c1 = min(ncb, wc1);
+    if (tile_pf && c1 > c0) // this warp's fused pass reads its cells' geometry from L2
+      prefetch_range_l2(p.geo + (tile * cb + c0) * Q3NC, (size_t)(c1 - c0) * Q3NC * sizeof(ST),
+                        lane, 32);
     if (is_full(tile))
       ok = __shfl_sync(0xffffffffu, (int)mbar_wait(&full[s], (unsigned)(it / NS) & 1u), 0) && ok;
     else
@@ -1620,7 +2175,7 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
     if (staged)
       Tile::fused(tv, sw, w, sg(s), 0);
     else
-      Tile::fused(tv, sw, w, p.geo, tile * cb, !p.host_io);
+      Tile::fused(tv, sw, w, p.geo, tile * cb, !p.host_io && !tile_pf);
     __syncwarp();
     if (lane == 0)
       mbar_arrive(&empty[s]); // this warp is done with stage s's u and geometry
@@ -1632,11 +2187,23 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
   }
 }
 
+// CTAs of 256 threads an SM must be able to hold (the register budget):
+// the paired FP32 tiles keep to 128 registers per thread, as the scalar
+// ones do without the bound (unbounded they took 170 at N = 5 and ran
+// slower for the lost occupancy).
+template <typename T, int N, int OP, int SEM, bool EVOD>
+constexpr int cell_min_blocks()
+{
+  return paired_tile<T, N, OP, SEM, EVOD>() ? 2 : 1;
+}
+
 template <typename T, int N, int Q, int OP, int SEM, int LANES, bool EVOD = false>
-__global__ void __launch_bounds__(kCellThreads)
+__global__ void __launch_bounds__(kCellThreads, (cell_min_blocks<T, N, OP, SEM, EVOD>()))
     cell_kernel(const __grid_constant__ CellParams<T> p)
 {
-  using Tile = SlabTile<T, N, Q, OP, SEM, LANES, EVOD, true>;
+  using Tile = typename std::conditional<paired_tile<T, N, OP, SEM, EVOD>(),
+                                         SlabTileF2<N, Q, OP, LANES, true>,
+                                         SlabTile<T, N, Q, OP, SEM, LANES, EVOD, true>>::type;
   if constexpr (Tile::kWarpSplit)
     stream_tiles_warp<T, Tile, N, Q, geo_nc(OP)>(p);
   else

@@ -166,6 +166,22 @@ __device__ __forceinline__ void prefetch_l2(const void* p)
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// Hint: fetch the 128-byte lines of [p, p + bytes) into L2; worker `id` of
+// `n` takes lines id, id + n, ...  Every address asked for lies inside the
+// range (the first line is asked for at p itself).
+__device__ __forceinline__ void prefetch_range_l2(const void* p, size_t bytes, int id, int n)
+{
+  const uintptr_t b = reinterpret_cast<uintptr_t>(p), e = b + bytes;
+  const uintptr_t a = b & ~uintptr_t(127);
+  for (uintptr_t k = (uintptr_t)id;; k += (uintptr_t)n)
+  {
+    const uintptr_t l = k == 0 ? b : a + k * 128u;
+    if (l >= e)
+      break;
+    prefetch_l2(reinterpret_cast<const void*>(l));
+  }
+}
+
 __device__ __forceinline__ void record_fault(unsigned bits)
 {
   atomicOr(&g_fault_word, bits);

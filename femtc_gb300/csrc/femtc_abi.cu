@@ -485,6 +485,40 @@ int slot_tensor_maps(CUtensorMap* tu, CUtensorMap* ty, const void* u, void* y, i
   return box;
 }
 
+// Pair tables of the paired FP32 slab tiles (SlabTileF2) in the parameter
+// block's table slots 2..6, from Phi(q,i) = tables[q + i*Q] and Gamma(q,i)
+// = tables[Q*N + q + i*Q]; zeros pad each table to whole pairs.
+void fill_pair_tables(CellParams<float>& p, const float* tables, int op, int n, int q)
+{
+  const float* phi = tables;
+  const float* gam = tables + n * q;
+  float* base = &p.tab[0][0];
+  auto put = [&](int slot, int idx, float a, float b) {
+    base[slot * kTabSlot + 2 * idx] = a;
+    base[slot * kTabSlot + 2 * idx + 1] = b;
+  };
+  const int np = (n + 1) / 2, qp = (q + 1) / 2;
+  if (op == FEMTC_OP_STIFFNESS)
+  {
+    for (int k = 0; k < q; ++k)
+      for (int i = 0; i < n; ++i)
+        put(kSlotPG, k * n + i, phi[k + i * q], gam[k + i * q]);
+    for (int h = 0; h < qp; ++h)
+      for (int i = 0; i < n; ++i)
+        put(kSlotGF, h * n + i, gam[2 * h + i * q], 2 * h + 1 < q ? gam[2 * h + 1 + i * q] : 0.f);
+    for (int h = 0; h < np; ++h)
+      for (int k = 0; k < q; ++k)
+        put(kSlotGB, h * q + k, gam[k + 2 * h * q], 2 * h + 1 < n ? gam[k + (2 * h + 1) * q] : 0.f);
+  }
+  else
+    for (int h = 0; h < qp; ++h)
+      for (int i = 0; i < n; ++i)
+        put(kSlotPF, h * n + i, phi[2 * h + i * q], 2 * h + 1 < q ? phi[2 * h + 1 + i * q] : 0.f);
+  for (int h = 0; h < np; ++h)
+    for (int k = 0; k < q; ++k)
+      put(kSlotPB, h * q + k, phi[k + 2 * h * q], 2 * h + 1 < n ? phi[k + (2 * h + 1) * q] : 0.f);
+}
+
 // Launch-parameter form of a table entry (double-float splits FP64).
 template <typename T>
 T param_value(storage_t<T> x)
@@ -553,6 +587,10 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
         if (affine)
           p.tab[2 + t][i] = param_value<T>((ST)(tables[t * v.n * v.q + i] * wq[i % v.q]));
       }
+  if constexpr (std::is_same<T, float>::value)
+    if (v.slab && v.dtype == FEMTC_F32 && v.sem == FEMTC_EXACT && !v.eo && v.n <= 5 &&
+        (v.op == FEMTC_OP_MASS || v.op == FEMTC_OP_STIFFNESS))
+      fill_pair_tables(p, tables, v.op, v.n, v.q);
   const unsigned smem = smem_of(v, cfg);
   int blocks = 0;
   int rc = prepare(v.fn, smem, cfg.nt, &blocks);
@@ -1104,11 +1142,12 @@ int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
   if (threads % 32 != 0 || threads > kCellThreads)
     return fail(FEMTC_ERR_INVALID, "threads must be a multiple of 32, <= %d",
                 kCellThreads);
-  const unsigned need =
-      smem_of(*v, with_layout(*v, cb, geo_staged ? 1 : 0, threads));
+  if (geo_staged < GEO_PENCIL_L2 || geo_staged > GEO_TILE_L2)
+    return fail(FEMTC_ERR_INVALID, "geo_staged: 0 pencil prefetch, 1 staged, 2 tile prefetch");
+  const unsigned need = smem_of(*v, with_layout(*v, cb, geo_staged, threads));
   if (need > 227u * 1024u)
     return fail(FEMTC_ERR_INVALID, "tile needs %u B of shared memory", need);
-  g_tile_cfg[k] = TileChoice{cb, geo_staged ? 1 : 0, threads, v->lanes};
+  g_tile_cfg[k] = TileChoice{cb, geo_staged, threads, v->lanes};
   return FEMTC_OK;
 }
 
@@ -1219,7 +1258,10 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
     const CellVariant* lv = find_cell(op, dtype, semantics, degree + 1, nquad, lanes);
     if (!lv)
       continue;
-    for (int staged = 0; staged <= (geo_nc(op) > 0 ? 1 : 0); ++staged)
+    // geometry modes (GeoMode): per-pencil L2 prefetch, staged by TMA, and
+    // for device buffers the tile-start L2 prefetch
+    const int nmodes = geo_nc(op) > 0 ? (host_io ? 2 : 3) : 1;
+    for (int staged = 0; staged < nmodes; ++staged)
       for (int nt : {64, 128, 256})
       {
         std::vector<std::pair<double, TileCfg>> opts;
@@ -1234,11 +1276,11 @@ int autotune_impl(int op, int dtype, int semantics, int degree, int nquad,
                   [](const auto& a, const auto& b) { return a.first > b.first; });
         for (size_t i = 0; i < opts.size() && i < 4; ++i)
           cands.push_back({lv, opts[i].second});
-        // and the largest tiles that let 2 or 3 CTAs share an SM's shared
-        // memory (228 KB, 1 KB reserved per CTA): lane efficiency does not
-        // see the CTAs that overlap one another's barriers and copies
+        // and the largest tiles that let 2, 3 or 4 CTAs share an SM's
+        // shared memory (228 KB, 1 KB reserved per CTA): lane efficiency
+        // does not see the CTAs that overlap one another's barriers and copies
         std::vector<int> extra = wave_cb;
-        for (int k = 2; k <= 3; ++k)
+        for (int k = 2; k <= 4; ++k)
         {
           int best_c = 0;
           for (int c = 4; c <= 128; c += 4)

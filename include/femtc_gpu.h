@@ -226,8 +226,11 @@ int femtc_even_odd_used(int op, int dtype, int semantics, int degree, int nquad,
  * an error). */
 int femtc_set_host_path(int mode);
 
-/* Tile shape of a variant: cells per tile cb (multiple of 4), whether the
- * geometry slab is staged through shared memory by TMA, threads per CTA
+/* Tile shape of a variant: cells per tile cb (multiple of 4), how the
+ * per-point geometry is read (geo_staged: 0 in the quadrature-point pass,
+ * each thread asking L2 for its next pencil's geometry; 1 staged through
+ * shared memory by TMA with the DOF slab; 2 in the quadrature-point pass,
+ * the tile's geometry asked of L2 when the tile starts), threads per CTA
  * (multiple of 32, at most 256; <= 0 means 256) and, for the FP32 CUDA-core
  * kernels, lanes per slab (1 or 2; <= 0 means the built-in choice).
  * cb <= 0 restores the built-in heuristic.  The autotuner writes these. */

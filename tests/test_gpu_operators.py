@@ -121,7 +121,7 @@ def test_misaligned_pointer_rejected(femtc, dev):
 
 @pytest.mark.parametrize("dtype,lanes", [(0, 1), (1, 1), (1, 2), (2, 1)])
 @pytest.mark.parametrize("P", [3, 4])
-@pytest.mark.parametrize("staged", [0, 1])
+@pytest.mark.parametrize("staged", [0, 1, 2])
 @pytest.mark.parametrize("cb,nt", [(4, 64), (8, 256), (12, 128), (28, 96)])
 def test_tile_configs_agree(femtc, orc, dev, dtype, lanes, P, staged, cb, nt):
     from femtc_gb300 import workloads as W
@@ -137,6 +137,34 @@ def test_tile_configs_agree(femtc, orc, dev, dtype, lanes, P, staged, cb, nt):
         femtc.set_tile_config(femtc.STIFFNESS, dtype, femtc.EXACT, P, Q, 0, 0)
     tol = {0: 1e-12, 1: 2e-6, 2: 1e-6}[dtype]
     assert relerr(y, orc.stiffness(orc.EXACT, P, Q, w.tables, w.u, w.geo)) <= tol
+
+
+@pytest.mark.parametrize("lanes", [1, 2])
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", range(1, 8))
+@pytest.mark.parametrize("dq", [0, 1, 2])
+def test_fp32_pairs_every_lane_count_vs_oracle(femtc, orc, dev, lanes, op, P, dq):
+    """The FP32 exact kernels (contractions on packed FP32 pairs where the
+    tile allows) with one and two lanes per slab, tile-start geometry
+    prefetch, tabulated and random (non-symmetric) tables."""
+    from femtc_gb300 import workloads as W
+    Q = P + 1 + dq
+    if not femtc.supported(op, 1, femtc.EXACT, P, Q):
+        pytest.skip("variant not built")
+    try:
+        femtc.set_tile_config(op, 1, femtc.EXACT, P, Q, 8, 2, 128, lanes)
+    except femtc.FemtcError:
+        pytest.skip("tile does not fit in shared memory")
+    try:
+        w = W.make_custom("t", op, P, Q, 203, seed=7 * P + dq + 50 * op + lanes)
+        y = run_gpu(femtc, dev, op, 1, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+        assert relerr(y, oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)) <= 2e-6
+        rng = np.random.default_rng(P + 10 * dq)
+        tabs = rng.uniform(-1.0, 1.0, size=w.tables.shape)
+        y = run_gpu(femtc, dev, op, 1, femtc.EXACT, P, Q, tabs, w.u, w.geo)
+        assert relerr(y, oracle_apply(orc, op, orc.EXACT, P, Q, tabs, w.u, w.geo)) <= 2e-6
+    finally:
+        femtc.set_tile_config(op, 1, femtc.EXACT, P, Q, 0, 0)
 
 
 @pytest.mark.parametrize("dtype", [0, 1, 3])

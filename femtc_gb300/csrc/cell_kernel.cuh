@@ -1714,6 +1714,17 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
         float* b1 = b0 + bstride;
         float* b2 = b1 + bstride;
         const float* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG;
+        // the pencil's geometry, [zz,yz,xz,yy,xy,xx] per point as three
+        // pairs, asked for before the contractions that precede its use
+        float2 gq[Q][3];
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+        {
+          const float2* g2 = reinterpret_cast<const float2*>(G + (long long)q * Q2 * NCG);
+          gq[q][0] = g2[0];
+          gq[q][1] = g2[1];
+          gq[q][2] = g2[2];
+        }
         float xa[N];
         float2 xgb[N]; // {AG, BA} along axis 0
 #pragma unroll
@@ -1747,9 +1758,8 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
 #pragma unroll
         for (int q = 0; q < Q; ++q)
         {
-          const float2* g2 = reinterpret_cast<const float2*>(G + (long long)q * Q2 * NCG);
-          const float2 g01 = g2[0], g23 = g2[1], g45 = g2[2];
-          const float zz = g01.x, yz = g01.y, xz = g23.x, yy = g23.y, xy = g45.x, xx = g45.y;
+          const float zz = gq[q][0].x, yz = gq[q][0].y, xz = gq[q][1].x, yy = gq[q][1].y,
+                      xy = gq[q][2].x, xx = gq[q][2].y;
           const float w0 = fx[q], w1 = fyz[q].x, w2 = fyz[q].y;
           fx[q] = xx * w0 + xy * w1 + xz * w2;
           fyz[q] = make_float2(xy * w0 + yy * w1 + yz * w2, xz * w0 + yz * w1 + zz * w2);

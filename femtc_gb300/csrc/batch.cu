@@ -488,6 +488,71 @@ int launch_eager(femtc_batch* b, cudaStream_t st)
   return e == cudaSuccess ? FEMTC_OK : aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
 }
 
+// Split plan: the batch kernels and single-mesh launches write disjoint
+// outputs, so the graph runs them on parallel branches, each launch on the
+// branch with the least estimated work so far (longest first): small
+// launches overlap one another and the tails of the large ones instead of
+// running one after another on a mostly idle GPU.
+int capture_branches(femtc_batch* b)
+{
+  constexpr int K = femtc_batch::kBranches;
+  for (int k = 0; k < K; ++k)
+  {
+    if (!b->side[k] && cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking) != cudaSuccess)
+      return aux_fail(FEMTC_ERR_CUDA, "batch: stream creation failed");
+    if (!b->join_ev[k] &&
+        cudaEventCreateWithFlags(&b->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return aux_fail(FEMTC_ERR_CUDA, "batch: event creation failed");
+  }
+  if (!b->fork_ev && cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+    return aux_fail(FEMTC_ERR_CUDA, "batch: event creation failed");
+  struct Task
+  {
+    double cost;
+    int part, solo;
+  };
+  std::vector<Task> tasks;
+  for (size_t i = 0; i < b->parts.size(); ++i)
+  {
+    double c = 0.0;
+    for (const auto& it : b->parts[i]->items)
+      c += cell_cost(it.op, it.degree + 1) * (double)it.ncells;
+    tasks.push_back({c, (int)i, -1});
+  }
+  for (size_t j = 0; j < b->solo.size(); ++j)
+  {
+    const femtc_batch_item& it = b->solo[j].it;
+    tasks.push_back({cell_cost(it.op, it.degree + 1) * (double)it.ncells, -1, (int)j});
+  }
+  std::stable_sort(tasks.begin(), tasks.end(),
+                   [](const Task& x, const Task& y) { return x.cost > y.cost; });
+  cudaEventRecord(b->fork_ev, b->cap_stream);
+  for (int k = 0; k < K; ++k)
+    cudaStreamWaitEvent(b->side[k], b->fork_ev, 0);
+  double load[K] = {};
+  int rc = FEMTC_OK;
+  for (const Task& t : tasks)
+  {
+    int k = 0;
+    for (int j = 1; j < K; ++j)
+      if (load[j] < load[k])
+        k = j;
+    load[k] += t.cost;
+    rc = t.part >= 0 ? launch_eager(b->parts[t.part].get(), b->side[k])
+                     : launch_solo(b->dtype, b->solo[t.solo], b->side[k]);
+    if (rc != FEMTC_OK)
+      break;
+  }
+  // every branch joins the capture stream, also after an error, so that
+  // the capture can end
+  for (int k = 0; k < K; ++k)
+  {
+    cudaEventRecord(b->join_ev[k], b->side[k]);
+    cudaStreamWaitEvent(b->cap_stream, b->join_ev[k], 0);
+  }
+  return rc;
+}
+
 int capture(femtc_batch* b)
 {
   if (b->exec)
@@ -502,7 +567,8 @@ int capture(femtc_batch* b)
   cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess)
     return aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
-  int rc = launch_eager(b, b->cap_stream);
+  int rc = (!b->parts.empty() || !b->solo.empty()) ? capture_branches(b)
+                                                   : launch_eager(b, b->cap_stream);
   e = cudaStreamEndCapture(b->cap_stream, &b->graph);
   if (rc != FEMTC_OK)
     return rc;

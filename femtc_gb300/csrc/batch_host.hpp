@@ -34,6 +34,12 @@ struct femtc_batch
   cudaStream_t cap_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // Split plan: the graph's parallel branches (streams and the fork and
+  // join events of the capture)
+  static constexpr int kBranches = 4;
+  cudaStream_t side[kBranches] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[kBranches] = {};
   // Split plan (chosen by the tuner when faster than one kernel over the
   // whole mix): one batch kernel per variant whose meshes run best
   // persistent, and single-mesh launches for the variants whose meshes are
@@ -49,6 +55,15 @@ struct femtc_batch
       cudaGraphDestroy(graph);
     if (cap_stream)
       cudaStreamDestroy(cap_stream);
+    for (int k = 0; k < kBranches; ++k)
+    {
+      if (side[k])
+        cudaStreamDestroy(side[k]);
+      if (join_ev[k])
+        cudaEventDestroy(join_ev[k]);
+    }
+    if (fork_ev)
+      cudaEventDestroy(fork_ev);
     if (d_tiles)
       cudaFree(d_tiles);
     if (d_items)

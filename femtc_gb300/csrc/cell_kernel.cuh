@@ -1490,14 +1490,14 @@ __device__ __forceinline__ float2 f2b(float x)
 }
 
 // The tiles that run on packed pairs (see SlabTileF2): FP32, exact
-// semantics, per-point mass and stiffness, N <= 5.  Above N = 5 the pair
+// semantics, per-point mass, stiffness and Helmholtz, N <= 5.  Above N = 5 the pair
 // accumulators and register tables outgrow the register file (measured at
 // N = 7: 255 registers against 204, and slower).
 template <typename T, int N, int OP, int SEM, bool EVOD>
 __host__ __device__ constexpr bool paired_tile()
 {
   return std::is_same<T, float>::value && SEM == SEM_EXACT && !EVOD &&
-         (OP == OP_MASS || OP == OP_STIFFNESS) && N <= 5;
+         (OP == OP_MASS || OP == OP_STIFFNESS || OP == OP_HELMHOLTZ) && N <= 5;
 }
 
 template <int N, int Q, int OP, int LANES, bool SLOTS>
@@ -1507,7 +1507,8 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
   static constexpr int S = B::S, N2 = B::N2, Q2 = B::Q2, Q3 = Q * Q * Q;
   static constexpr int SQ = B::SQ, SBC = B::SBC, QS = B::QS, UNR = B::UNR;
   static constexpr bool kGrad = B::kGrad;
-  static_assert(OP == OP_MASS || OP == OP_STIFFNESS, "paired tile: per-point mass and stiffness");
+  static_assert(OP == OP_MASS || OP == OP_STIFFNESS || OP == OP_HELMHOLTZ,
+                "paired tile: per-point mass, stiffness and Helmholtz");
   static_assert(N <= 8 && 2 * Q * N <= 2 * kTabSlot, "pair tables sized for the slab degrees");
   static constexpr int NP = (N + 1) / 2, QP = (Q + 1) / 2; // whole pairs (padded)
   static constexpr int NF = N / 2;                           // full pairs of N
@@ -1657,6 +1658,7 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
                                                long long geo_cell0, bool l2pf = false)
   {
     const float* __restrict__ P = p.P;
+    const float2* __restrict__ PG = slot(p, kSlotPG);
     const float2* __restrict__ PF = slot(p, kSlotPF);
     const float2* __restrict__ GF = slot(p, kSlotGF);
     const float2* __restrict__ GB = slot(p, kSlotGB);
@@ -1716,14 +1718,15 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
         const float* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG;
         // the pencil's geometry, [zz,yz,xz,yy,xy,xx] per point as three
         // pairs, asked for before the contractions that precede its use
-        float2 gq[Q][3];
+        constexpr int NG2 = NCG / 2; // pairs per point (Helmholtz: the mass factor too)
+        float2 gq[Q][NG2];
 #pragma unroll
         for (int q = 0; q < Q; ++q)
         {
           const float2* g2 = reinterpret_cast<const float2*>(G + (long long)q * Q2 * NCG);
-          gq[q][0] = g2[0];
-          gq[q][1] = g2[1];
-          gq[q][2] = g2[2];
+#pragma unroll
+          for (int j = 0; j < NG2; ++j)
+            gq[q][j] = g2[j];
         }
         float xa[N];
         float2 xgb[N]; // {AG, BA} along axis 0
@@ -1735,6 +1738,7 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
         }
         float2 fyz[Q]; // {d/dy, d/dz}: Phi on axis 0
         float fx[2 * QP];
+        float2 fmx[OP == OP_HELMHOLTZ ? Q : 1]; // Helmholtz: {u, d/dx} at the points
 #pragma unroll
         for (int q = 0; q < Q; ++q)
         {
@@ -1744,15 +1748,31 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
             s = f2fma(f2b(P[q + k * Q]), xgb[k], s);
           fyz[q] = s;
         }
-#pragma unroll
-        for (int h = 0; h < QP; ++h) // d/dx: Gamma on axis 0, two points at once
+        if constexpr (OP == OP_HELMHOLTZ)
         {
-          float2 s = f2mul(GF[h * N], f2b(xa[0]));
 #pragma unroll
-          for (int k = 1; k < N; ++k)
-            s = f2fma(GF[h * N + k], f2b(xa[k]), s);
-          fx[2 * h] = s.x;
-          fx[2 * h + 1] = s.y;
+          for (int q = 0; q < Q; ++q) // {Phi, Gamma} on axis 0: the value and d/dx
+          {
+            float2 s = f2mul(PG[q * N], f2b(xa[0]));
+#pragma unroll
+            for (int k = 1; k < N; ++k)
+              s = f2fma(PG[q * N + k], f2b(xa[k]), s);
+            fmx[q] = s;
+            fx[q] = s.y;
+          }
+        }
+        else
+        {
+#pragma unroll
+          for (int h = 0; h < QP; ++h) // d/dx: Gamma on axis 0, two points at once
+          {
+            float2 s = f2mul(GF[h * N], f2b(xa[0]));
+#pragma unroll
+            for (int k = 1; k < N; ++k)
+              s = f2fma(GF[h * N + k], f2b(xa[k]), s);
+            fx[2 * h] = s.x;
+            fx[2 * h + 1] = s.y;
+          }
         }
         // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx]
 #pragma unroll
@@ -1763,6 +1783,8 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
           const float w0 = fx[q], w1 = fyz[q].x, w2 = fyz[q].y;
           fx[q] = xx * w0 + xy * w1 + xz * w2;
           fyz[q] = make_float2(xy * w0 + yy * w1 + yz * w2, xz * w0 + yz * w1 + zz * w2);
+          if constexpr (OP == OP_HELMHOLTZ) // the mass term: alpha detJ w u
+            fmx[q] = make_float2(fmx[q].x * gq[q][3].x, fx[q]);
         }
 #pragma unroll
         for (int k = 0; k < N; ++k) // {y, z} back: Phi^T
@@ -1774,16 +1796,31 @@ struct SlabTileF2 : SlabTile<float, N, Q, OP, SEM_EXACT, LANES, false, SLOTS>
           b1[k * sq] = o.x;
           b2[k * sq] = o.y;
         }
-#pragma unroll
-        for (int h = 0; h < NP; ++h) // x back: Gamma^T, two DOFs at once
+        if constexpr (OP == OP_HELMHOLTZ)
         {
-          float2 o = f2mul(GB[h * Q], f2b(fx[0]));
 #pragma unroll
-          for (int q = 1; q < Q; ++q)
-            o = f2fma(GB[h * Q + q], f2b(fx[q]), o);
-          b0[(2 * h) * sq] = o.x;
-          if (2 * h + 1 < N)
-            b0[(2 * h + 1) * sq] = o.y;
+          for (int k = 0; k < N; ++k) // Phi^T (m u) + Gamma^T x, the halves summed
+          {
+            float2 o = f2mul(PG[k], fmx[0]);
+#pragma unroll
+            for (int q = 1; q < Q; ++q)
+              o = f2fma(PG[q * N + k], fmx[q], o);
+            b0[k * sq] = o.x + o.y;
+          }
+        }
+        else
+        {
+#pragma unroll
+          for (int h = 0; h < NP; ++h) // x back: Gamma^T, two DOFs at once
+          {
+            float2 o = f2mul(GB[h * Q], f2b(fx[0]));
+#pragma unroll
+            for (int q = 1; q < Q; ++q)
+              o = f2fma(GB[h * Q + q], f2b(fx[q]), o);
+            b0[(2 * h) * sq] = o.x;
+            if (2 * h + 1 < N)
+              b0[(2 * h + 1) * sq] = o.y;
+          }
         }
       }
     }

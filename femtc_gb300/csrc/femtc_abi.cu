@@ -498,7 +498,7 @@ void fill_pair_tables(CellParams<float>& p, const float* tables, int op, int n, 
     base[slot * kTabSlot + 2 * idx + 1] = b;
   };
   const int np = (n + 1) / 2, qp = (q + 1) / 2;
-  if (op == FEMTC_OP_STIFFNESS)
+  if (op != FEMTC_OP_MASS) // stiffness and Helmholtz
   {
     for (int k = 0; k < q; ++k)
       for (int i = 0; i < n; ++i)
@@ -589,7 +589,7 @@ int launch_cell(const CellVariant& v, const TileCfg& cfg,
       }
   if constexpr (std::is_same<T, float>::value)
     if (v.slab && v.dtype == FEMTC_F32 && v.sem == FEMTC_EXACT && !v.eo && v.n <= 5 &&
-        (v.op == FEMTC_OP_MASS || v.op == FEMTC_OP_STIFFNESS))
+        (v.op == FEMTC_OP_MASS || v.op == FEMTC_OP_STIFFNESS || v.op == FEMTC_OP_HELMHOLTZ))
       fill_pair_tables(p, tables, v.op, v.n, v.q);
   const unsigned smem = smem_of(v, cfg);
   int blocks = 0;

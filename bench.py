@@ -520,7 +520,28 @@ def run_serve(args, rank, world, dev, pg):
         b = rng.standard_normal((n, (P + 1) ** 3))
         probs.append(F.Problem(P, P + 2, J, b, alpha=1.0, beta=sigma, rtol=1e-8,
                                inner_dtype=inner))
-    arrivals = np.cumsum(rng.exponential(1.0 / 2000.0, size=nreq))
+    # optional operator applications in the same stream (FP64, mass or
+    # stiffness, the solves' degree and cell distributions)
+    apps = []
+    for _ in range(args.serve_applications):
+        P = int(rng.integers(2, 8))
+        n = int(round(10 ** rng.uniform(3.0, np.log10(2e5))))
+        if args.cells:
+            n = max(1, n * args.cells // 200000)
+        op = int(rng.integers(0, 2))
+        w = W.make_custom("serve_apply", op, P, P + 2, n, seed=int(rng.integers(1 << 30)))
+        apps.append(F.Application(op, F.F64, F.EXACT, P, P + 2, w.tables, w.u, w.geo))
+    kinds = [0] * nreq + [1] * len(apps)
+    rng.shuffle(kinds)
+    reqs, ia, ip = [], 0, 0
+    for k in kinds:
+        if k:
+            reqs.append(apps[ia])
+            ia += 1
+        else:
+            reqs.append(probs[ip])
+            ip += 1
+    arrivals = np.cumsum(rng.exponential(1.0 / 2000.0, size=len(reqs)))
     free = torch_free_bytes(dev)
     budget = int(min(free * 0.6, 120e9))
     # warm the kernels used by the solves (setup, outside the timed region)
@@ -530,23 +551,25 @@ def run_serve(args, rank, world, dev, pg):
         F.solve(wp)
     policy = F.SERVE_FIFO if args.serve_policy == "fifo" else F.SERVE_SHORTEST_FIRST
     srv = F.Server(budget, max_active=8, policy=policy)
-    tickets = [None] * nreq
+    tickets = [None] * len(reqs)
     t0 = time.perf_counter()
 
     def feeder():
-        for i, p in enumerate(probs):
+        for i, p in enumerate(reqs):
             delay = arrivals[i] - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
-            tickets[i] = srv.submit(p)
+            tickets[i] = srv.submit_apply(p) if kinds[i] else srv.submit(p)
 
     th = threading.Thread(target=feeder)
     th.start()
     th.join()
-    results = [srv.wait(t, 3600.0) for t in tickets]
+    all_results = [srv.wait(t, 3600.0) for t in tickets]
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
+    results = [r for r, k in zip(all_results, kinds) if not k]
+    app_results = [r for r, k in zip(all_results, kinds) if k]
     lat = np.array([r["t_done_ms"] - r["t_submit_ms"] for r in results])
     svc = np.array([r["ms_total"] for r in results])
     ok = sum(1 for r in results if r["rc"] == 0)
@@ -572,6 +595,17 @@ def run_serve(args, rank, world, dev, pg):
             "mean_outer_iters": float(np.mean([r["outer_iters"] for r in results])),
             "mean_inner_iters": float(np.mean([r["inner_iters"] for r in results])),
         }
+        if app_results:
+            alat = np.array([r["t_done_ms"] - r["t_submit_ms"] for r in app_results])
+            line["applications"] = {
+                "requests": len(app_results), "dtype": "f64",
+                "completed_ok": sum(1 for r in app_results if r["rc"] == 0),
+                "p50_ms": float(np.percentile(alat, 50)),
+                "p99_ms": float(np.percentile(alat, 99)),
+                "service_p50_ms": float(np.percentile([r["ms_total"] for r in app_results], 50)),
+                "dofs": int(sum(a.u.size for a in apps)),
+            }
+            line["config"]["operator_applications"] = len(app_results)
         return line
     return None
 
@@ -925,6 +959,9 @@ def main():
                          f"reported under 'extra' (default with the default workload: "
                          f"{EXTRA_DEFAULT}; 'none' for none)")
     ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
+    ap.add_argument("--serve-applications", type=int, default=0,
+                    help="serve: operator applications (FP64 mass or stiffness) mixed into "
+                         "the request stream, reported under 'applications'")
     ap.add_argument("--serve-policy", default="shortest", choices=["shortest", "fifo"],
                     help="serve: admission order (shortest estimated work first, with aging; "
                          "or arrival order)")

@@ -5,7 +5,7 @@ drop-in header include/femtc_gpu/operators.hpp.  This package builds it
 in-tree and binds it with ctypes for Python callers, tests and benchmarks.
 """
 from ._lib import (  # noqa: F401
-    BATCH_SPLIT, BATCH_TUNE, Batch, NOT_CONVERGED, SERVE_FIFO, SERVE_SHORTEST_FIRST, batch_apply_static, Problem, Server, solve, solve_bytes,
+    Application, BATCH_SPLIT, BATCH_TUNE, Batch, NOT_CONVERGED, SERVE_FIFO, SERVE_SHORTEST_FIRST, batch_apply_static, Problem, Server, solve, solve_bytes,
     BF16X3, EXACT, F16X2, F32, F64, F64E, FP64_STORAGE, HELMHOLTZ, MASS, REFERENCE, STIFFNESS,
     DTYPE_NAMES, helmholtz_apply, helmholtz_geometry,
     MASS_AFFINE, STIFFNESS_AFFINE, affine_apply, affine_tables,

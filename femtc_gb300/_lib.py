@@ -88,6 +88,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "femtc_solve": ([vp, vp, vp], c_int),
         "femtc_server_create": ([c_size, c_int, ctypes.POINTER(vp)], c_int),
         "femtc_server_submit": ([vp, vp, ctypes.POINTER(ctypes.c_longlong)], c_int),
+        "femtc_server_submit_apply": ([vp, vp, ctypes.POINTER(ctypes.c_longlong)], c_int),
         "femtc_server_wait": ([vp, ctypes.c_longlong, ctypes.c_double, vp], c_int),
         "femtc_server_get_stats": ([vp, vp], c_int),
         "femtc_server_set_policy": ([vp, c_int], c_int),
@@ -475,6 +476,29 @@ class SolveResult(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ApplyRequest(ctypes.Structure):
+    """femtc_apply_request (include/femtc_gpu.h)."""
+    _fields_ = [("op", ctypes.c_int), ("dtype", ctypes.c_int), ("semantics", ctypes.c_int),
+                ("degree", ctypes.c_int), ("nquad", ctypes.c_int), ("ncells", ctypes.c_size_t),
+                ("tables", ctypes.c_void_p), ("u", ctypes.c_void_p), ("geo", ctypes.c_void_p),
+                ("y", ctypes.c_void_p)]
+
+
+class Application:
+    """Host data of one served operator application y = A u (keeps the
+    arrays alive; y holds the result once the request completes)."""
+
+    def __init__(self, op, dtype, semantics, degree, nquad, tables, u, geo):
+        st = np.float64 if dtype in FP64_STORAGE else np.float32
+        self.tables = host_tables(tables, dtype)
+        self.u = np.ascontiguousarray(u, dtype=st)
+        self.geo = np.ascontiguousarray(geo, dtype=st)
+        self.y = np.zeros_like(self.u)
+        self.req = ApplyRequest(op, dtype, semantics, degree, nquad, self.u.shape[0],
+                                self.tables.ctypes.data, self.u.ctypes.data,
+                                self.geo.ctypes.data, self.y.ctypes.data)
+
+
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
                 ("rejected", ctypes.c_longlong), ("queued", ctypes.c_longlong),
@@ -529,6 +553,14 @@ class Server:
         t = ctypes.c_longlong()
         check(load().femtc_server_submit(self.handle, ctypes.byref(problem.req), ctypes.byref(t)))
         self._live[t.value] = problem
+        return t.value
+
+    def submit_apply(self, app: "Application") -> int:
+        """Queue an operator application (femtc_server_submit_apply)."""
+        t = ctypes.c_longlong()
+        check(load().femtc_server_submit_apply(self.handle, ctypes.byref(app.req),
+                                               ctypes.byref(t)))
+        self._live[t.value] = app
         return t.value
 
     def wait(self, ticket: int, timeout_s: float = 600.0) -> dict:

@@ -1,8 +1,8 @@
 // Serving loop (femtc_server_* in femtc_gpu.h): continuous batching of
-// matrix-free solves.  A fixed pool of host workers, each with its own CUDA
-// stream, takes requests from one queue as soon as a worker is free and the
-// request fits in the HBM budget next to the solves already running;
-// running solves overlap on the device.  The next request is the oldest
+// matrix-free solves and operator applications.  A fixed pool of host
+// workers, each with its own CUDA stream, takes requests from one queue as
+// soon as a worker is free and the request fits in the HBM budget next to
+// the requests already running; running requests overlap on the device.  The next request is the oldest
 // (FIFO) or, by default, the one with the least estimated work less the
 // time it has waited (shortest first with aging: no request waits longer
 // than the estimate of the work admitted ahead of it).  Timestamps (submit,
@@ -12,6 +12,7 @@
 
 #include <chrono>
 #include <condition_variable>
+#include <cstring>
 #include <cuda_runtime.h>
 #include <deque>
 #include <map>
@@ -28,6 +29,65 @@ size_t solve_bytes(int degree, int nquad, size_t ncells);
 
 using namespace femtc;
 
+namespace
+{
+size_t storage_bytes(int dtype)
+{
+  return (dtype == FEMTC_F64 || dtype == FEMTC_F64E) ? 8 : 4;
+}
+
+size_t apply_geo_values(const femtc_apply_request& rq)
+{
+  const size_t q = (size_t)rq.nquad;
+  return (rq.op == FEMTC_OP_MASS ? 1 : 6) * q * q * q;
+}
+
+// Device bytes of an operator application: its copies of u, the geometry
+// and y (each allocation rounded up to 256 bytes).
+size_t apply_bytes(const femtc_apply_request& rq)
+{
+  const size_t n = (size_t)rq.degree + 1;
+  const size_t es = storage_bytes(rq.dtype);
+  return rq.ncells * es * (2 * n * n * n + apply_geo_values(rq)) + 3 * 256;
+}
+
+// One operator application on `st`: device copies in, the operator, y back
+// to the host; waits for the stream.
+int apply_on_stream(const femtc_apply_request& rq, const void* tables, femtc_solve_result* res,
+                    cudaStream_t st)
+{
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t n = (size_t)rq.degree + 1, es = storage_bytes(rq.dtype);
+  const size_t bu = rq.ncells * n * n * n * es, bg = rq.ncells * apply_geo_values(rq) * es;
+  void *du = nullptr, *dg = nullptr, *dy = nullptr;
+  int rc = FEMTC_OK;
+  if (cudaMallocAsync(&du, bu, st) != cudaSuccess || cudaMallocAsync(&dg, bg, st) != cudaSuccess ||
+      cudaMallocAsync(&dy, bu, st) != cudaSuccess)
+    rc = aux_fail(FEMTC_ERR_NOMEM, "server: operator application: device allocation failed");
+  if (rc == FEMTC_OK && (cudaMemcpyAsync(du, rq.u, bu, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                         cudaMemcpyAsync(dg, rq.geo, bg, cudaMemcpyHostToDevice, st) != cudaSuccess))
+    rc = aux_fail(FEMTC_ERR_CUDA, "server: operator application: copy in failed");
+  if (rc == FEMTC_OK)
+    rc = rq.op == FEMTC_OP_MASS
+             ? femtc_mass_apply(rq.dtype, rq.semantics, rq.degree, rq.nquad, tables, du, dy, dg,
+                                rq.ncells, st)
+             : femtc_stiffness_apply(rq.dtype, rq.semantics, rq.degree, rq.nquad, tables, du, dy,
+                                     dg, rq.ncells, st);
+  if (rc == FEMTC_OK && cudaMemcpyAsync(rq.y, dy, bu, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    rc = aux_fail(FEMTC_ERR_CUDA, "server: operator application: copy out failed");
+  for (void* p : {du, dg, dy})
+    if (p)
+      cudaFreeAsync(p, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (rc == FEMTC_OK && e != cudaSuccess)
+    rc = aux_fail(FEMTC_ERR_CUDA, cudaGetErrorString(e));
+  res->status = rc;
+  res->ms_total =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+} // namespace
+
 struct femtc_server
 {
   using clk = std::chrono::steady_clock;
@@ -38,6 +98,9 @@ struct femtc_server
     size_t bytes;
     double t_submit;
     double est_ms; // estimated work, in the units of the aging clock
+    bool apply = false;          // an operator application (ap) instead of a solve
+    femtc_apply_request ap{};
+    std::vector<unsigned char> tab; // the application's tables, copied at submit
   };
   // Estimated work of a solve: DOFs times the operator's work per DOF
   // (sum factorisation: about N flops per DOF per contraction), scaled to
@@ -106,7 +169,7 @@ struct femtc_server
         cv_work.wait(lk, [&] { return stop || (idx = pick()) >= 0; });
         if (stop)
           break;
-        job = queue[(size_t)idx];
+        job = std::move(queue[(size_t)idx]);
         queue.erase(queue.begin() + idx);
         in_use += job.bytes;
         peak = std::max(peak, in_use);
@@ -115,10 +178,12 @@ struct femtc_server
       }
       femtc_solve_result res{};
       const double t_admit = now_ms();
-      if (st)
-        solve_on_stream(&job.rq, &res, st);
-      else
+      if (!st)
         res.status = aux_fail(FEMTC_ERR_CUDA, "server: no CUDA stream on this worker");
+      else if (job.apply)
+        apply_on_stream(job.ap, job.tab.data(), &res, st);
+      else
+        solve_on_stream(&job.rq, &res, st);
       {
         std::lock_guard<std::mutex> lk(m);
         res.t_submit_ms = job.t_submit;
@@ -169,6 +234,44 @@ int femtc_server_submit(femtc_server* s, const femtc_solve_request* rq, long lon
   *ticket = s->next_ticket++;
   s->queue.push_back(
       femtc_server::Job{*ticket, *rq, bytes, s->now_ms(), femtc_server::estimate_ms(*rq)});
+  ++s->submitted;
+  s->cv_work.notify_one();
+  return FEMTC_OK;
+}
+
+int femtc_server_submit_apply(femtc_server* s, const femtc_apply_request* rq, long long* ticket)
+{
+  if (!s || !rq || !ticket)
+    return aux_fail(FEMTC_ERR_INVALID, "server: null argument");
+  if ((rq->op != FEMTC_OP_MASS && rq->op != FEMTC_OP_STIFFNESS) || rq->ncells == 0 ||
+      !rq->tables || !rq->u || !rq->geo || !rq->y)
+    return aux_fail(FEMTC_ERR_INVALID, "server: malformed operator application");
+  if (femtc_supported(rq->op, rq->dtype, rq->semantics, rq->degree, rq->nquad) != 1)
+    return aux_fail(FEMTC_ERR_UNSUPPORTED, "server: operator application: variant not built");
+  const size_t bytes = apply_bytes(*rq);
+  const size_t ntab = 2 * (size_t)(rq->degree + 1) * (size_t)rq->nquad * storage_bytes(rq->dtype);
+  femtc_server::Job job{};
+  job.rq = femtc_solve_request{};
+  job.bytes = bytes;
+  job.apply = true;
+  job.ap = *rq;
+  job.tab.resize(ntab);
+  std::memcpy(job.tab.data(), rq->tables, ntab);
+  // about one operator application of a solve's several hundred
+  femtc_solve_request like{};
+  like.degree = rq->degree;
+  like.ncells = rq->ncells;
+  job.est_ms = femtc_server::estimate_ms(like) / 400.0;
+  std::lock_guard<std::mutex> lk(s->m);
+  if (bytes > s->budget)
+  {
+    ++s->rejected;
+    return aux_fail(FEMTC_ERR_NOMEM, "server: request exceeds the HBM budget");
+  }
+  *ticket = s->next_ticket++;
+  job.ticket = *ticket;
+  job.t_submit = s->now_ms();
+  s->queue.push_back(std::move(job));
   ++s->submitted;
   s->cv_work.notify_one();
   return FEMTC_OK;

@@ -430,9 +430,10 @@ size_t femtc_solve_bytes(int degree, int nquad, size_t ncells);
 int femtc_solve(const femtc_solve_request* rq, femtc_solve_result* res,
                 void* stream);
 
-/* Serving loop with continuous batching: up to max_active solves run at
- * once, each on its own stream and host worker, so their kernels overlap on
- * the device; queued requests are admitted as slots and HBM budget free up
+/* Serving loop with continuous batching: up to max_active requests (solves
+ * and operator applications) run at once, each on its own stream and host
+ * worker, so their kernels overlap on the device; queued requests are
+ * admitted as slots and HBM budget free up
  * (a request larger than the whole budget is rejected at submit with
  * FEMTC_ERR_NOMEM).  Request memory (J, b, x) must stay valid until the
  * request's result has been collected. */
@@ -453,10 +454,35 @@ typedef struct
   int max_concurrent;  /* most solves seen running at once */
 } femtc_server_stats;
 
+/* An operator application served beside the solves: y = A u on host
+ * buffers, as femtc_mass_apply_host / femtc_stiffness_apply_host with the
+ * same arguments.  The worker that admits it allocates device copies of u,
+ * the geometry and y on its stream, copies in, applies the operator and
+ * copies y back; those device bytes count against the HBM budget.  The
+ * tables are copied at submit; u, geo and y must stay valid until the
+ * result has been collected. */
+typedef struct
+{
+  int op;              /* FEMTC_OP_MASS or FEMTC_OP_STIFFNESS */
+  int dtype;           /* any dtype of femtc_*_apply */
+  int semantics;       /* FEMTC_EXACT or FEMTC_REFERENCE */
+  int degree, nquad;
+  size_t ncells;
+  const void* tables;  /* host, as femtc_*_apply */
+  const void* u;       /* host [ncells][N^3] (FP64 for F64/F64E, else FP32) */
+  const void* geo;     /* host geometry, as femtc_*_apply */
+  void* y;             /* host [ncells][N^3], written on completion */
+} femtc_apply_request;
+
 int femtc_server_create(size_t hbm_budget_bytes, int max_active,
                         femtc_server** out);
 int femtc_server_submit(femtc_server* s, const femtc_solve_request* rq,
                         long long* ticket);
+/* Queues an operator application (result through femtc_server_wait: status,
+ * ms_total and the timestamps; the iteration counts are 0).  No reference
+ * counterpart: the reference applies operators in its own benchmark loop. */
+int femtc_server_submit_apply(femtc_server* s, const femtc_apply_request* rq,
+                              long long* ticket);
 /* Waits up to timeout_s seconds for the ticket's result (FEMTC_ERR_TIMEOUT
  * otherwise); returns the solve's status and fills *res. */
 int femtc_server_wait(femtc_server* s, long long ticket, double timeout_s,

@@ -75,6 +75,54 @@ def test_server_mix_equals_alone(femtc, dev):
         assert r["t_submit_ms"] <= r["t_admit_ms"] <= r["t_done_ms"]
 
 
+def test_server_applications_and_solves_mixed(femtc, orc, dev):
+    """Operator applications served beside solves: each application's y is
+    the same bits as the same application run alone through the host-buffer
+    entry point, and matches the oracle; the solves are unchanged."""
+    from femtc_gb300 import workloads as W
+    probs = [problem(femtc, P, P + 2, n, s, seed=20 + i)[0]
+             for i, (P, n, s) in enumerate([(3, 200, 1.0), (5, 60, 0.5), (2, 400, 4.0)])]
+    alone_x = []
+    for p in probs:
+        femtc.solve(p)
+        alone_x.append(p.x.copy())
+        p.x[:] = 0.0
+    apps, alone_y, refs = [], [], []
+    for i, (op, dt, P, Q, n) in enumerate([(1, femtc.F64, 4, 6, 700), (0, femtc.F32, 3, 5, 900),
+                                           (1, femtc.F64E, 3, 5, 300), (1, femtc.F32, 7, 9, 50),
+                                           (0, femtc.F64, 9, 10, 20)]):
+        w = W.make_custom("a", op, P, Q, n, seed=40 + i)
+        a = femtc.Application(op, dt, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+        y = np.empty_like(a.u)
+        femtc.apply_host(op, dt, femtc.EXACT, P, Q, w.tables, a.u, y, a.geo, n)
+        apps.append(a)
+        alone_y.append(y)
+        fn = orc.mass if op == 0 else orc.stiffness
+        refs.append((fn(orc.EXACT, P, Q, w.tables, w.u, w.geo), 2e-6 if dt == femtc.F32 else 1e-12))
+    srv = femtc.Server(hbm_budget_bytes=8 << 30, max_active=4)
+    try:
+        tickets = []
+        for k in range(max(len(probs), len(apps))):
+            if k < len(apps):
+                tickets.append(srv.submit_apply(apps[k]))
+            if k < len(probs):
+                tickets.append(srv.submit(probs[k]))
+        results = [srv.wait(t, 300.0) for t in tickets]
+        st = srv.stats()
+    finally:
+        srv.close()
+    assert all(r["rc"] == 0 for r in results)
+    assert st["completed"] == len(tickets)
+    for a, y, (ref, tol) in zip(apps, alone_y, refs):
+        assert np.array_equal(a.y, y)  # same bits alone and in the mix
+        err = np.abs(a.y - ref).max() / np.abs(ref).max()
+        assert err <= tol, err
+    for p, x in zip(probs, alone_x):
+        assert np.array_equal(p.x, x)
+    for r in results:
+        assert r["t_submit_ms"] <= r["t_admit_ms"] <= r["t_done_ms"]
+
+
 def test_server_budget_serialises(femtc, dev):
     p1 = problem(femtc, 3, 5, 400, 1.0, seed=1)[0]
     p2 = problem(femtc, 3, 5, 400, 1.0, seed=2)[0]

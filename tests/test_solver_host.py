@@ -34,6 +34,33 @@ def test_server_rejects_over_budget_and_malformed(femtc):
         s.close()
 
 
+def test_server_rejects_bad_applications(femtc):
+    s = femtc.Server(hbm_budget_bytes=1 << 20, max_active=1)  # 1 MiB budget
+    try:
+        t = np.zeros(2 * 4 * 5)
+        big = femtc.Application(1, femtc.F64, femtc.EXACT, 3, 5, t, np.zeros((5000, 64)),
+                                np.zeros((5000, 125 * 6)))
+        with pytest.raises(femtc.FemtcError) as e:
+            s.submit_apply(big)
+        assert e.value.status == -4  # FEMTC_ERR_NOMEM: over the whole budget
+        bad = femtc.Application(1, femtc.F64, femtc.EXACT, 3, 5, t, np.zeros((1, 64)),
+                                np.zeros((1, 125 * 6)))
+        bad.req.op = 7
+        with pytest.raises(femtc.FemtcError) as e:
+            s.submit_apply(bad)
+        assert e.value.status == -1  # FEMTC_ERR_INVALID
+        bad.req.op = 1
+        bad.req.dtype = femtc.F16X2
+        bad.req.degree = 12
+        with pytest.raises(femtc.FemtcError) as e:
+            s.submit_apply(bad)  # the tensor-core forms stop at degree 7
+        assert e.value.status == -2  # FEMTC_ERR_UNSUPPORTED
+        st = s.stats()
+        assert st["rejected"] == 1 and st["submitted"] == 0
+    finally:
+        s.close()
+
+
 def test_server_policy_validation(femtc):
     s = femtc.Server(hbm_budget_bytes=1 << 20, max_active=1, policy=femtc.SERVE_FIFO)
     try:

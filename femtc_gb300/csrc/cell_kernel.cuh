@@ -714,7 +714,11 @@ struct SlabTile
   // TMA stages.  The warp-split loop takes any count; a third stage (two
   // tiles in flight ahead of the one computed) measured slower than two:
   // its shared memory costs more occupancy than the deeper prefetch gains.
-  static constexpr int kStages = 2;
+  // FP32 tiles from N = 6 keep one: their work buffers make the shared
+  // memory set the CTAs per SM, and the stage is refilled as soon as every
+  // warp is done with it (after the quadrature-point pass), behind the
+  // backward pass.
+  static constexpr int kStages = (sizeof(T) == 4 && N >= 6) ? 1 : 2;
   static constexpr int NBUF =
       (op_base(OP) == OP_MASS) ? 1 : ((SEM == SEM_EXACT) ? 3 : 2);
   // work-buffer strides (slab_strides.hpp): compile-time, so every work
@@ -2173,8 +2177,9 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
     const int s = it % NS;
     const long long ahead = tile + (long long)(NS - 1) * gridDim.x;
     // warp 0 refills stage (it-1) % NS with the tile NS-1 iterations ahead
-    // once every warp has released it
-    if (warp == 0 && ahead < ntiles && is_full(ahead))
+    // once every warp has released it (one stage: only the first tile here,
+    // the others after the previous tile's quadrature-point pass)
+    if (warp == 0 && ahead < ntiles && is_full(ahead) && (NS > 1 || it == 0))
     {
       if (it >= 1)
         ok = __shfl_sync(0xffffffffu,
@@ -2226,6 +2231,21 @@ __device__ __forceinline__ void stream_tiles_warp(const CellParams<T>& p)
     __syncwarp();
     if (lane == 0)
       mbar_arrive(&empty[s]); // this warp is done with stage s's u and geometry
+    if constexpr (NS == 1)
+    {
+      // one stage: warp 0 refills it with this CTA's next tile as soon as
+      // every warp is done with it, while the backward passes run
+      const long long nxt = tile + gridDim.x;
+      if (warp == 0 && ok && nxt < ntiles && is_full(nxt))
+      {
+        ok = __shfl_sync(0xffffffffu, (int)mbar_wait(&empty[0], (unsigned)it & 1u), 0) && ok;
+        if (ok)
+        {
+          issue(nxt, 0);
+          issued = it + 1;
+        }
+      }
+    }
     Tile::backward(tv, sw, sy, w);
     __syncwarp();
     // this warp's outputs: coalesced stores from the output slabs

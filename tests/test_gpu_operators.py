@@ -167,6 +167,30 @@ def test_fp32_pairs_every_lane_count_vs_oracle(femtc, orc, dev, lanes, op, P, dq
         femtc.set_tile_config(op, 1, femtc.EXACT, P, Q, 0, 0)
 
 
+@pytest.mark.parametrize("dtype,op,P,lanes,ncells", [
+    (1, 1, 4, 2, 20001), (1, 1, 4, 2, 33333), (1, 0, 3, 1, 20001), (1, 0, 3, 1, 33335),
+    (1, 1, 6, 1, 9001), (0, 0, 3, 1, 20003), (0, 1, 3, 1, 33333), (1, 1, 2, 2, 47779)])
+def test_several_rounds_and_ragged_tail_vs_oracle(femtc, orc, dev, dtype, op, P, lanes, ncells):
+    """Meshes of several rounds of tiles over every CTA plus a ragged last
+    tile (8-cell tiles, 64-thread CTAs, so that a round is a few thousand
+    cells), through both TMA stage counts.  Every cell is checked against
+    the oracle, and none is left unwritten (y starts as NaN)."""
+    from femtc_gb300 import workloads as W
+    Q = P + 2
+    try:
+        femtc.set_tile_config(op, dtype, femtc.EXACT, P, Q, 8, 0, 64, lanes)
+    except femtc.FemtcError:
+        pytest.skip("tile does not fit in shared memory")
+    try:
+        w = W.make_custom("t", op, P, Q, ncells, seed=ncells % 97 + P)
+        y = run_gpu(femtc, dev, op, dtype, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+    finally:
+        femtc.set_tile_config(op, dtype, femtc.EXACT, P, Q, 0, 0)
+    assert np.isfinite(y).all()
+    ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
+    assert relerr(y, ref) <= TOL[dtype]
+
+
 @pytest.mark.parametrize("dtype", [0, 1, 3])
 def test_autotune_then_parity(femtc, orc, dev, dtype):
     import torch

@@ -86,6 +86,24 @@ def test_tile_config_roundtrip(femtc, tmp_path):
     femtc.set_tile_config(femtc.MASS, femtc.F64, femtc.EXACT, 3, 5, 0, 0)
 
 
+def test_geometry_modes_of_a_tile(femtc, tmp_path):
+    """Geometry modes 0 (per-pencil L2 prefetch), 1 (TMA-staged) and 2
+    (tile-start L2 prefetch) are accepted, stored and saved; others rejected."""
+    key = (femtc.STIFFNESS, femtc.F32, femtc.EXACT, 4, 6)
+    for mode in (0, 1, 2):
+        femtc.set_tile_config(*key, 12, mode, 128, 2)
+        assert femtc.get_tile_config(*key) == (12, mode, 128, 2)
+    db = str(tmp_path / "tiles.txt")
+    femtc.tile_db_save(db)
+    femtc.set_tile_config(*key, 0, 0)
+    assert femtc.tile_db_load(db) >= 1
+    assert femtc.get_tile_config(*key) == (12, 2, 128, 2)
+    for bad in (3, -1):
+        with pytest.raises(femtc.FemtcError):
+            femtc.set_tile_config(*key, 12, bad, 128, 2)
+    femtc.set_tile_config(*key, 0, 0)
+
+
 def test_fp32_lanes_choice_roundtrip(femtc):
     key = (femtc.STIFFNESS, femtc.F32, femtc.EXACT, 4, 6)
     for lanes in (1, 2):

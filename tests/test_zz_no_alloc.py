@@ -101,6 +101,65 @@ def test_static_batch_rejects_a_capturing_stream(femtc, dev):
     assert femtc.device_status() == 0
 
 
+def test_static_batch_while_another_thread_captures(femtc, dev):
+    """The case the entry exists for: another thread captures a CUDA graph in
+    global mode (cudaMalloc is then refused everywhere in the process) while
+    this thread calls the entry on its own stream.  The call succeeds, the
+    capture ends cleanly, and the results match the graph-built batch."""
+    import threading
+    import torch
+    ms = meshes(femtc, dev, 15, 1)
+    ref_meshes, st_meshes = [], []
+    for m in ms:
+        a, b = list(m), list(m)
+        a[5] = torch.full_like(m[4], float("nan"))
+        b[5] = torch.full_like(m[4], float("nan"))
+        ref_meshes.append(tuple(a))
+        st_meshes.append(tuple(b))
+    batch = femtc.Batch(1, ref_meshes)
+    batch.launch()
+    femtc.batch_apply_static(1, st_meshes)  # first call on the device, outside capture
+    torch.cuda.synchronize()
+    for m in st_meshes:
+        m[5].fill_(float("nan"))
+    st = torch.cuda.Stream(device=dev)
+    x = torch.zeros(1024, device=dev)
+    capturing, called = threading.Event(), threading.Event()
+    errors = []
+
+    def capturer():
+        s = torch.cuda.Stream(device=dev)
+        g = torch.cuda.CUDAGraph()
+        try:
+            with torch.cuda.graph(g, stream=s, capture_error_mode="global"):
+                x.add_(1.0)
+                capturing.set()
+                called.wait(120)
+                x.add_(1.0)
+        except Exception as e:  # an unsafe call elsewhere invalidates the capture
+            errors.append(e)
+        finally:
+            capturing.set()
+
+    th = threading.Thread(target=capturer)
+    th.start()
+    capturing.wait(120)
+    try:
+        femtc.batch_apply_static(1, st_meshes, stream=st)
+    finally:
+        called.set()
+        th.join(120)
+    assert not errors, errors
+    torch.cuda.synchronize()
+    assert femtc.device_status() == 0
+    for r, s_ in zip(ref_meshes, st_meshes):
+        yr = r[5].double().cpu().numpy()
+        ys = s_[5].double().cpu().numpy()
+        assert np.isfinite(ys).all()
+        assert np.abs(ys - yr).max() <= 1e-6 * np.abs(yr).max()
+    batch.close()
+
+
 def test_static_batch_rejects_oversize(femtc, dev):
     import torch
     # more meshes than the static mesh table holds

@@ -55,6 +55,11 @@ struct SplitTraits<SPLIT_F16X2>
   {
     return __half2float(__float2half_rn(x));
   }
+  // the two values of a pack() result (a in the low half), as floats
+  static __device__ __forceinline__ float2 unpack(uint32_t r)
+  {
+    return __half22float2(*reinterpret_cast<const __half2*>(&r));
+  }
   static __device__ __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4],
                                              uint32_t b0, uint32_t b1)
   {
@@ -95,6 +100,12 @@ struct SplitTraits<SPLIT_BF16X3>
   static __device__ __forceinline__ float round(float x)
   {
     return __bfloat162float(__float2bfloat16_rn(x));
+  }
+  // the two values of a pack() result (a in the low half), as floats: a
+  // BF16 value is the high half of its FP32 bit pattern
+  static __device__ __forceinline__ float2 unpack(uint32_t r)
+  {
+    return make_float2(__uint_as_float(r << 16), __uint_as_float(r & 0xffff0000u));
   }
   static __device__ __forceinline__ void mma(float (&d)[4], const uint32_t (&a)[4],
                                              uint32_t b0, uint32_t b1)
@@ -160,25 +171,35 @@ struct AFrag
       s0 = row_scale(m0);
       s1 = row_scale(m1);
 #pragma unroll
-      for (int i = 0; i < NV; ++i)
-        v[i] *= ((i >> 1) & 1) ? s1 : s0;
+      for (int q = 0; q < NR; ++q) // values 2q, 2q+1 share a row
+      {
+        const float2 sv = __fmul2_rn(make_float2(v[2 * q], v[2 * q + 1]),
+                                     make_float2((q & 1) ? s1 : s0, (q & 1) ? s1 : s0));
+        v[2 * q] = sv.x;
+        v[2 * q + 1] = sv.y;
+      }
     }
     inv0 = 1.0f / s0;
     inv1 = 1.0f / s1;
+    // Each term: the pair rounded and packed in one conversion, the packed
+    // values read back, and the remainder v - h formed for both values in
+    // one packed FMA (the same values as rounding and subtracting one at a
+    // time).
 #pragma unroll
     for (int j = 0; j < Tr::terms; ++j)
-    {
-      float h[NV];
-#pragma unroll
-      for (int i = 0; i < NV; ++i)
-      {
-        h[i] = (j + 1 < Tr::terms) ? Tr::round(v[i]) : v[i];
-        v[i] -= h[i];
-      }
 #pragma unroll
       for (int q = 0; q < NR; ++q)
-        r[j][q] = Tr::pack(h[2 * q], h[2 * q + 1]);
-    }
+      {
+        r[j][q] = Tr::pack(v[2 * q], v[2 * q + 1]);
+        if (j + 1 < Tr::terms)
+        {
+          const float2 h = Tr::unpack(r[j][q]);
+          const float2 d = __ffma2_rn(h, make_float2(-1.0f, -1.0f),
+                                      make_float2(v[2 * q], v[2 * q + 1]));
+          v[2 * q] = d.x;
+          v[2 * q + 1] = d.y;
+        }
+      }
   }
 };
 

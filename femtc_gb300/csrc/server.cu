@@ -12,6 +12,7 @@
 
 #include <chrono>
 #include <condition_variable>
+#include <cstdint>
 #include <cstring>
 #include <cuda_runtime.h>
 #include <deque>
@@ -248,8 +249,16 @@ int femtc_server_submit_apply(femtc_server* s, const femtc_apply_request* rq, lo
     return aux_fail(FEMTC_ERR_INVALID, "server: malformed operator application");
   if (femtc_supported(rq->op, rq->dtype, rq->semantics, rq->degree, rq->nquad) != 1)
     return aux_fail(FEMTC_ERR_UNSUPPORTED, "server: operator application: variant not built");
+  {
+    const size_t n = (size_t)rq->degree + 1;
+    const size_t per_cell = storage_bytes(rq->dtype) * (2 * n * n * n + apply_geo_values(*rq));
+    if (rq->ncells > (SIZE_MAX - 3 * 256) / per_cell)
+      return aux_fail(FEMTC_ERR_INVALID, "server: operator application: too many cells");
+  }
   const size_t bytes = apply_bytes(*rq);
-  const size_t ntab = 2 * (size_t)(rq->degree + 1) * (size_t)rq->nquad * storage_bytes(rq->dtype);
+  // mass reads Phi only (Q x N values), stiffness Phi then Gamma
+  const size_t ntab = (rq->op == FEMTC_OP_MASS ? 1 : 2) * (size_t)(rq->degree + 1) *
+                      (size_t)rq->nquad * storage_bytes(rq->dtype);
   femtc_server::Job job{};
   job.rq = femtc_solve_request{};
   job.bytes = bytes;

@@ -49,6 +49,11 @@ def test_server_rejects_bad_applications(femtc):
         with pytest.raises(femtc.FemtcError) as e:
             s.submit_apply(bad)
         assert e.value.status == -1  # FEMTC_ERR_INVALID
+        bad.req.ncells = 1 << 60  # its byte count would overflow size_t
+        with pytest.raises(femtc.FemtcError) as e:
+            s.submit_apply(bad)
+        assert e.value.status == -1  # FEMTC_ERR_INVALID
+        bad.req.ncells = 1
         bad.req.op = 1
         bad.req.dtype = femtc.F16X2
         bad.req.degree = 12

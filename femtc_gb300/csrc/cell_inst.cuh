@@ -31,16 +31,17 @@ void add_variant(std::vector<CellVariant>& v, int dtype)
                           L, EVOD ? 1 : 0});
 }
 
-// Even-odd variants (exact semantics, one lane), N = N0..MAXN, Q = N..N+2.
-template <typename T, int OP, int N, int MAXN>
+// Even-odd variants (exact semantics, L lanes per slab), N = N0..MAXN,
+// Q = N..N+2.
+template <typename T, int OP, int N, int MAXN, int L = 1>
 void add_even_odd(std::vector<CellVariant>& v, int dtype)
 {
   if constexpr (N <= MAXN)
   {
-    add_variant<T, N, N, OP, SEM_EXACT, 1, true>(v, dtype);
-    add_variant<T, N, N + 1, OP, SEM_EXACT, 1, true>(v, dtype);
-    add_variant<T, N, N + 2, OP, SEM_EXACT, 1, true>(v, dtype);
-    add_even_odd<T, OP, N + 1, MAXN>(v, dtype);
+    add_variant<T, N, N, OP, SEM_EXACT, L, true>(v, dtype);
+    add_variant<T, N, N + 1, OP, SEM_EXACT, L, true>(v, dtype);
+    add_variant<T, N, N + 2, OP, SEM_EXACT, L, true>(v, dtype);
+    add_even_odd<T, OP, N + 1, MAXN, L>(v, dtype);
   }
 }
 

@@ -704,7 +704,7 @@ struct SlabTile
   static constexpr bool kAffine = op_affine(OP);
   static_assert(OP != OP_HELMHOLTZ || SEM == SEM_EXACT, "Helmholtz: exact semantics only");
   static_assert(!kAffine || SEM == SEM_EXACT, "affine forms: exact semantics only");
-  static_assert(!EVOD || (SEM == SEM_EXACT && LANES == 1), "even-odd: exact, one lane per slab");
+  static_assert(!EVOD || (SEM == SEM_EXACT && LANES <= 2), "even-odd: exact, one or two lanes per slab");
   // Streaming loop: work split by warps (stream_tiles_warp) where its extra
   // live state costs no occupancy -- FP32 and N <= 4; the register-heavy
   // FP64 and double-float tiles of higher degree keep the CTA-wide loop
@@ -923,6 +923,142 @@ struct SlabTile
     }
   }
 
+  // Even-odd forward with S lanes per slab: lane s takes the column pairs
+  // j = s, s+S, ... (the middle column of odd Q goes to the lane with fewer
+  // pairs).  The lanes' rows of the even-odd tables differ, so each lane
+  // loads its rows into registers once: every multiply-add keeps a register
+  // operand instead of a lane-dependent constant load.
+  static __device__ __forceinline__ void forward_eo2(const TabView<T>& p,
+                                                     const ST* __restrict__ su,
+                                                     T* __restrict__ sw, const Part& w)
+  {
+    using E = EO<Q, N>; // forward tables: Q x N
+    constexpr int JL = (E::M2 + S - 1) / S > 0 ? (E::M2 + S - 1) / S : 1; // pairs per lane
+    constexpr int MIDLANE = E::M2 % S;
+    const T* __restrict__ PF = p.P;
+    const T* __restrict__ DF = p.D;
+    const int bstride = w.ncb * SBC;
+    const int ls = threadIdx.x % S;
+    T tp[JL][N], td[JL][N];
+#pragma unroll
+    for (int jj = 0; jj < JL; ++jj)
+    {
+      const int j = ls + jj * S;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+      {
+        tp[jj][k] = j < E::M2 ? PF[j * N + k] : T(0);
+        td[jj][k] = j < E::M2 ? DF[j * N + k] : T(0);
+      }
+    }
+    for (int ts = w.c0 * N * S + w.tid; ts < w.c1 * N * S; ts += w.nthr)
+    {
+      const int sl = ts / S;
+      const int c = sl / N, i0 = sl - c * N;
+      T x[N2];
+      load_slab(su + sl * US, x);
+      T xe[N][E::K2 > 0 ? E::K2 : 1], xo[N][E::K2 > 0 ? E::K2 : 1];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+#pragma unroll
+        for (int k = 0; k < E::K2; ++k)
+        {
+          xe[i1][k] = x[i1 * N + k] + x[i1 * N + N - 1 - k];
+          xo[i1][k] = x[i1 * N + k] - x[i1 * N + N - 1 - k];
+        }
+      T* b0 = sw + c * SBC + i0 * SQ;
+      T* b1 = b0 + bstride;
+      T* b2 = b1 + bstride;
+      // axis 1 of one column: AA, AG, BA (the same tables in every lane)
+      auto emit = [&](int q2, const T(&a)[N], const T(&g)[N]) {
+        T o[Q];
+        mv_eo<Q, N, 1>(PF, a, o);
+#pragma unroll
+        for (int q1 = 0; q1 < Q; ++q1)
+          b0[q1 * Q + q2] = o[q1];
+        if constexpr (kGrad)
+        {
+          mv_eo<Q, N, -1>(DF, a, o);
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+            b1[q1 * Q + q2] = o[q1];
+          mv_eo<Q, N, 1>(PF, g, o);
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+            b2[q1 * Q + q2] = o[q1];
+        }
+      };
+      // even and odd sums of row i1 against one even-odd table row
+      auto sums = [&](const T(&t)[N], int i1, T& s, T& d) {
+        acc_t<T> sa = acc_mul(t[E::E], xe[i1][0]);
+#pragma unroll
+        for (int k = 1; k < E::K2; ++k)
+          sa = acc_fma(t[E::E + k], xe[i1][k], sa);
+        if constexpr (E::KM)
+          sa = acc_fma(t[E::C], x[i1 * N + E::K2], sa);
+        acc_t<T> da = acc_mul(t[E::O], xo[i1][0]);
+#pragma unroll
+        for (int k = 1; k < E::K2; ++k)
+          da = acc_fma(t[E::O + k], xo[i1][k], da);
+        s = acc_val(sa);
+        d = acc_val(da);
+      };
+#pragma unroll
+      for (int jj = 0; jj < JL; ++jj) // this lane's column pairs (j, Q-1-j)
+      {
+        const int j = ls + jj * S;
+        if (j < E::M2)
+        {
+          T a0[N], a1[N], g0[N], g1[N];
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+          {
+            T s, d;
+            sums(tp[jj], i1, s, d);
+            a0[i1] = s + d;
+            a1[i1] = s - d;
+            if constexpr (kGrad)
+            {
+              sums(td[jj], i1, s, d);
+              g0[i1] = s + d;
+              g1[i1] = d - s;
+            }
+          }
+          emit(j, a0, g0);
+          emit(Q - 1 - j, a1, g1);
+        }
+      }
+      if constexpr (E::MM) // middle column of odd Q
+      {
+        if (ls == MIDLANE)
+        {
+          constexpr int j = E::M2;
+          T a[N], g[N];
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+          {
+            acc_t<T> sa = acc_mul(PF[j * N + E::E], xe[i1][0]);
+#pragma unroll
+            for (int k = 1; k < E::K2; ++k)
+              sa = acc_fma(PF[j * N + E::E + k], xe[i1][k], sa);
+            if constexpr (E::KM)
+              sa = acc_fma(PF[j * N + E::C], x[i1 * N + E::K2], sa);
+            a[i1] = acc_val(sa);
+            if constexpr (kGrad)
+            {
+              acc_t<T> da = acc_mul(DF[j * N + E::O], xo[i1][0]);
+#pragma unroll
+              for (int k = 1; k < E::K2; ++k)
+                da = acc_fma(DF[j * N + E::O + k], xo[i1][k], da);
+              g[i1] = acc_val(da);
+            }
+          }
+          emit(j, a, g);
+        }
+      }
+    }
+  }
+
   static __device__ __forceinline__ void forward(const TabView<T>& p,
                                                  const ST* __restrict__ su,
                                                  T* __restrict__ sw, int ncb)
@@ -934,9 +1070,14 @@ struct SlabTile
                                                  const ST* __restrict__ su,
                                                  T* __restrict__ sw, const Part& w)
   {
-    if constexpr (EVOD)
+    if constexpr (EVOD && S == 1)
     {
       forward_eo(p, su, sw, w);
+      return;
+    }
+    else if constexpr (EVOD)
+    {
+      forward_eo2(p, su, sw, w);
       return;
     }
     const T* __restrict__ P = p.P;
@@ -1312,6 +1453,175 @@ struct SlabTile
     }
   }
 
+  // Even-odd backward with S lanes per slab: lane s accumulates the column
+  // pairs j = s, s+S, ... (the middle column of odd Q goes to the lane with
+  // fewer pairs) with its table entries in registers, then the S lanes sum
+  // their accumulators with shuffles and hold the same output slab.  Every
+  // lane of a warp runs the same number of rounds, so the shuffles see the
+  // whole warp.
+  static __device__ __forceinline__ void backward_eo2(const TabView<T>& p,
+                                                      const T* __restrict__ sw,
+                                                      ST* __restrict__ sy, const Part& w)
+  {
+    using E = EO<N, Q>; // backward tables: N x Q
+    constexpr int JL = (E::K2 + S - 1) / S > 0 ? (E::K2 + S - 1) / S : 1; // pairs per lane
+    constexpr int MIDLANE = E::K2 % S;
+    constexpr int MR = E::M2 > 0 ? E::M2 : 1;
+    const T* __restrict__ PB = p.PB;
+    const T* __restrict__ DB = p.DB;
+    const int bstride = w.ncb * SBC;
+    const int ls = threadIdx.x % S;
+    // this lane's entries of the backward tables for its column pairs
+    T pe[JL][MR], po[JL][MR], de[JL][MR], dq[JL][MR], pm[JL], dm[JL];
+#pragma unroll
+    for (int jj = 0; jj < JL; ++jj)
+    {
+      const int j = ls + jj * S;
+      const bool ok = j < E::K2;
+#pragma unroll
+      for (int i2 = 0; i2 < E::M2; ++i2)
+      {
+        pe[jj][i2] = ok ? PB[i2 * Q + E::E + j] : T(0);
+        po[jj][i2] = ok ? PB[i2 * Q + E::O + j] : T(0);
+        de[jj][i2] = ok ? DB[i2 * Q + E::E + j] : T(0);
+        dq[jj][i2] = ok ? DB[i2 * Q + E::O + j] : T(0);
+      }
+      pm[jj] = (ok && E::MM) ? PB[E::M2 * Q + E::E + j] : T(0);
+      dm[jj] = (ok && E::MM) ? DB[E::M2 * Q + E::O + j] : T(0);
+    }
+    const int base = w.c0 * N * S, cnt = (w.c1 - w.c0) * N * S;
+    const int rounds = (cnt + w.nthr - 1) / w.nthr;
+    for (int r = 0; r < rounds; ++r)
+    {
+      const int idx = r * w.nthr + w.tid;
+      const bool live = idx < cnt;
+      const int sl = live ? (base + idx) / S : w.c0 * N; // idle lanes read a valid slab
+      const int c = sl / N, i0 = sl - c * N;
+      const T* b0 = sw + c * SBC + i0 * SQ;
+      const T* b1 = b0 + bstride;
+      const T* b2 = b1 + bstride;
+      acc_t<T> A[N][MR], B[N][MR], Mid[N];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+      {
+#pragma unroll
+        for (int i2 = 0; i2 < E::M2; ++i2)
+          A[i1][i2] = B[i1][i2] = acc_zero<T>();
+        Mid[i1] = acc_zero<T>();
+      }
+      // axis 1 back of column q2: u1 = Phi^T X (+ Gamma^T Y), u2 = Phi^T Z
+      auto column = [&](int q2, T(&u1)[N], T(&u2)[N]) {
+        T X[Q];
+#pragma unroll
+        for (int q1 = 0; q1 < Q; ++q1)
+          X[q1] = b0[q1 * Q + q2];
+        mv_eo<N, Q, 1>(PB, X, u1);
+        if constexpr (kGrad)
+        {
+          T Y[Q], Z[Q], t[N];
+#pragma unroll
+          for (int q1 = 0; q1 < Q; ++q1)
+          {
+            Y[q1] = b1[q1 * Q + q2];
+            Z[q1] = b2[q1 * Q + q2];
+          }
+          mv_eo<N, Q, -1>(DB, Y, t);
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+            u1[i] += t[i];
+          mv_eo<N, Q, 1>(PB, Z, u2);
+        }
+      };
+#pragma unroll
+      for (int jj = 0; jj < JL; ++jj) // this lane's column pairs (j, Q-1-j)
+      {
+        const int j = ls + jj * S;
+        if (j < E::K2)
+        {
+          T u1a[N], u2a[N], u1b[N], u2b[N];
+          column(j, u1a, u2a);
+          column(Q - 1 - j, u1b, u2b);
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+          {
+            const T e1 = u1a[i1] + u1b[i1], o1 = u1a[i1] - u1b[i1];
+#pragma unroll
+            for (int i2 = 0; i2 < E::M2; ++i2)
+            {
+              A[i1][i2] = acc_fma(pe[jj][i2], e1, A[i1][i2]);
+              B[i1][i2] = acc_fma(po[jj][i2], o1, B[i1][i2]);
+            }
+            if constexpr (E::MM)
+              Mid[i1] = acc_fma(pm[jj], e1, Mid[i1]);
+            if constexpr (kGrad)
+            {
+              const T e2 = u2a[i1] + u2b[i1], o2 = u2a[i1] - u2b[i1];
+#pragma unroll
+              for (int i2 = 0; i2 < E::M2; ++i2)
+              {
+                A[i1][i2] = acc_fma(dq[jj][i2], o2, A[i1][i2]); // d_Gamma
+                B[i1][i2] = acc_fma(de[jj][i2], e2, B[i1][i2]); // s_Gamma
+              }
+              if constexpr (E::MM)
+                Mid[i1] = acc_fma(dm[jj], o2, Mid[i1]);
+            }
+          }
+        }
+      }
+      if constexpr (E::KM) // middle column of odd Q: the C entries
+      {
+        if (ls == MIDLANE)
+        {
+          T u1[N], u2[N];
+          column(E::K2, u1, u2);
+#pragma unroll
+          for (int i1 = 0; i1 < N; ++i1)
+          {
+#pragma unroll
+            for (int i2 = 0; i2 < E::M2; ++i2)
+            {
+              A[i1][i2] = acc_fma(PB[i2 * Q + E::C], u1[i1], A[i1][i2]); // s_Phi
+              if constexpr (kGrad)
+                B[i1][i2] = acc_fma(DB[i2 * Q + E::C], u2[i1], B[i1][i2]); // s_Gamma
+            }
+            if constexpr (E::MM) // Gamma^T vanishes at the centre
+              Mid[i1] = acc_fma(PB[E::M2 * Q + E::C], u1[i1], Mid[i1]);
+          }
+        }
+      }
+      // the S lanes' partial sums, then the output pairs
+      T y[N2];
+#pragma unroll
+      for (int i1 = 0; i1 < N; ++i1)
+      {
+#pragma unroll
+        for (int i2 = 0; i2 < E::M2; ++i2)
+        {
+          T av = acc_val(A[i1][i2]), bv = acc_val(B[i1][i2]);
+#pragma unroll
+          for (int o = 1; o < S; o <<= 1)
+          {
+            av += shfl_xor(av, o);
+            bv += shfl_xor(bv, o);
+          }
+          y[i1 * N + i2] = av + bv;
+          y[i1 * N + N - 1 - i2] = av - bv;
+        }
+        if constexpr (E::MM)
+        {
+          T mv = acc_val(Mid[i1]);
+#pragma unroll
+          for (int o = 1; o < S; o <<= 1)
+            mv += shfl_xor(mv, o);
+          y[i1 * N + E::M2] = mv;
+        }
+      }
+      // the S lanes of a slab hold the same sums: the store is one write
+      if (live)
+        store_slab(sy + sl * US, y);
+    }
+  }
+
   static __device__ __forceinline__ void backward(const TabView<T>& p,
                                                   const T* __restrict__ sw,
                                                   ST* __restrict__ sy, int ncb)
@@ -1323,9 +1633,14 @@ struct SlabTile
                                                   const T* __restrict__ sw,
                                                   ST* __restrict__ sy, const Part& w)
   {
-    if constexpr (EVOD)
+    if constexpr (EVOD && S == 1)
     {
       backward_eo(p, sw, sy, w);
+      return;
+    }
+    else if constexpr (EVOD)
+    {
+      backward_eo2(p, sw, sy, w);
       return;
     }
     const T* __restrict__ P = kAffine ? p.PB : p.P; // affine: weighted tables

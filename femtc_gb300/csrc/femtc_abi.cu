@@ -68,6 +68,7 @@ Registry& registry()
     register_cell_f32eo_stiffness(r.cells, r.faults);
     register_cell_f64eeo_mass(r.cells, r.faults);
     register_cell_f64eeo_stiffness(r.cells, r.faults);
+    register_cell_f64eeo_l2(r.cells, r.faults);
     register_cell_affine_f64_mass(r.cells, r.faults);
     register_cell_affine_f64_stiffness(r.cells, r.faults);
     register_cell_affine_f32_mass(r.cells, r.faults);
@@ -149,9 +150,10 @@ bool symmetric_weights(const S* w, int q)
 const CellVariant& launch_form(const CellVariant& v, const void* tables)
 {
   if (v.eo || !g_even_odd.load(std::memory_order_relaxed) || v.dtype == FEMTC_F16X2 ||
-      v.dtype == FEMTC_BF16X3 || v.sem != FEMTC_EXACT || v.lanes != 1)
+      v.dtype == FEMTC_BF16X3 || v.sem != FEMTC_EXACT)
     return v;
-  const CellVariant* t = find_cell(v.op, v.dtype, v.sem, v.n, v.q, 1, 1);
+  // one lane: every even-odd form; two lanes: the double-float ones
+  const CellVariant* t = find_cell(v.op, v.dtype, v.sem, v.n, v.q, v.lanes, 1);
   if (!t)
     return v;
   const int ntab = op_base(v.op) == FEMTC_OP_MASS ? 1 : 2;

@@ -169,8 +169,9 @@ def test_affine_even_odd_selection(femtc):
 
 def test_even_odd_selection(femtc):
     """Host-side choice of the even-odd kernels: FP64 exact with the
-    tabulated (symmetric) tables, not with random tables, not for FP32, not
-    when switched off, not for stiffness N = 8 (the plain form there)."""
+    tabulated (symmetric) tables, not with random tables, not for FP32 with
+    two lanes, double-float with one or two lanes, not when switched off,
+    not for stiffness N = 8 (the plain form there)."""
     t4 = femtc.tabulate(4, 6)[0]
     assert femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, t4)
     assert femtc.even_odd_used(femtc.MASS, femtc.F64, femtc.EXACT, 7, 9, femtc.tabulate(7, 9)[0])
@@ -179,6 +180,13 @@ def test_even_odd_selection(femtc):
     assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F32, femtc.EXACT, 4, 6, t4)
     rnd = np.random.default_rng(0).uniform(-1, 1, t4.size)
     assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, rnd)
+    # double-float with two lanes per slab: the two-lane even-odd twin
+    femtc.set_tile_config(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 4, 6, 12, 0, 256, 2)
+    try:
+        assert femtc.even_odd_used(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 4, 6, t4)
+        assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 4, 6, rnd)
+    finally:
+        femtc.set_tile_config(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 4, 6, 0, 0)
     femtc.set_even_odd(False)
     try:
         assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, t4)

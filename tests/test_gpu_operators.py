@@ -307,6 +307,44 @@ def test_fp64_even_odd_and_plain_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
     assert relerr(y_eo, y_plain) <= 1e-13
 
 
+@pytest.mark.parametrize("lanes", [1, 2])
+@pytest.mark.parametrize("op", [0, 1])
+@pytest.mark.parametrize("P", range(1, 5))
+@pytest.mark.parametrize("dq", [0, 1, 2])
+def test_f64e_even_odd_lanes_vs_plain_and_oracle(femtc, orc, dev, lanes, op, P, dq):
+    """Double-float with one or two lanes per slab: the even-odd kernels (the
+    default for tabulated tables; with two lanes the column pairs are split
+    between the lanes and their sums combined by shuffles, including the
+    middle column of odd Q) against the plain kernels and the oracle, on a
+    ragged cell count and on several tile shapes of both streaming loops."""
+    from femtc_gb300 import workloads as W
+    Q = P + 1 + dq
+    w = W.make_custom("eo2", op, P, Q, 1001, seed=17 * P + dq + 3 * op)
+    ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
+    ran = 0
+    for cb, nt in ((8, 256), (12, 128), (20, 64)):
+        try:
+            femtc.set_tile_config(op, femtc.F64E, femtc.EXACT, P, Q, cb, 0, nt, lanes)
+        except femtc.FemtcError:
+            continue
+        try:
+            assert femtc.even_odd_used(op, femtc.F64E, femtc.EXACT, P, Q, w.tables)
+            y_eo = run_gpu(femtc, dev, op, femtc.F64E, femtc.EXACT, P, Q, w.tables, w.u, w.geo)
+            femtc.set_even_odd(False)
+            try:
+                y_plain = run_gpu(femtc, dev, op, femtc.F64E, femtc.EXACT, P, Q, w.tables, w.u,
+                                  w.geo)
+            finally:
+                femtc.set_even_odd(True)
+        finally:
+            femtc.set_tile_config(op, femtc.F64E, femtc.EXACT, P, Q, 0, 0)
+        assert relerr(y_eo, ref) <= 1e-12
+        assert relerr(y_plain, ref) <= 1e-12
+        assert relerr(y_eo, y_plain) <= 1e-13
+        ran += 1
+    assert ran > 0
+
+
 @pytest.mark.parametrize("op", [0, 1])
 @pytest.mark.parametrize("P", range(1, 5))
 @pytest.mark.parametrize("dq", [0, 1, 2])

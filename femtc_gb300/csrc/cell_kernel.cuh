@@ -925,9 +925,11 @@ struct SlabTile
 
   // Even-odd forward with S lanes per slab: lane s takes the column pairs
   // j = s, s+S, ... (the middle column of odd Q goes to the lane with fewer
-  // pairs).  The lanes' rows of the even-odd tables differ, so each lane
-  // loads its rows into registers once: every multiply-add keeps a register
-  // operand instead of a lane-dependent constant load.
+  // pairs).  The pair loop and the loop over a pair's two columns are not
+  // unrolled: one copy of the (large, double-float) column code serves every
+  // column of a lane, which keeps the kernel within the instruction cache.
+  // A pair's table rows are read from the parameter block at the top of its
+  // iteration.
   static __device__ __forceinline__ void forward_eo2(const TabView<T>& p,
                                                      const ST* __restrict__ su,
                                                      T* __restrict__ sw, const Part& w)
@@ -939,18 +941,6 @@ struct SlabTile
     const T* __restrict__ DF = p.D;
     const int bstride = w.ncb * SBC;
     const int ls = threadIdx.x % S;
-    T tp[JL][N], td[JL][N];
-#pragma unroll
-    for (int jj = 0; jj < JL; ++jj)
-    {
-      const int j = ls + jj * S;
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-      {
-        tp[jj][k] = j < E::M2 ? PF[j * N + k] : T(0);
-        td[jj][k] = j < E::M2 ? DF[j * N + k] : T(0);
-      }
-    }
     for (int ts = w.c0 * N * S + w.tid; ts < w.c1 * N * S; ts += w.nthr)
     {
       const int sl = ts / S;
@@ -1003,29 +993,47 @@ struct SlabTile
         s = acc_val(sa);
         d = acc_val(da);
       };
-#pragma unroll
+#pragma unroll 1
       for (int jj = 0; jj < JL; ++jj) // this lane's column pairs (j, Q-1-j)
       {
         const int j = ls + jj * S;
-        if (j < E::M2)
+        if (j >= E::M2)
+          break;
+        T tp[N], td[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
         {
-          T a0[N], a1[N], g0[N], g1[N];
+          tp[k] = PF[j * N + k];
+          if constexpr (kGrad)
+            td[k] = DF[j * N + k];
+        }
+        T a0[N], a1[N], g0[N], g1[N];
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          T s, d;
+          sums(tp, i1, s, d);
+          a0[i1] = s + d;
+          a1[i1] = s - d;
+          if constexpr (kGrad)
+          {
+            sums(td, i1, s, d);
+            g0[i1] = s + d;
+            g1[i1] = d - s;
+          }
+        }
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) // column j, then column Q-1-j
+        {
+          T a[N], g[N];
 #pragma unroll
           for (int i1 = 0; i1 < N; ++i1)
           {
-            T s, d;
-            sums(tp[jj], i1, s, d);
-            a0[i1] = s + d;
-            a1[i1] = s - d;
+            a[i1] = h ? a1[i1] : a0[i1];
             if constexpr (kGrad)
-            {
-              sums(td[jj], i1, s, d);
-              g0[i1] = s + d;
-              g1[i1] = d - s;
-            }
+              g[i1] = h ? g1[i1] : g0[i1];
           }
-          emit(j, a0, g0);
-          emit(Q - 1 - j, a1, g1);
+          emit(h ? Q - 1 - j : j, a, g);
         }
       }
       if constexpr (E::MM) // middle column of odd Q
@@ -1455,10 +1463,12 @@ struct SlabTile
 
   // Even-odd backward with S lanes per slab: lane s accumulates the column
   // pairs j = s, s+S, ... (the middle column of odd Q goes to the lane with
-  // fewer pairs) with its table entries in registers, then the S lanes sum
-  // their accumulators with shuffles and hold the same output slab.  Every
-  // lane of a warp runs the same number of rounds, so the shuffles see the
-  // whole warp.
+  // fewer pairs), then the S lanes sum their accumulators with shuffles and
+  // hold the same output slab.  Every lane of a warp runs the same number of
+  // rounds, so the shuffles see the whole warp.  As in forward_eo2 the pair
+  // loop and the loop over a pair's two columns are not unrolled (one copy of
+  // the column code), and a pair's table entries are read at the top of its
+  // iteration.
   static __device__ __forceinline__ void backward_eo2(const TabView<T>& p,
                                                       const T* __restrict__ sw,
                                                       ST* __restrict__ sy, const Part& w)
@@ -1471,24 +1481,6 @@ struct SlabTile
     const T* __restrict__ DB = p.DB;
     const int bstride = w.ncb * SBC;
     const int ls = threadIdx.x % S;
-    // this lane's entries of the backward tables for its column pairs
-    T pe[JL][MR], po[JL][MR], de[JL][MR], dq[JL][MR], pm[JL], dm[JL];
-#pragma unroll
-    for (int jj = 0; jj < JL; ++jj)
-    {
-      const int j = ls + jj * S;
-      const bool ok = j < E::K2;
-#pragma unroll
-      for (int i2 = 0; i2 < E::M2; ++i2)
-      {
-        pe[jj][i2] = ok ? PB[i2 * Q + E::E + j] : T(0);
-        po[jj][i2] = ok ? PB[i2 * Q + E::O + j] : T(0);
-        de[jj][i2] = ok ? DB[i2 * Q + E::E + j] : T(0);
-        dq[jj][i2] = ok ? DB[i2 * Q + E::O + j] : T(0);
-      }
-      pm[jj] = (ok && E::MM) ? PB[E::M2 * Q + E::E + j] : T(0);
-      dm[jj] = (ok && E::MM) ? DB[E::M2 * Q + E::O + j] : T(0);
-    }
     const int base = w.c0 * N * S, cnt = (w.c1 - w.c0) * N * S;
     const int rounds = (cnt + w.nthr - 1) / w.nthr;
     for (int r = 0; r < rounds; ++r)
@@ -1532,39 +1524,72 @@ struct SlabTile
           mv_eo<N, Q, 1>(PB, Z, u2);
         }
       };
-#pragma unroll
+#pragma unroll 1
       for (int jj = 0; jj < JL; ++jj) // this lane's column pairs (j, Q-1-j)
       {
         const int j = ls + jj * S;
-        if (j < E::K2)
+        if (j >= E::K2)
+          break;
+        T u1a[N], u2a[N], u1b[N], u2b[N];
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) // column j, then column Q-1-j
         {
-          T u1a[N], u2a[N], u1b[N], u2b[N];
-          column(j, u1a, u2a);
-          column(Q - 1 - j, u1b, u2b);
+          T u1[N], u2[N];
+          column(h ? Q - 1 - j : j, u1, u2);
 #pragma unroll
           for (int i1 = 0; i1 < N; ++i1)
           {
-            const T e1 = u1a[i1] + u1b[i1], o1 = u1a[i1] - u1b[i1];
+            u1b[i1] = u1[i1];
+            u1a[i1] = h ? u1a[i1] : u1[i1];
+            if constexpr (kGrad)
+            {
+              u2b[i1] = u2[i1];
+              u2a[i1] = h ? u2a[i1] : u2[i1];
+            }
+          }
+        }
+        // this pair's entries of the backward tables
+        T pe[MR], po[MR], de[MR], dq[MR], pm = T(0), dm = T(0);
+#pragma unroll
+        for (int i2 = 0; i2 < E::M2; ++i2)
+        {
+          pe[i2] = PB[i2 * Q + E::E + j];
+          po[i2] = PB[i2 * Q + E::O + j];
+          if constexpr (kGrad)
+          {
+            de[i2] = DB[i2 * Q + E::E + j];
+            dq[i2] = DB[i2 * Q + E::O + j];
+          }
+        }
+        if constexpr (E::MM)
+        {
+          pm = PB[E::M2 * Q + E::E + j];
+          if constexpr (kGrad)
+            dm = DB[E::M2 * Q + E::O + j];
+        }
+#pragma unroll
+        for (int i1 = 0; i1 < N; ++i1)
+        {
+          const T e1 = u1a[i1] + u1b[i1], o1 = u1a[i1] - u1b[i1];
+#pragma unroll
+          for (int i2 = 0; i2 < E::M2; ++i2)
+          {
+            A[i1][i2] = acc_fma(pe[i2], e1, A[i1][i2]);
+            B[i1][i2] = acc_fma(po[i2], o1, B[i1][i2]);
+          }
+          if constexpr (E::MM)
+            Mid[i1] = acc_fma(pm, e1, Mid[i1]);
+          if constexpr (kGrad)
+          {
+            const T e2 = u2a[i1] + u2b[i1], o2 = u2a[i1] - u2b[i1];
 #pragma unroll
             for (int i2 = 0; i2 < E::M2; ++i2)
             {
-              A[i1][i2] = acc_fma(pe[jj][i2], e1, A[i1][i2]);
-              B[i1][i2] = acc_fma(po[jj][i2], o1, B[i1][i2]);
+              A[i1][i2] = acc_fma(dq[i2], o2, A[i1][i2]); // d_Gamma
+              B[i1][i2] = acc_fma(de[i2], e2, B[i1][i2]); // s_Gamma
             }
             if constexpr (E::MM)
-              Mid[i1] = acc_fma(pm[jj], e1, Mid[i1]);
-            if constexpr (kGrad)
-            {
-              const T e2 = u2a[i1] + u2b[i1], o2 = u2a[i1] - u2b[i1];
-#pragma unroll
-              for (int i2 = 0; i2 < E::M2; ++i2)
-              {
-                A[i1][i2] = acc_fma(dq[jj][i2], o2, A[i1][i2]); // d_Gamma
-                B[i1][i2] = acc_fma(de[jj][i2], e2, B[i1][i2]); // s_Gamma
-              }
-              if constexpr (E::MM)
-                Mid[i1] = acc_fma(dm[jj], o2, Mid[i1]);
-            }
+              Mid[i1] = acc_fma(dm, o2, Mid[i1]);
           }
         }
       }

@@ -395,6 +395,66 @@ __device__ __forceinline__ void mv_eo(const T* __restrict__ t, const T (&x)[K], 
   }
 }
 
+// mv_eo with the symmetry as a run-time flag (neg: SIG < 0), so that one
+// copy of the code serves Phi and Gamma.  Same results bit for bit: the
+// mirrored output is negated instead of subtracted the other way (IEEE
+// subtraction under round-to-nearest is antisymmetric, and so are the
+// double-float sums built from it); the middle row of odd M takes the even
+// or the odd sum, as in mv_eo.
+template <int M, int K, typename T>
+__device__ __forceinline__ void mv_eo_rt(const T* __restrict__ t, const T (&x)[K], T (&y)[M],
+                                         bool neg)
+{
+  using S = EO<M, K>;
+  T xe[S::K2], xo[S::K2];
+#pragma unroll
+  for (int k = 0; k < S::K2; ++k)
+  {
+    xe[k] = x[k] + x[K - 1 - k];
+    xo[k] = x[k] - x[K - 1 - k];
+  }
+#pragma unroll
+  for (int m = 0; m < S::M2; ++m)
+  {
+    acc_t<T> sa = acc_mul(t[m * K + S::E], xe[0]);
+#pragma unroll
+    for (int k = 1; k < S::K2; ++k)
+      sa = acc_fma(t[m * K + S::E + k], xe[k], sa);
+    if constexpr (S::KM)
+      sa = acc_fma(t[m * K + S::C], x[S::K2], sa);
+    acc_t<T> da = acc_mul(t[m * K + S::O], xo[0]);
+#pragma unroll
+    for (int k = 1; k < S::K2; ++k)
+      da = acc_fma(t[m * K + S::O + k], xo[k], da);
+    const T s = acc_val(sa), d = acc_val(da);
+    y[m] = s + d;
+    const T r = s - d;
+    y[M - 1 - m] = neg ? -r : r;
+  }
+  if constexpr (S::MM)
+  {
+    constexpr int m = S::M2;
+    acc_t<T> a;
+    if (!neg)
+    {
+      a = acc_mul(t[m * K + S::E], xe[0]);
+#pragma unroll
+      for (int k = 1; k < S::K2; ++k)
+        a = acc_fma(t[m * K + S::E + k], xe[k], a);
+      if constexpr (S::KM)
+        a = acc_fma(t[m * K + S::C], x[S::K2], a);
+    }
+    else
+    {
+      a = acc_mul(t[m * K + S::O], xo[0]);
+#pragma unroll
+      for (int k = 1; k < S::K2; ++k)
+        a = acc_fma(t[m * K + S::O + k], xo[k], a);
+    }
+    y[m] = acc_val(a);
+  }
+}
+
 // Host: the even-odd table of an M x K matrix A(m,k) = a[m*sm + k*sk] (see
 // mv_eo), in the arithmetic of S; entries past the used rows are left as
 // they are.
@@ -711,6 +771,11 @@ struct SlabTile
   // (stream_tiles).  The host's tile model (lane_efficiency) follows the
   // same rule.
   static constexpr bool kWarpSplit = sizeof(T) == 4 || N <= 4;
+  // double-float even-odd stiffness: the quadrature-point pass loops over
+  // its three forward and three backward contractions with one copy of the
+  // code (its unrolled double-float form overflows the instruction cache)
+  static constexpr bool kCompactFused =
+      std::is_same<T, df64>::value && EVOD && OP == OP_STIFFNESS && SEM == SEM_EXACT;
   // TMA stages.  The warp-split loop takes any count; a third stage (two
   // tiles in flight ahead of the one computed) measured slower than two:
   // its shared memory costs more occupancy than the deeper prefetch gains.
@@ -1250,29 +1315,58 @@ struct SlabTile
       {
         constexpr int NCG = geo_nc(OP);
         const ST* G = geo + ((geo_cell0 + c) * Q3 + r) * NCG; // unused by affine forms
-        T xa[N], xg[N], fx[Q], fy[Q], fz[Q];
+        T fx[Q], fy[Q], fz[Q];
         T fm[OP == OP_HELMHOLTZ ? Q : 1];
-#pragma unroll
-        for (int k = 0; k < N; ++k)
+        if constexpr (kCompactFused)
         {
-          xa[k] = b0[k * sq];
-          xg[k] = b1[k * sq];
-        }
-        fwd<-1>(D, xa, fx); // d/dx: Gamma on axis 0
-        fwd<1>(P, xg, fy);  // d/dy: Gamma was applied on axis 1
-        if constexpr (OP == OP_HELMHOLTZ)
-          fwd<1>(P, xa, fm); // the value u at the points (mass term)
-        if constexpr (SEM == SEM_EXACT)
-        {
-          T xb[N];
+          // one copy of the contraction for d/dx (Gamma on axis 0, input
+          // b0), d/dy (b1) and d/dz (b2); the outputs rotate into fx, fy, fz
 #pragma unroll
-          for (int k = 0; k < N; ++k)
-            xb[k] = b2[k * sq];
-          fwd<1>(P, xb, fz); // d/dz: Gamma was applied on axis 2
+          for (int q = 0; q < Q; ++q)
+            fy[q] = fz[q] = T(0);
+#pragma unroll 1
+          for (int dir = 0; dir < 3; ++dir)
+          {
+            const T* src = dir == 0 ? b0 : (dir == 1 ? b1 : b2);
+            T x[N], o[Q];
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+              x[k] = src[k * sq];
+            mv_eo_rt<Q, N>(dir == 0 ? D : P, x, o, dir == 0);
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+            {
+              fx[q] = fy[q];
+              fy[q] = fz[q];
+              fz[q] = o[q];
+            }
+          }
         }
         else
         {
-          fwd<1>(P, xa, fz); // reference: W_z carries no derivative
+          T xa[N], xg[N];
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+          {
+            xa[k] = b0[k * sq];
+            xg[k] = b1[k * sq];
+          }
+          fwd<-1>(D, xa, fx); // d/dx: Gamma on axis 0
+          fwd<1>(P, xg, fy);  // d/dy: Gamma was applied on axis 1
+          if constexpr (OP == OP_HELMHOLTZ)
+            fwd<1>(P, xa, fm); // the value u at the points (mass term)
+          if constexpr (SEM == SEM_EXACT)
+          {
+            T xb[N];
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+              xb[k] = b2[k * sq];
+            fwd<1>(P, xb, fz); // d/dz: Gamma was applied on axis 2
+          }
+          else
+          {
+            fwd<1>(P, xa, fz); // reference: W_z carries no derivative
+          }
         }
         // G transform (src/stiffness.hpp:14-29), [zz,yz,xz,yy,xy,xx], read
         // as three 8/16-byte pairs (Helmholtz: a fourth pair holds the mass
@@ -1306,7 +1400,29 @@ struct SlabTile
           fz[q] = xz * w0 + yz * w1 + zz * w2;
         }
         T o[N];
-        if constexpr (SEM == SEM_EXACT)
+        if constexpr (kCompactFused)
+        {
+          // one copy of the contraction for x (Gamma^T, into b0), y (b1)
+          // and z (b2)
+#pragma unroll 1
+          for (int dir = 0; dir < 3; ++dir)
+          {
+            T in[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+            {
+              in[q] = fx[q];
+              fx[q] = fy[q];
+              fy[q] = fz[q];
+            }
+            mv_eo_rt<N, Q>(dir == 0 ? DB : PB, in, o, dir == 0);
+            T* dst = dir == 0 ? b0 : (dir == 1 ? b1 : b2);
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+              dst[k * sq] = o[k];
+          }
+        }
+        else if constexpr (SEM == SEM_EXACT)
         {
           bwd<-1>(DB, fx, o);
           if constexpr (OP == OP_HELMHOLTZ && EVOD)

@@ -69,6 +69,7 @@ Registry& registry()
     register_cell_f64eeo_mass(r.cells, r.faults);
     register_cell_f64eeo_stiffness(r.cells, r.faults);
     register_cell_f64eeo_l2(r.cells, r.faults);
+    register_cell_f64e_p6(r.cells, r.faults);
     register_cell_affine_f64_mass(r.cells, r.faults);
     register_cell_affine_f64_stiffness(r.cells, r.faults);
     register_cell_affine_f32_mass(r.cells, r.faults);
@@ -416,6 +417,11 @@ int check_common(int op, int dtype, int sem, int degree, int nquad,
   if (op_affine(op) && sem != FEMTC_EXACT)
     return fail(FEMTC_ERR_INVALID, "affine forms: exact semantics only");
   const CellVariant* v = find_cell(op, dtype, sem, degree + 1, nquad);
+  // double-float slab kernels above degree 4: the even-odd kernel beats the
+  // general-degree kernel (P=6: 7.99 against 6.35 GDoF/s) but its plain twin
+  // spills, so tables without the symmetry go to the general kernel
+  if (v && v->dtype == FEMTC_F64E && v->n >= 6 && !launch_form(*v, tables).eo)
+    v = nullptr;
   if (!v && !general_supported(op, dtype, sem, degree + 1, nquad))
     return fail(FEMTC_ERR_UNSUPPORTED,
                 "no %s kernel for dtype %d, semantics %d, degree %d, nquad %d",
@@ -1125,9 +1131,12 @@ int femtc_set_tile_config(int op, int dtype, int semantics, int degree,
                           int nquad, int cb, int geo_staged, int threads,
                           int lanes)
 {
-  if (lanes <= 0)
+  const bool dflt = lanes <= 0;
+  if (dflt)
     lanes = default_lanes(op, dtype, degree + 1);
   const CellVariant* v = find_cell(op, dtype, semantics, degree + 1, nquad, lanes);
+  if (!v && dflt) // a variant built with other lanes only
+    v = find_cell(op, dtype, semantics, degree + 1, nquad);
   if (!v)
     return fail(FEMTC_ERR_UNSUPPORTED, "no such kernel variant");
   std::lock_guard<std::mutex> lk(g_cfg_mutex);

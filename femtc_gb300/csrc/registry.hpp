@@ -40,6 +40,7 @@ void register_cell_f32eo_stiffness(std::vector<CellVariant>&, std::vector<FaultR
 void register_cell_f64eeo_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64eeo_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64eeo_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);
+void register_cell_f64e_p6(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_mass(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_stiffness(std::vector<CellVariant>&, std::vector<FaultReader>&);
 void register_cell_f64e_mass_l2(std::vector<CellVariant>&, std::vector<FaultReader>&);

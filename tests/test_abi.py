@@ -180,6 +180,16 @@ def test_even_odd_selection(femtc):
     assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F32, femtc.EXACT, 4, 6, t4)
     rnd = np.random.default_rng(0).uniform(-1, 1, t4.size)
     assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64, femtc.EXACT, 4, 6, rnd)
+    # double-float at degree 6 (Q = 8): the even-odd slab kernel for the
+    # tabulated tables; the general-degree kernel (no even-odd form) for others
+    t6 = femtc.tabulate(6, 8)[0]
+    assert femtc.even_odd_used(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 6, 8, t6)
+    rnd6 = np.random.default_rng(1).uniform(-1, 1, t6.size)
+    assert not femtc.even_odd_used(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 6, 8, rnd6)
+    # built with two lanes only: the built-in lane choice falls back to them
+    femtc.set_tile_config(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 6, 8, 8, 0, 256)
+    assert femtc.get_tile_config(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 6, 8)[3] == 2
+    femtc.set_tile_config(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 6, 8, 0, 0)
     # double-float with two lanes per slab: the two-lane even-odd twin
     femtc.set_tile_config(femtc.STIFFNESS, femtc.F64E, femtc.EXACT, 4, 6, 12, 0, 256, 2)
     try:

@@ -309,15 +309,19 @@ def test_fp64_even_odd_and_plain_vs_oracle(femtc, orc, dev, dtype, op, P, dq):
 
 @pytest.mark.parametrize("lanes", [1, 2])
 @pytest.mark.parametrize("op", [0, 1])
-@pytest.mark.parametrize("P", range(1, 5))
+@pytest.mark.parametrize("P", [1, 2, 3, 4, 6])
 @pytest.mark.parametrize("dq", [0, 1, 2])
 def test_f64e_even_odd_lanes_vs_plain_and_oracle(femtc, orc, dev, lanes, op, P, dq):
     """Double-float with one or two lanes per slab: the even-odd kernels (the
     default for tabulated tables; with two lanes the column pairs are split
     between the lanes and their sums combined by shuffles, including the
     middle column of odd Q) against the plain kernels and the oracle, on a
-    ragged cell count and on several tile shapes of both streaming loops."""
+    ragged cell count and on several tile shapes of both streaming loops.
+    At degree 6 (stiffness, Q = 8, two lanes) the even-odd slab kernel runs
+    against the general-degree kernel, which serves the switched-off case."""
     from femtc_gb300 import workloads as W
+    if P == 6 and (op != 1 or dq != 1 or lanes != 2):
+        pytest.skip("degree 6: the slab kernel is built for stiffness, Q = 8, two lanes")
     Q = P + 1 + dq
     w = W.make_custom("eo2", op, P, Q, 1001, seed=17 * P + dq + 3 * op)
     ref = oracle_apply(orc, op, orc.EXACT, P, Q, w.tables, w.u, w.geo)
